@@ -1,0 +1,71 @@
+// Internal helpers shared by the libarlgpu translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include "../../include/arlgpu.h"
+
+namespace arlgpu {
+
+int fail(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define ARL_CUDA(call)                                                         \
+  do {                                                                         \
+    cudaError_t _e = (call);                                                   \
+    if (_e != cudaSuccess) return ::arlgpu::cuda_fail(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define ARL_LAUNCH_CHECK() ARL_CUDA(cudaGetLastError())
+
+#define ARL_TRY(expr)                 \
+  do {                                \
+    int _s = (expr);                  \
+    if (_s != ARLGPU_OK) return _s;   \
+  } while (0)
+
+template <typename R> struct Cplx;
+template <> struct Cplx<float> { using T = float2; };
+template <> struct Cplx<double> { using T = double2; };
+
+// Per-row result of the uvw -> grid mapping, 16 bytes.
+//   pu, pv : nearest grid pixel (ARL pu_grid / pv_grid)
+//   sub    : pu_off | pv_off << 8 | pwc << 16
+//   cz     : pfreq | pwg << 16
+struct RowMap {
+  int32_t pu, pv;
+  uint32_t sub, cz;
+};
+
+// Geometry handed to the device kernels by value.
+struct Geom {
+  int32_t nchan, npol, nw, ny, nx;     // grid
+  int32_t cf_nchan, cf_npol, nz, O, S; // cf
+  int64_t cf_chan_stride, cf_pol_stride, cf_z_stride;
+  arlgpu_axis gu, gv, gw, gf, cdu, cdv, cz;
+  double rcp_gu, rcp_gv, rcp_gw, rcp_gf, rcp_cdu, rcp_cdv, rcp_cz;
+  const int32_t *plane_support;        // device, may be null
+  // binning
+  int32_t T;       // tile edge (grid pixels)
+  int32_t SG;      // staged subgrid edge = T + S
+  int32_t ntu, ntv;
+  uint32_t nbins;  // nchan * nw * ntv * ntu; key == nbins marks a rejected row
+};
+
+int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precision, Geom *g);
+
+// Workspace carve-up for a plan over nvis rows.
+struct PlanBufs {
+  uint32_t *keys;
+  RowMap *maps;
+  uint32_t *sidx;
+  RowMap *smap;
+  uint32_t *hist;     // nbins + 1
+  uint32_t *offsets;  // nbins + 2
+};
+size_t plan_bytes(int64_t nvis, const Geom &g);
+int plan_carve(void *ws, size_t bytes, int64_t nvis, const Geom &g, PlanBufs *b);
+int plan_build(const double *uvw, const double *freq, int64_t nvis, const Geom &g, const PlanBufs &b,
+               int64_t *n_bad_dev, cudaStream_t st);
+
+}  // namespace arlgpu

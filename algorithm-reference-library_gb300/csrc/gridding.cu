@@ -1,0 +1,769 @@
+// Mapping (K1), tile binning (K2), gridder (K3) and degridder (K4).
+//
+// Reference behaviour: processing_components/griddata/gridding.py
+//   convolution_mapping            :24-96
+//   grid_visibility_to_griddata    :99-133
+//   degrid_visibility_from_griddata:233-267
+//
+// Data flow on the device
+//   k_map      uvw, frequency -> RowMap + bin key per row, histogram of keys
+//   k_scan     exclusive scan of the histogram -> bin offsets
+//   k_scatter  rows -> bin order (sidx = original row id, smap = RowMap)
+//   k_grid     one CTA per chunk of sorted rows; each run of rows of one
+//              (chan, w-plane, uv-tile) bin accumulates into a shared-memory
+//              subgrid (tile + kernel halo) that is flushed to the grid with
+//              one vector atomic per touched cell
+//   k_degrid   same chunking; the bin's subgrid is staged in shared memory and
+//              each row is a warp-wide dot product reduced with shuffles
+#include <cstdarg>
+#include <cstring>
+#include <atomic>
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+
+namespace arlgpu {
+
+static thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+  return fail(ARLGPU_ERR_CUDA, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+
+const char *last_error() { return g_last_error.c_str(); }
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// ---------------------------------------------------------------------------
+// Exact FP64 linear-axis transforms in numpy's operation order.
+//   world2pix0(x) = ((x - crval) / cdelt + crpix) - 1
+//   pix2world0(p) = ((p + 1) - crpix) * cdelt + crval
+// Each operation is rounded on its own (no FMA contraction).  The division is
+// first done as a multiply by the rounded reciprocal; when the result lies
+// within a few ulps of the rounding boundary that decides the integer index
+// (a half-integer for round-half-even, an integer for floor) the exact IEEE
+// division recomputes it, so the index always equals numpy's.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double w2p_tail(double q, const arlgpu_axis &a) {
+  return __dsub_rn(__dadd_rn(q, a.crpix), 1.0);
+}
+__device__ __forceinline__ double w2p_fast(double x, const arlgpu_axis &a, double rcp) {
+  return w2p_tail(__dmul_rn(__dsub_rn(x, a.crval), rcp), a);
+}
+__device__ __forceinline__ double w2p_exact(double x, const arlgpu_axis &a) {
+  return w2p_tail(__ddiv_rn(__dsub_rn(x, a.crval), a.cdelt), a);
+}
+__device__ __forceinline__ double p2w(double p, const arlgpu_axis &a) {
+  return __dadd_rn(__dmul_rn(__dsub_rn(__dadd_rn(p, 1.0), a.crpix), a.cdelt), a.crval);
+}
+__device__ __forceinline__ double near_tol(double p) { return 1e-11 * (1.0 + fabs(p)); }
+
+// numpy.round(world2pix0(x))
+__device__ __forceinline__ double round_w2p(double x, const arlgpu_axis &a, double rcp) {
+  double p = w2p_fast(x, a, rcp);
+  double f = p - floor(p);
+  if (fabs(f - 0.5) < near_tol(p)) p = w2p_exact(x, a);
+  return rint(p);
+}
+// numpy.floor(world2pix0(x))
+__device__ __forceinline__ double floor_w2p(double x, const arlgpu_axis &a, double rcp) {
+  double p = w2p_fast(x, a, rcp);
+  double f = p - rint(p);
+  if (fabs(f) < near_tol(p)) p = w2p_exact(x, a);
+  return floor(p);
+}
+
+struct Mapped {
+  int32_t pu, pv, uf, vf, zg, zc, ch;
+  bool ok;
+};
+
+__device__ __forceinline__ Mapped map_row(double u, double v, double w, double f, const Geom &g) {
+  Mapped m;
+  double pu = round_w2p(u, g.gu, g.rcp_gu);
+  double pv = round_w2p(v, g.gv, g.rcp_gv);
+  double du = __dsub_rn(u, p2w(pu, g.gu));
+  double dv = __dsub_rn(v, p2w(pv, g.gv));
+  double uf = floor_w2p(du, g.cdu, g.rcp_cdu);
+  double vf = floor_w2p(dv, g.cdv, g.rcp_cdv);
+  double zg = round_w2p(w, g.gw, g.rcp_gw);
+  double zc = round_w2p(w, g.cz, g.rcp_cz);
+  double ch = round_w2p(f, g.gf, g.rcp_gf);
+  // Range checks in double so huge values cannot wrap when narrowed.
+  bool ok = pu >= 0.0 && pu < g.nx && pv >= 0.0 && pv < g.ny && uf >= 0.0 && uf < g.O &&
+            vf >= 0.0 && vf < g.O && zg >= 0.0 && zg < g.nw && zc >= 0.0 && zc < g.nz &&
+            ch >= 0.0 && ch < g.nchan && ch < g.cf_nchan;
+  m.pu = ok ? (int32_t)pu : -1;
+  m.pv = ok ? (int32_t)pv : -1;
+  m.uf = ok ? (int32_t)uf : 0;
+  m.vf = ok ? (int32_t)vf : 0;
+  m.zg = ok ? (int32_t)zg : 0;
+  m.zc = ok ? (int32_t)zc : 0;
+  m.ch = ok ? (int32_t)ch : 0;
+  if (ok) {
+    int sz = g.plane_support ? g.plane_support[m.zc] : g.S;
+    int h = sz >> 1;
+    ok = (m.pu - h >= 0) && (m.pu + h <= g.nx) && (m.pv - h >= 0) && (m.pv + h <= g.ny);
+  }
+  m.ok = ok;
+  return m;
+}
+
+__device__ __forceinline__ uint32_t bin_of(int ch, int zg, int pu, int pv, const Geom &g) {
+  return (((uint32_t)ch * g.nw + zg) * g.ntv + pv / g.T) * g.ntu + pu / g.T;
+}
+
+// K1: mapping + bin key + histogram.
+__global__ void k_map(const double *__restrict__ uvw, const double *__restrict__ freq, int64_t nvis,
+                      Geom g, uint32_t *__restrict__ keys, RowMap *__restrict__ maps,
+                      uint32_t *__restrict__ hist) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nvis;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = base + threadIdx.x;
+    uint32_t key = 0xffffffffu;
+    if (r < nvis) {
+      Mapped m = map_row(uvw[3 * r], uvw[3 * r + 1], uvw[3 * r + 2], freq[r], g);
+      RowMap rm;
+      rm.pu = m.pu;
+      rm.pv = m.pv;
+      rm.sub = (uint32_t)m.uf | ((uint32_t)m.vf << 8) | ((uint32_t)m.zc << 16);
+      rm.cz = (uint32_t)m.ch | ((uint32_t)m.zg << 16);
+      key = m.ok ? bin_of(m.ch, m.zg, m.pu, m.pv, g) : g.nbins;
+      maps[r] = rm;
+      keys[r] = key;
+    }
+    // Warp-aggregated histogram increment.
+    unsigned same = __match_any_sync(0xffffffffu, key);
+    if (key != 0xffffffffu && lane == __ffs(same) - 1) atomicAdd(&hist[key], (uint32_t)__popc(same));
+  }
+}
+
+// Exact-mapping export for arlgpu_convolution_mapping.
+__global__ void k_map_export(const double *__restrict__ uvw, const double *__restrict__ freq, int64_t nvis,
+                             Geom g, int32_t *pu, int32_t *puo, int32_t *pv, int32_t *pvo, int32_t *pwg,
+                             int32_t *pwc, int32_t *pf, unsigned long long *nbad) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nvis;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    double u = uvw[3 * r], v = uvw[3 * r + 1], w = uvw[3 * r + 2], f = freq[r];
+    double dpu = round_w2p(u, g.gu, g.rcp_gu);
+    double dpv = round_w2p(v, g.gv, g.rcp_gv);
+    double uf = floor_w2p(__dsub_rn(u, p2w(dpu, g.gu)), g.cdu, g.rcp_cdu);
+    double vf = floor_w2p(__dsub_rn(v, p2w(dpv, g.gv)), g.cdv, g.rcp_cdv);
+    pu[r] = (int32_t)fmax(fmin(dpu, 2e9), -2e9);
+    pv[r] = (int32_t)fmax(fmin(dpv, 2e9), -2e9);
+    puo[r] = (int32_t)fmax(fmin(uf, 2e9), -2e9);
+    pvo[r] = (int32_t)fmax(fmin(vf, 2e9), -2e9);
+    pwg[r] = (int32_t)fmax(fmin(round_w2p(w, g.gw, g.rcp_gw), 2e9), -2e9);
+    pwc[r] = (int32_t)fmax(fmin(round_w2p(w, g.cz, g.rcp_cz), 2e9), -2e9);
+    pf[r] = (int32_t)fmax(fmin(round_w2p(f, g.gf, g.rcp_gf), 2e9), -2e9);
+    Mapped m = map_row(u, v, w, f, g);
+    if (!m.ok) atomicAdd(nbad, 1ull);
+  }
+}
+
+// K2a: exclusive scan of hist[0..n) into off[0..n]; one CTA of 1024 threads.
+__global__ void k_scan(const uint32_t *__restrict__ hist, uint32_t n, uint32_t *__restrict__ off,
+                       int64_t *n_bad_dev, uint32_t nbins) {
+  __shared__ uint32_t part[1024];
+  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  const uint32_t b = threadIdx.x * per;
+  const uint32_t e = min(b + per, n);
+  uint32_t s = 0;
+  for (uint32_t i = b; i < e; ++i) s += hist[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t d = 1; d < blockDim.x; d <<= 1) {
+    uint32_t t = threadIdx.x >= d ? part[threadIdx.x - d] : 0;
+    __syncthreads();
+    part[threadIdx.x] += t;
+    __syncthreads();
+  }
+  uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+  for (uint32_t i = b; i < e; ++i) {
+    off[i] = run;
+    run += hist[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) off[n] = part[blockDim.x - 1];
+  if (threadIdx.x == 0 && n_bad_dev) *n_bad_dev = (int64_t)hist[nbins];
+}
+
+// K2b: scatter rows into bin order (hist reused as zeroed per-bin cursors).
+__global__ void k_scatter(const uint32_t *__restrict__ keys, const RowMap *__restrict__ maps, int64_t nvis,
+                          const uint32_t *__restrict__ off, uint32_t *__restrict__ cursor,
+                          uint32_t *__restrict__ sidx, RowMap *__restrict__ smap) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nvis;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = base + threadIdx.x;
+    uint32_t key = r < nvis ? keys[r] : 0xffffffffu;
+    unsigned same = __match_any_sync(0xffffffffu, key);
+    int leader = __ffs(same) - 1;
+    uint32_t start = 0;
+    if (key != 0xffffffffu && lane == leader) start = atomicAdd(&cursor[key], (uint32_t)__popc(same));
+    start = __shfl_sync(0xffffffffu, start, leader);
+    if (key != 0xffffffffu) {
+      uint32_t pos = off[key] + start + __popc(same & ((1u << lane) - 1u));
+      sidx[pos] = (uint32_t)r;
+      smap[pos] = maps[r];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Complex helpers
+// ---------------------------------------------------------------------------
+template <typename CT> __device__ __forceinline__ CT czero();
+template <> __device__ __forceinline__ float2 czero<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
+
+template <typename CT> __device__ __forceinline__ void red_global(CT *p, CT v);
+template <> __device__ __forceinline__ void red_global<float2>(float2 *p, float2 v) { atomicAdd(p, v); }
+template <> __device__ __forceinline__ void red_global<double2>(double2 *p, double2 v) {
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+
+// Shared-memory accumulation of one complex value.  The FP32 variant keeps a
+// compensation term per cell: the atomic returns the value it replaced, so the
+// exact rounding error of that addition (Knuth TwoSum) can be added to a second
+// accumulator; the cell's value is sum + compensation.
+template <typename R> struct SmemAcc;
+template <> struct SmemAcc<float> {
+  static constexpr int kWords = 2;  // float2 sum + float2 compensation per cell
+  __device__ static __forceinline__ void add(float2 *sum, float2 *comp, float2 v) {
+    float o = atomicAdd(&sum->x, v.x);
+    float s = o + v.x, bp = s - o;
+    float e = (o - (s - bp)) + (v.x - bp);
+    atomicAdd(&comp->x, e);
+    o = atomicAdd(&sum->y, v.y);
+    s = o + v.y;
+    bp = s - o;
+    e = (o - (s - bp)) + (v.y - bp);
+    atomicAdd(&comp->y, e);
+  }
+};
+template <> struct SmemAcc<double> {
+  static constexpr int kWords = 1;
+  __device__ static __forceinline__ void add(double2 *sum, double2 *, double2 v) {
+    atomicAdd(&sum->x, v.x);
+    atomicAdd(&sum->y, v.y);
+  }
+};
+
+template <typename R> struct VisT;
+template <> struct VisT<float> { using C = float2; using W = float; };
+template <> struct VisT<double> { using C = double2; using W = double; };
+
+struct SegInfo {
+  uint32_t end;
+  int ch, zg, u0, v0;
+  bool direct;
+};
+
+// Resolve the bin run that starts at sorted position pos inside [.., c1).
+__device__ __forceinline__ SegInfo seg_at(uint32_t pos, uint32_t c1, const RowMap *smap,
+                                          const uint32_t *off, const Geom &g) {
+  SegInfo s;
+  RowMap m = smap[pos];
+  s.ch = m.cz & 0xffff;
+  s.zg = m.cz >> 16;
+  uint32_t key = bin_of(s.ch, s.zg, m.pu, m.pv, g);
+  s.end = min(off[key + 1], c1);
+  s.u0 = (m.pu / g.T) * g.T - (g.S >> 1);
+  s.v0 = (m.pv / g.T) * g.T - (g.S >> 1);
+  // Few rows for a whole subgrid: go straight to global memory.
+  s.direct = (uint64_t)(s.end - pos) * g.S * g.S * 2ull < (uint64_t)g.SG * g.SG;
+  return s;
+}
+
+template <typename R, int NW>
+__global__ void __launch_bounds__(NW * 32)
+k_grid(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
+       const uint32_t *__restrict__ off, uint32_t chunk,
+       const typename VisT<R>::C *__restrict__ vis, const typename VisT<R>::W *__restrict__ wt,
+       const typename Cplx<R>::T *__restrict__ cf, typename Cplx<R>::T *__restrict__ grid,
+       double *__restrict__ sumwt) {
+  using CT = typename Cplx<R>::T;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int SG = g.SG, SG2 = SG * SG, npol = g.npol;
+  CT *sub = reinterpret_cast<CT *>(smraw);
+  CT *comp = sub + (size_t)npol * SG2;  // used by the FP32 variant only
+  const uint32_t nvalid = off[g.nbins];
+  const uint32_t c0 = blockIdx.x * chunk;
+  if (c0 >= nvalid) return;
+  const uint32_t c1 = min(c0 + chunk, nvalid);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int S = g.S, O = g.O;
+  const int64_t plane_elems = (int64_t)g.ny * g.nx;
+
+  uint32_t pos = c0;
+  while (pos < c1) {
+    const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    if (!sg.direct) {
+      for (int k = threadIdx.x; k < npol * SG2 * SmemAcc<R>::kWords; k += blockDim.x) sub[k] = czero<CT>();
+      __syncthreads();
+    }
+    double wsum[4] = {0.0, 0.0, 0.0, 0.0};
+    for (uint32_t r = pos + warp; r < sg.end; r += NW) {
+      const RowMap m = smap[r];
+      const uint32_t idx = sidx[r];
+      const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+      const int sz = g.plane_support ? g.plane_support[zc] : S;
+      const int toff = (S - sz) >> 1;
+      const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);  // window origin, grid pixels
+      CT vw[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        if (p < npol) {
+          CT v = vis[(size_t)idx * npol + p];
+          R w = wt[(size_t)idx * npol + p];
+          vw[p].x = v.x * w;
+          vw[p].y = v.y * w;
+          if (lane == 0) wsum[p] += (double)w;
+        }
+      }
+      const CT *cfr = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                      ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+      const int n = sz * sz, q = 32 / sz, rr = 32 - q * sz;
+      int j = lane / sz, i = lane - j * sz;
+      for (int t = lane; t < n; t += 32) {
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          if (p < npol) {
+            CT tp = cfr[p * g.cf_pol_stride + j * S + i];
+            CT c;  // conj(tap) * vw
+            c.x = tp.x * vw[p].x + tp.y * vw[p].y;
+            c.y = tp.x * vw[p].y - tp.y * vw[p].x;
+            if (sg.direct) {
+              red_global<CT>(grid + ((int64_t)(sg.ch * npol + p) * g.nw + sg.zg) * plane_elems +
+                                 (int64_t)(wv + j) * g.nx + (wu + i),
+                             c);
+            } else {
+              const int cell = p * SG2 + (wv - sg.v0 + j) * SG + (wu - sg.u0 + i);
+              SmemAcc<R>::add(sub + cell, comp + cell, c);
+            }
+          }
+        }
+        i += rr;
+        j += q;
+        if (i >= sz) {
+          i -= sz;
+          ++j;
+        }
+      }
+    }
+    // Per-segment weight sums: all rows of a segment share one channel.
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      if (p < npol) {
+        double s = wsum[p];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0 && s != 0.0) atomicAdd(&sumwt[sg.ch * npol + p], s);
+      }
+    }
+    if (!sg.direct) {
+      __syncthreads();
+      for (int k = threadIdx.x; k < npol * SG2; k += blockDim.x) {
+        CT val = sub[k];
+        if (SmemAcc<R>::kWords == 2) {
+          CT e = comp[k];
+          val.x += e.x;
+          val.y += e.y;
+        }
+        if (val.x == (R)0 && val.y == (R)0) continue;
+        const int p = k / SG2, rem = k - p * SG2, y = rem / SG, x = rem - y * SG;
+        const int gy = sg.v0 + y, gx = sg.u0 + x;
+        if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
+        red_global<CT>(grid + ((int64_t)(sg.ch * npol + p) * g.nw + sg.zg) * plane_elems +
+                           (int64_t)gy * g.nx + gx,
+                       val);
+      }
+      __syncthreads();
+    }
+    pos = sg.end;
+  }
+}
+
+template <typename R, int NW>
+__global__ void __launch_bounds__(NW * 32)
+k_degrid(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
+         const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
+         const typename Cplx<R>::T *__restrict__ cf, const typename Cplx<R>::T *__restrict__ grid,
+         typename VisT<R>::C *__restrict__ vis_out) {
+  using CT = typename Cplx<R>::T;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int SG = g.SG, SG2 = SG * SG, npol = g.npol;
+  CT *sub = reinterpret_cast<CT *>(smraw);
+  const uint32_t nvalid = off[g.nbins];
+  const uint32_t c0 = blockIdx.x * chunk;
+  if (c0 >= (uint32_t)nvis) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (c0 + chunk > nvalid) {
+    // Rejected rows (sorted after every valid row) are predicted as zero.
+    const uint32_t b = max(c0, nvalid), e = min(c0 + chunk, (uint32_t)nvis);
+    for (uint32_t r = b + threadIdx.x; r < e; r += blockDim.x)
+      for (int p = 0; p < npol; ++p) vis_out[(size_t)sidx[r] * npol + p] = czero<CT>();
+    if (c0 >= nvalid) return;
+  }
+  const uint32_t c1 = min(c0 + chunk, nvalid);
+  const int S = g.S, O = g.O;
+  const int64_t plane_elems = (int64_t)g.ny * g.nx;
+
+  uint32_t pos = c0;
+  while (pos < c1) {
+    const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    const CT *gplane = grid + (int64_t)(sg.ch * npol) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems;
+    if (!sg.direct) {
+      for (int k = threadIdx.x; k < npol * SG2; k += blockDim.x) {
+        const int p = k / SG2, rem = k - p * SG2, y = rem / SG, x = rem - y * SG;
+        const int gy = sg.v0 + y, gx = sg.u0 + x;
+        CT val = czero<CT>();
+        if (gy >= 0 && gy < g.ny && gx >= 0 && gx < g.nx)
+          val = gplane[(int64_t)p * g.nw * plane_elems + (int64_t)gy * g.nx + gx];
+        sub[k] = val;
+      }
+      __syncthreads();
+    }
+    for (uint32_t r = pos + warp; r < sg.end; r += NW) {
+      const RowMap m = smap[r];
+      const uint32_t idx = sidx[r];
+      const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+      const int sz = g.plane_support ? g.plane_support[zc] : S;
+      const int toff = (S - sz) >> 1;
+      const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
+      const CT *cfr = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                      ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+      CT acc[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) acc[p] = czero<CT>();
+      const int n = sz * sz, q = 32 / sz, rr = 32 - q * sz;
+      int j = lane / sz, i = lane - j * sz;
+      for (int t = lane; t < n; t += 32) {
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          if (p < npol) {
+            CT tp = cfr[p * g.cf_pol_stride + j * S + i];
+            CT gv;
+            if (sg.direct)
+              gv = gplane[(int64_t)p * g.nw * plane_elems + (int64_t)(wv + j) * g.nx + (wu + i)];
+            else
+              gv = sub[p * SG2 + (wv - sg.v0 + j) * SG + (wu - sg.u0 + i)];
+            acc[p].x += gv.x * tp.x - gv.y * tp.y;
+            acc[p].y += gv.x * tp.y + gv.y * tp.x;
+          }
+        }
+        i += rr;
+        j += q;
+        if (i >= sz) {
+          i -= sz;
+          ++j;
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        if (p < npol) {
+          R ax = acc[p].x, ay = acc[p].y;
+          for (int o = 16; o > 0; o >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o);
+          }
+          if (lane == p) {
+            CT out;
+            out.x = ax;
+            out.y = ay;
+            vis_out[(size_t)idx * npol + p] = out;
+          }
+        }
+      }
+    }
+    if (!sg.direct) __syncthreads();
+    pos = sg.end;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static double rcp(double x) { return 1.0 / x; }
+
+int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precision, Geom *g) {
+  if (!gd || !cd) return fail(ARLGPU_ERR_INVALID, "null descriptor");
+  if (precision != ARLGPU_FP32C && precision != ARLGPU_FP64)
+    return fail(ARLGPU_ERR_INVALID, "precision must be ARLGPU_FP32C or ARLGPU_FP64");
+  if (gd->nchan < 1 || gd->npol < 1 || gd->nw < 1 || gd->ny < 2 || gd->nx < 2)
+    return fail(ARLGPU_ERR_INVALID, "bad grid shape");
+  if (gd->npol > 4) return fail(ARLGPU_ERR_UNSUPPORTED, "npol > 4");
+  if (cd->npol != gd->npol && !(cd->npol == 1 && cd->pol_stride == 0))
+    return fail(ARLGPU_ERR_INVALID, "cf npol %d != grid npol %d", cd->npol, gd->npol);
+  if (cd->oversampling < 1 || cd->oversampling > 256) return fail(ARLGPU_ERR_UNSUPPORTED, "oversampling must be 1..256");
+  if (cd->support < 2 || (cd->support & 1)) return fail(ARLGPU_ERR_UNSUPPORTED, "support must be even (ARL slices v-S/2:v+S/2)");
+  if (cd->support > 64) return fail(ARLGPU_ERR_UNSUPPORTED, "support > 64");
+  if (cd->nz < 1 || cd->nz > 65535 || gd->nw > 65535 || gd->nchan > 65535)
+    return fail(ARLGPU_ERR_UNSUPPORTED, "nz, nw and nchan must be < 65536");
+  if (gd->ny > (1 << 20) || gd->nx > (1 << 20)) return fail(ARLGPU_ERR_UNSUPPORTED, "grid too large");
+  memset(g, 0, sizeof *g);
+  g->nchan = gd->nchan;
+  g->npol = gd->npol;
+  g->nw = gd->nw;
+  g->ny = gd->ny;
+  g->nx = gd->nx;
+  g->cf_nchan = cd->nchan;
+  g->cf_npol = cd->npol;
+  g->nz = cd->nz;
+  g->O = cd->oversampling;
+  g->S = cd->support;
+  g->cf_chan_stride = cd->chan_stride;
+  g->cf_pol_stride = cd->pol_stride;
+  g->cf_z_stride = (int64_t)cd->oversampling * cd->oversampling * cd->support * cd->support;
+  g->gu = gd->u;
+  g->gv = gd->v;
+  g->gw = gd->w;
+  g->gf = gd->f;
+  g->cdu = cd->du;
+  g->cdv = cd->dv;
+  g->cz = cd->z;
+  g->rcp_gu = rcp(gd->u.cdelt);
+  g->rcp_gv = rcp(gd->v.cdelt);
+  g->rcp_gw = rcp(gd->w.cdelt);
+  g->rcp_gf = rcp(gd->f.cdelt);
+  g->rcp_cdu = rcp(cd->du.cdelt);
+  g->rcp_cdv = rcp(cd->dv.cdelt);
+  g->rcp_cz = rcp(cd->z.cdelt);
+  g->plane_support = cd->plane_support;
+  // Subgrid edge: 64 cells when npol planes of it (with the FP32 compensation
+  // words) fit in 64 KiB of shared memory, else 32.
+  const size_t cell = precision == ARLGPU_FP64 ? 16 : 16;  // c128, or c64 sum + c64 comp
+  int SG = 64;
+  if ((size_t)g->npol * SG * SG * cell > 64 * 1024) SG = 32;
+  if (SG - g->S < 8) SG = ((g->S + 8 + 7) / 8) * 8;
+  g->SG = SG;
+  g->T = SG - g->S;
+  g->ntu = (g->nx + g->T - 1) / g->T;
+  g->ntv = (g->ny + g->T - 1) / g->T;
+  uint64_t nb = (uint64_t)g->nchan * g->nw * g->ntv * g->ntu;
+  if (nb >= 0x7fffffffull) return fail(ARLGPU_ERR_UNSUPPORTED, "too many bins");
+  g->nbins = (uint32_t)nb;
+  return ARLGPU_OK;
+}
+
+static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t plan_bytes(int64_t nvis, const Geom &g) {
+  size_t n = (size_t)nvis;
+  return align_up(n * 4) + align_up(n * sizeof(RowMap)) + align_up(n * 4) + align_up(n * sizeof(RowMap)) +
+         align_up(((size_t)g.nbins + 1) * 4) + align_up(((size_t)g.nbins + 2) * 4);
+}
+
+int plan_carve(void *ws, size_t bytes, int64_t nvis, const Geom &g, PlanBufs *b) {
+  size_t need = plan_bytes(nvis, g);
+  if (!ws || bytes < need)
+    return fail(ARLGPU_ERR_WORKSPACE, "workspace of %zu bytes is smaller than the %zu needed", bytes, need);
+  char *p = static_cast<char *>(ws);
+  size_t n = (size_t)nvis;
+  b->keys = reinterpret_cast<uint32_t *>(p);
+  p += align_up(n * 4);
+  b->maps = reinterpret_cast<RowMap *>(p);
+  p += align_up(n * sizeof(RowMap));
+  b->sidx = reinterpret_cast<uint32_t *>(p);
+  p += align_up(n * 4);
+  b->smap = reinterpret_cast<RowMap *>(p);
+  p += align_up(n * sizeof(RowMap));
+  b->hist = reinterpret_cast<uint32_t *>(p);
+  p += align_up(((size_t)g.nbins + 1) * 4);
+  b->offsets = reinterpret_cast<uint32_t *>(p);
+  return ARLGPU_OK;
+}
+
+static int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+int plan_build(const double *uvw, const double *freq, int64_t nvis, const Geom &g, const PlanBufs &b,
+               int64_t *n_bad_dev, cudaStream_t st) {
+  const uint32_t nh = g.nbins + 1;
+  ARL_CUDA(cudaMemsetAsync(b.hist, 0, (size_t)nh * 4, st));
+  if (nvis > 0) {
+    int blocks = (int)std::min<int64_t>((nvis + 255) / 256, (int64_t)num_sms() * 16);
+    k_map<<<blocks, 256, 0, st>>>(uvw, freq, nvis, g, b.keys, b.maps, b.hist);
+    ARL_LAUNCH_CHECK();
+    count_launch(1);
+  }
+  k_scan<<<1, 1024, 0, st>>>(b.hist, nh, b.offsets, n_bad_dev, g.nbins);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  ARL_CUDA(cudaMemsetAsync(b.hist, 0, (size_t)nh * 4, st));
+  if (nvis > 0) {
+    int blocks = (int)std::min<int64_t>((nvis + 255) / 256, (int64_t)num_sms() * 16);
+    k_scatter<<<blocks, 256, 0, st>>>(b.keys, b.maps, nvis, b.offsets, b.hist, b.sidx, b.smap);
+    ARL_LAUNCH_CHECK();
+    count_launch(1);
+  }
+  return ARLGPU_OK;
+}
+
+static constexpr int kWarps = 8;
+static constexpr uint32_t kChunk = 512;
+
+template <typename R>
+static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const void *vis, const void *wt,
+                       const void *cf, void *grid, double *sumwt, cudaStream_t st) {
+  size_t smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T) * SmemAcc<R>::kWords;
+  auto kern = k_grid<R, kWarps>;
+  ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  unsigned blocks = (unsigned)((nvis + kChunk - 1) / kChunk);
+  if (blocks == 0) return ARLGPU_OK;
+  kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, kChunk,
+                                          static_cast<const typename VisT<R>::C *>(vis),
+                                          static_cast<const typename VisT<R>::W *>(wt),
+                                          static_cast<const typename Cplx<R>::T *>(cf),
+                                          static_cast<typename Cplx<R>::T *>(grid), sumwt);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
+}
+
+template <typename R>
+static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const void *cf, const void *grid,
+                         void *vis_out, cudaStream_t st) {
+  size_t smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T);
+  auto kern = k_degrid<R, kWarps>;
+  ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  unsigned blocks = (unsigned)((nvis + kChunk - 1) / kChunk);
+  if (blocks == 0) return ARLGPU_OK;
+  kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, kChunk, nvis,
+                                          static_cast<const typename Cplx<R>::T *>(cf),
+                                          static_cast<const typename Cplx<R>::T *>(grid),
+                                          static_cast<typename VisT<R>::C *>(vis_out));
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
+}
+
+static int check_rows(int64_t nvis) {
+  if (nvis < 0) return fail(ARLGPU_ERR_INVALID, "nvis < 0");
+  if (nvis >= 0xffffffffll) return fail(ARLGPU_ERR_UNSUPPORTED, "nvis must be < 2^32 per call");
+  return ARLGPU_OK;
+}
+
+}  // namespace arlgpu
+
+using namespace arlgpu;
+
+extern "C" const char *arlgpu_version(void) { return "arlgpu 0.1 (sm_103a)"; }
+extern "C" const char *arlgpu_last_error(void) { return arlgpu::last_error(); }
+
+extern "C" int arlgpu_convolution_mapping(const double *uvw, const double *frequency, int64_t nvis,
+                                          const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int32_t *pu,
+                                          int32_t *pu_off, int32_t *pv, int32_t *pv_off, int32_t *pwg,
+                                          int32_t *pwc, int32_t *pfreq, int64_t *n_bad_host, void *stream) {
+  Geom g;
+  ARL_TRY(make_geom(gd, cd, ARLGPU_FP64, &g));
+  ARL_TRY(check_rows(nvis));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned long long *d_bad = nullptr;
+  ARL_CUDA(cudaMallocAsync(&d_bad, sizeof(unsigned long long), st));
+  ARL_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(unsigned long long), st));
+  if (nvis > 0) {
+    int blocks = (int)std::min<int64_t>((nvis + 255) / 256, (int64_t)num_sms() * 16);
+    k_map_export<<<blocks, 256, 0, st>>>(uvw, frequency, nvis, g, pu, pu_off, pv, pv_off, pwg, pwc, pfreq, d_bad);
+    ARL_LAUNCH_CHECK();
+  }
+  unsigned long long h = 0;
+  ARL_CUDA(cudaMemcpyAsync(&h, d_bad, sizeof h, cudaMemcpyDeviceToHost, st));
+  ARL_CUDA(cudaFreeAsync(d_bad, st));
+  ARL_CUDA(cudaStreamSynchronize(st));
+  if (n_bad_host) *n_bad_host = (int64_t)h;
+  return ARLGPU_OK;
+}
+
+extern "C" int arlgpu_plan_workspace_bytes(int64_t nvis, const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd,
+                                           size_t *bytes_host) {
+  Geom g;
+  ARL_TRY(make_geom(gd, cd, ARLGPU_FP32C, &g));
+  ARL_TRY(check_rows(nvis));
+  if (!bytes_host) return fail(ARLGPU_ERR_INVALID, "null bytes_host");
+  *bytes_host = plan_bytes(nvis, g);
+  return ARLGPU_OK;
+}
+
+extern "C" int arlgpu_plan_build(const double *uvw, const double *frequency, int64_t nvis,
+                                 const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, void *workspace,
+                                 size_t workspace_bytes, int64_t *n_bad_dev, void *stream) {
+  Geom g;
+  ARL_TRY(make_geom(gd, cd, ARLGPU_FP32C, &g));
+  ARL_TRY(check_rows(nvis));
+  if (nvis > 0 && (!uvw || !frequency)) return fail(ARLGPU_ERR_INVALID, "null uvw / frequency");
+  PlanBufs b;
+  ARL_TRY(plan_carve(workspace, workspace_bytes, nvis, g, &b));
+  return plan_build(uvw, frequency, nvis, g, b, n_bad_dev, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int arlgpu_grid_planned(const void *vis, const void *weight, int64_t nvis, int precision, const void *cf,
+                                   const arlgpu_cf_desc *cd, void *grid, const arlgpu_grid_desc *gd, double *sumwt,
+                                   const void *workspace, size_t workspace_bytes, void *stream) {
+  Geom g;
+  ARL_TRY(make_geom(gd, cd, precision, &g));
+  ARL_TRY(check_rows(nvis));
+  if (!grid || !sumwt || !cf || (nvis > 0 && (!vis || !weight))) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  PlanBufs b;
+  ARL_TRY(plan_carve(const_cast<void *>(workspace), workspace_bytes, nvis, g, &b));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t csz = precision == ARLGPU_FP64 ? 16 : 8;
+  ARL_CUDA(cudaMemsetAsync(grid, 0, (size_t)g.nchan * g.npol * g.nw * g.ny * g.nx * csz, st));
+  ARL_CUDA(cudaMemsetAsync(sumwt, 0, (size_t)g.nchan * g.npol * sizeof(double), st));
+  if (precision == ARLGPU_FP64) return launch_grid<double>(g, b, nvis, vis, weight, cf, grid, sumwt, st);
+  return launch_grid<float>(g, b, nvis, vis, weight, cf, grid, sumwt, st);
+}
+
+extern "C" int arlgpu_degrid_planned(int64_t nvis, int precision, const void *cf, const arlgpu_cf_desc *cd,
+                                     const void *grid, const arlgpu_grid_desc *gd, void *vis_out,
+                                     const void *workspace, size_t workspace_bytes, void *stream) {
+  Geom g;
+  ARL_TRY(make_geom(gd, cd, precision, &g));
+  ARL_TRY(check_rows(nvis));
+  if (!grid || !cf || (nvis > 0 && !vis_out)) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  PlanBufs b;
+  ARL_TRY(plan_carve(const_cast<void *>(workspace), workspace_bytes, nvis, g, &b));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (precision == ARLGPU_FP64) return launch_degrid<double>(g, b, nvis, cf, grid, vis_out, st);
+  return launch_degrid<float>(g, b, nvis, cf, grid, vis_out, st);
+}
+
+extern "C" int arlgpu_grid(const double *uvw, const double *frequency, const void *vis, const void *weight,
+                           int64_t nvis, int precision, const void *cf, const arlgpu_cf_desc *cd, void *grid,
+                           const arlgpu_grid_desc *gd, double *sumwt, int64_t *n_bad_dev, void *workspace,
+                           size_t workspace_bytes, void *stream) {
+  ARL_TRY(arlgpu_plan_build(uvw, frequency, nvis, gd, cd, workspace, workspace_bytes, n_bad_dev, stream));
+  return arlgpu_grid_planned(vis, weight, nvis, precision, cf, cd, grid, gd, sumwt, workspace, workspace_bytes,
+                             stream);
+}
+
+extern "C" int arlgpu_degrid(const double *uvw, const double *frequency, int64_t nvis, int precision,
+                             const void *cf, const arlgpu_cf_desc *cd, const void *grid,
+                             const arlgpu_grid_desc *gd, void *vis_out, int64_t *n_bad_dev, void *workspace,
+                             size_t workspace_bytes, void *stream) {
+  ARL_TRY(arlgpu_plan_build(uvw, frequency, nvis, gd, cd, workspace, workspace_bytes, n_bad_dev, stream));
+  return arlgpu_degrid_planned(nvis, precision, cf, cd, grid, gd, vis_out, workspace, workspace_bytes, stream);
+}
+
+extern "C" unsigned long long arlgpu_kernel_launches(void) { return g_launches.load(); }

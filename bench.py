@@ -1,0 +1,554 @@
+"""Benchmark of ARL's gridding hot path on GB300.
+
+Workload (default, --workload C2): W-projection grid + degrid of the C2
+observation -- 256 antennas in a 5 km-radius disk, 4 channels 100-120 MHz, 120
+times over +/-2 h, 1024 x 1024 x 4-channel grid, cellsize 5e-4 rad, 64 w-planes
+with support growing 8 -> 32 with |w|, oversampling 8, 50 point sources.  Rows
+whose 32 x 32 window would leave the grid are cut (4.34 M of 15.67 M rows stay).
+
+One step = map + bin the rows (FP64), grid them (zeroed grid), degrid them:
+arlgpu_plan_build + arlgpu_grid_planned + arlgpu_degrid_planned on device
+tensors.  `value` = rows / step time (vis/s), FP32C path.  The FP64 path, the
+end-to-end figure through the C ABI with pinned host buffers, the roofline of
+the dominant kernel, clocks and the CPU baseline are reported alongside.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+With --gpus N > 1 (launched by torch.distributed.run) every rank runs its own
+replica of the workload (no data-path collective); value = N * rows / max time.
+"""
+import argparse
+import ctypes
+import importlib
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "vis/s grid+degrid FP32 vs FP64 GPU path at ≤1e-5 rel err; % of HBM roofline"
+L2_FLUSH_BYTES = 256 << 20
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--workload', default='C2')
+    ap.add_argument('--no-fp64', action='store_true', help='skip the FP64 comparison arm')
+    ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline')
+    ap.add_argument('--cpu-seconds', type=float, default=12.0, help='CPU-baseline time budget')
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# Distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+def dist_setup(torch):
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        import torch.distributed as tdist
+        backend = 'nccl' if torch.cuda.is_available() else 'gloo'
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        tdist.init_process_group(backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(torch, world):
+    if world > 1:
+        import torch.distributed as tdist
+        if torch.cuda.is_available():
+            tdist.barrier(device_ids=[torch.cuda.current_device()])
+        else:
+            tdist.barrier()
+
+
+def max_over_ranks(torch, world, x):
+    if world == 1:
+        return x
+    import torch.distributed as tdist
+    t = torch.tensor([x], dtype=torch.float64, device='cuda' if torch.cuda.is_available() else 'cpu')
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# Clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.f = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
+        try:
+            self.p = subprocess.Popen(['nvidia-smi', '-i', str(gpu_index), '--query-gpu=' + self.Q,
+                                       '--format=csv,noheader,nounits', '-lms', '200'],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(mx), 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def measured_hbm():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return float(json.load(f)['hbm_gbs']), 'measured'
+    except (OSError, ValueError, KeyError):
+        return FALLBACK_HBM_GBS, 'fallback'
+
+
+def traffic_per_row(kernel):
+    """DRAM bytes per row of `kernel` from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, 'profiles', 'ncu_dram_per_row.txt')
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == kernel and parts[1] == 'dram_bytes_per_row':
+                return float(parts[2])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# Workload
+# ---------------------------------------------------------------------------
+def build_context(arl, torch, w, precision, device):
+    dv = arl.device
+    im = arl.create_image(npixel=w['npixel'], cellsize=w['cellsize'], frequency=numpy.asarray(w['freqs']),
+                          channel_bandwidth=numpy.array([w['channel_bandwidth']]),
+                          phasecentre=arl.PhaseCentre(0.0, -45.0))
+    if w['kernel'] == 'wproj':
+        gcf, cf = arl.create_awterm_convolutionfunction(im, nw=w['nwplanes'], wstep=w['wstep'],
+                                                        oversampling=w['oversampling'], support=w['support'],
+                                                        plane_support=w['plane_support'])
+    else:
+        gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=w['oversampling'], support=w['support'])
+    gd = dv.grid_desc(arl.kernels._grid_wcs(im, 1, 1e15), (im.nchan, im.npol, 1, w['npixel'], w['npixel']))
+    cf_t, cs, ps, psup = dv.device_cf(cf, precision, device)
+    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup)
+    n = w['uvw'].shape[0]
+    npol = w['npol']
+    ctx = dict(precision=precision, n=n, gd=gd, cd=cd, cf_t=cf_t, psup=psup, im=im, cf=cf, gcf=gcf)
+    ctx['uvw'] = torch.as_tensor(w['uvw'], device=device)
+    ctx['freq'] = torch.as_tensor(w['frequency'], device=device)
+    ctx['vis'] = w['vis'].to(device=device, dtype=dv.CDTYPE[precision]).contiguous()
+    ctx['wt'] = torch.as_tensor(w['weight'], device=device).to(dv.RDTYPE[precision]).contiguous()
+    ctx['grid'] = torch.empty((gd.nchan, gd.npol, gd.nw, gd.ny, gd.nx), dtype=dv.CDTYPE[precision], device=device)
+    ctx['sumwt'] = torch.empty((gd.nchan, gd.npol), dtype=torch.float64, device=device)
+    ctx['out'] = torch.empty((n, npol), dtype=dv.CDTYPE[precision], device=device)
+    ctx['nbad'] = torch.zeros(1, dtype=torch.int64, device=device)
+    nbytes = dv.plan_bytes(n, gd, cd)
+    ctx['ws'] = torch.empty(nbytes, dtype=torch.uint8, device=device)
+    return ctx
+
+
+def run_step(arl, ctx, stream, ev=None):
+    """plan + grid + degrid; ev = (e0, e1, e2, e3) events recorded between stages."""
+    nat = arl._native
+    lib = nat.load()
+    P = nat.PRECISIONS[ctx['precision']]
+    gd, cd, ws = ctx['gd'], ctx['cd'], ctx['ws']
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    if ev:
+        ev[0].record(stream)
+    nat.check(lib.arlgpu_plan_build(nat.ptr(ctx['uvw']), nat.ptr(ctx['freq']), ctx['n'], ctypes.byref(gd),
+                                    ctypes.byref(cd), nat.ptr(ws), ws.numel(), nat.ptr(ctx['nbad']), sp))
+    if ev:
+        ev[1].record(stream)
+    nat.check(lib.arlgpu_grid_planned(nat.ptr(ctx['vis']), nat.ptr(ctx['wt']), ctx['n'], P, nat.ptr(ctx['cf_t']),
+                                      ctypes.byref(cd), nat.ptr(ctx['grid']), ctypes.byref(gd), nat.ptr(ctx['sumwt']),
+                                      nat.ptr(ws), ws.numel(), sp))
+    if ev:
+        ev[2].record(stream)
+    nat.check(lib.arlgpu_degrid_planned(ctx['n'], P, nat.ptr(ctx['cf_t']), ctypes.byref(cd), nat.ptr(ctx['grid']),
+                                        ctypes.byref(gd), nat.ptr(ctx['out']), nat.ptr(ws), ws.numel(), sp))
+    if ev:
+        ev[3].record(stream)
+
+
+def timed_steps(arl, torch, ctx, steps, warmup, world, flush):
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        run_step(arl, ctx, stream)
+    torch.cuda.synchronize()
+    assert int(ctx['nbad'].item()) == 0
+    lib = arl._native.load()
+    launches0 = lib.arlgpu_kernel_launches()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(steps)]
+    barrier(torch, world)
+    torch.cuda.synchronize()
+    for k in range(steps):
+        flush.zero_()                       # L2 flush, outside the timed events
+        run_step(arl, ctx, stream, evs[k])
+    torch.cuda.synchronize()
+    barrier(torch, world)
+    launches = lib.arlgpu_kernel_launches() - launches0
+    plan = [e[0].elapsed_time(e[1]) for e in evs]
+    grid = [e[1].elapsed_time(e[2]) for e in evs]
+    degrid = [e[2].elapsed_time(e[3]) for e in evs]
+    total = sum(e[0].elapsed_time(e[3]) for e in evs)
+    return dict(total_ms=total, plan_ms=sum(plan) / steps, grid_ms=sum(grid) / steps, degrid_ms=sum(degrid) / steps,
+                launches=int(launches))
+
+
+def e2e_steps(arl, torch, ctx, steps, warmup):
+    """Same step through the C ABI from pinned host buffers: H2D of uvw,
+    frequency, vis, weight; D2H of the grid and the degridded vis."""
+    dev = ctx['uvw'].device
+    host = {k: ctx[k].cpu().pin_memory() for k in ('uvw', 'freq', 'vis', 'wt')}
+    gh = torch.empty(ctx['grid'].shape, dtype=ctx['grid'].dtype).pin_memory()
+    oh = torch.empty(ctx['out'].shape, dtype=ctx['out'].dtype).pin_memory()
+    stream = torch.cuda.current_stream()
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = gh.numel() * gh.element_size() + oh.numel() * oh.element_size()
+
+    def one():
+        for k, t in host.items():
+            ctx[k].copy_(t, non_blocking=True)
+        run_step(arl, ctx, stream)
+        gh.copy_(ctx['grid'], non_blocking=True)
+        oh.copy_(ctx['out'], non_blocking=True)
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        one()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    del dev
+    return e0.elapsed_time(e1) / steps, h2d, d2h
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle's reference-faithful per-row loops
+# ---------------------------------------------------------------------------
+_W = {}
+
+
+def _cpu_init(cf, img, nz, wstep, O, S):
+    """Per-process state of the CPU baseline: the kernel table and geometry."""
+    from oracle import arl_oracle as orc
+    _W.update(cf=cf, ccf=numpy.conjugate(cf), gax=orc.grid_axes(img),
+              cax=orc.cf_axes(img, O, S, nz=nz, zstep=wstep))
+    _W['grid'] = numpy.zeros(_W['gax']['shape'], complex)
+    _W['sumwt'] = numpy.zeros(_W['gax']['shape'][:2])
+
+
+def _cpu_worker(args):
+    """Grid then degrid rows with the oracle's per-row loops, each for half of
+    `budget` seconds; returns (rows gridded, s, rows degridded, s)."""
+    uvw, freq, vis, wt, budget = args
+    from oracle import arl_oracle as orc
+    maps = orc.convolution_mapping(uvw, freq, _W['gax'], _W['cax'])
+    n = uvw.shape[0]
+    chunk = 256
+    t0 = time.perf_counter()
+    done_g = 0
+    while done_g < n and time.perf_counter() - t0 < budget / 2:
+        e = min(done_g + chunk, n)
+        orc.grid_loop(vis[done_g:e], wt[done_g:e], tuple(a[done_g:e] for a in maps), _W['cf'], _W['gax']['shape'],
+                      out=(_W['grid'], _W['sumwt']), ccf=_W['ccf'])
+        done_g = e
+    tg = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    done_d = 0
+    while done_d < n and time.perf_counter() - t1 < budget / 2:
+        e = min(done_d + chunk, n)
+        orc.degrid_loop(_W['grid'], tuple(a[done_d:e] for a in maps), _W['cf'])
+        done_d = e
+    td = time.perf_counter() - t1
+    return done_g, tg, done_d, td
+
+
+class CpuBaseline:
+    """The oracle's reference-faithful loops (complex128, per-row, NumPy FFT)
+    on `procs` processes (spawned, so no process inherits a CUDA context)."""
+
+    def __init__(self, w, cf, procs):
+        from oracle import arl_oracle as orc
+        self.w = w
+        self.procs = procs
+        img = orc.image_geometry(w['npixel'], w['cellsize'], len(w['freqs']), w['npol'], w['freqs'][0],
+                                 w['channel_bandwidth'])
+        init = (cf, img, cf.shape[2], float(w.get('wstep', 1e15)), w['oversampling'], w['support'])
+        self.vis = w['vis'].cpu().numpy() if hasattr(w['vis'], 'cpu') else numpy.asarray(w['vis'])
+        self.rng = numpy.random.default_rng(7)
+        if procs == 1:
+            _cpu_init(*init)
+            self.pool = None
+        else:
+            self.pool = mp.get_context('spawn').Pool(procs, initializer=_cpu_init, initargs=init)
+
+    def rate(self, budget, sample_rows):
+        """Summed rows/s over the processes of grid+degrid, 1/(1/r_grid + 1/r_degrid)."""
+        n = self.w['uvw'].shape[0]
+        jobs = []
+        for _ in range(self.procs):
+            sel = numpy.sort(self.rng.choice(n, min(sample_rows, n), replace=False))
+            jobs.append((self.w['uvw'][sel], self.w['frequency'][sel], self.vis[sel], self.w['weight'][sel], budget))
+        res = [_cpu_worker(jobs[0])] if self.pool is None else self.pool.map(_cpu_worker, jobs)
+        rate, rows = 0.0, 0
+        for done_g, tg, done_d, td in res:
+            rate += 1.0 / (tg / done_g + td / done_d)
+            rows += done_g + done_d
+        return rate, rows
+
+    def close(self):
+        if self.pool is not None:
+            self.pool.close()
+            self.pool.join()
+
+
+def cpu_model():
+    try:
+        for line in open('/proc/cpuinfo'):
+            if line.lower().startswith(('model name', 'cpu part')):
+                return line.split(':', 1)[1].strip()
+    except OSError:
+        pass
+    return 'unknown'
+
+
+def oracle_errors(arl, torch, w, cf, ctx, nsub=20000):
+    """Max-norm and RMS error of the GPU grid and degrid (this context's
+    precision) against the complex128 oracle on a seeded row subsample."""
+    from oracle import arl_oracle as orc
+    dv = arl.device
+    rng = numpy.random.default_rng(11)
+    n = w['uvw'].shape[0]
+    sel = numpy.sort(rng.choice(n, min(nsub, n), replace=False))
+    uvw, f = w['uvw'][sel], w['frequency'][sel]
+    vis = w['vis'].cpu().numpy()[sel]
+    wt = w['weight'][sel]
+    img = orc.image_geometry(w['npixel'], w['cellsize'], len(w['freqs']), w['npol'], w['freqs'][0],
+                             w['channel_bandwidth'])
+    gax = orc.grid_axes(img)
+    cax = orc.cf_axes(img, w['oversampling'], w['support'], nz=cf.shape[2], zstep=float(w.get('wstep', 1e15)))
+    maps = orc.convolution_mapping(uvw, f, gax, cax)
+    g_ref, _ = orc.grid_vec(vis, wt, maps, cf, gax['shape'])
+    d_ref = orc.degrid_vec(g_ref, maps, cf)
+    p = ctx['precision']
+    dev = ctx['uvw'].device
+    t_uvw = torch.as_tensor(uvw, device=dev)
+    t_f = torch.as_tensor(f, device=dev)
+    t_v = torch.as_tensor(vis, device=dev).to(dv.CDTYPE[p])
+    t_w = torch.as_tensor(wt, device=dev).to(dv.RDTYPE[p])
+    g, _, _ = dv.grid(t_uvw, t_f, t_v, t_w, ctx['cf_t'], ctx['cd'], ctx['gd'], p)
+    gr = torch.as_tensor(g_ref, device=dev).to(dv.CDTYPE[p])
+    d, _ = dv.degrid(t_uvw, t_f, gr, ctx['cf_t'], ctx['cd'], ctx['gd'], p)
+    g = g.to(torch.complex128).cpu().numpy()
+    d = d.to(torch.complex128).cpu().numpy()
+
+    def err(a, b):
+        return {'max_rel': float(numpy.max(numpy.abs(a - b)) / numpy.max(numpy.abs(b))),
+                'rms_rel': float(numpy.sqrt(numpy.mean(numpy.abs(a - b) ** 2)) / numpy.sqrt(numpy.mean(numpy.abs(b) ** 2)))}
+    return {'rows': int(sel.size), 'grid': err(g, g_ref), 'degrid': err(d, d_ref)}
+
+
+# ---------------------------------------------------------------------------
+# Arms
+# ---------------------------------------------------------------------------
+def workload_label(w):
+    return ('%s W-projection grid+degrid: %d antennas / %.0f km disk, %d chan %.0f-%.0f MHz, %d times, %d^2 grid, '
+            'cell %.0e rad, %d w-planes support %d->%d, O=%d, %d rows after uv-cut of %d' %
+            (w['name'], w['nants'], w['radius'] / 1e3, len(w['freqs']), w['freqs'][0] / 1e6, w['freqs'][-1] / 1e6,
+             w['ntimes'], w['npixel'], w['cellsize'], w.get('nwplanes', 1), w.get('support_min', w['support']),
+             w['support'], w['oversampling'], w['uvw'].shape[0], w['nrows_generated']))
+
+
+def arm_gb300(args, torch, world, rank, local):
+    arl = importlib.import_module('algorithm-reference-library_gb300')
+    sim = importlib.import_module('algorithm-reference-library_gb300.simulation')
+    device = torch.device('cuda', local)
+    w = sim.make_workload(args.workload, device=device)
+    w['name'] = args.workload
+    n = w['uvw'].shape[0]
+    ctx = build_context(arl, torch, w, 'fp32c', device)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+    clocks = Clocks(local)
+    r = timed_steps(arl, torch, ctx, args.steps, args.warmup, world, flush)
+    clk = clocks.stop()
+    t_max = max_over_ranks(torch, world, r['total_ms'])
+    ms = t_max / args.steps
+    value = world * n / (ms / 1e3)
+
+    out = {}
+    if not args.no_fp64:
+        ctx64 = build_context(arl, torch, w, 'fp64', device)
+        r64 = timed_steps(arl, torch, ctx64, max(3, args.steps // 2), 2, world, flush)
+        ms64 = max_over_ranks(torch, world, r64['total_ms']) / max(3, args.steps // 2)
+        g32 = ctx['grid'].to(torch.complex128)
+        run_step(arl, ctx, torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        g32 = ctx['grid'].to(torch.complex128)
+        run_step(arl, ctx64, torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        gerr = float((g32 - ctx64['grid']).abs().max() / ctx64['grid'].abs().max())
+        derr = float((ctx['out'].to(torch.complex128) - ctx64['out']).abs().max() / ctx64['out'].abs().max())
+        out['fp64'] = {'value': world * n / (ms64 / 1e3), 'ms_per_step': ms64, 'plan_ms': r64['plan_ms'],
+                       'grid_ms': r64['grid_ms'], 'degrid_ms': r64['degrid_ms'],
+                       'fp32c_speedup': ms64 / ms,
+                       'fp32c_vs_fp64_max_rel_err': {'grid': gerr, 'degrid': derr}}
+        del ctx64
+        torch.cuda.empty_cache()
+
+    e2e_ms, h2d, d2h = e2e_steps(arl, torch, ctx, max(3, args.steps // 2), 2)
+    e2e_ms = max_over_ranks(torch, world, e2e_ms)
+
+    # Roofline of the dominant kernel (grid or degrid launch), HBM-bound.
+    npol = w['npol']
+    gd = ctx['gd']
+    grid_bytes = 8 * gd.ny * gd.nx * gd.npol * gd.nchan * gd.nw
+    alg = {'grid': n * (20 + 12 * npol) + grid_bytes, 'degrid': n * (20 + 8 * npol) + grid_bytes}
+    kern = 'grid' if r['grid_ms'] >= r['degrid_ms'] else 'degrid'
+    kms = r[kern + '_ms']
+    peak, peak_kind = measured_hbm()
+    achieved = alg[kern] / (kms / 1e3) / 1e9
+    tr = traffic_per_row('k_' + kern)
+    step_alg = n * (24 + 8 * npol + 4 * npol + 4) + grid_bytes + n * (24 + 4 + 8 * npol) + grid_bytes
+    line = {
+        'metric': METRIC, 'value': value, 'unit': 'vis/s', 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded; ARL create_visibility row layout)',
+        'config': {'workload': workload_label(w), 'nvis': n, 'precision': 'fp32c (complex64 storage, compensated FP32)',
+                   'l2': 'flushed between steps (256 MiB write outside the timed events)',
+                   'parallelism': 'replicas' if world > 1 else 'single GPU',
+                   'step': 'plan (FP64 map + tile bin) + grid + degrid'},
+        'breakdown_ms': {'plan': r['plan_ms'], 'grid': r['grid_ms'], 'degrid': r['degrid_ms']},
+        'roofline': {'bound': 'hbm', 'kernel': 'k_' + kern, 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak, 'peak_source': peak_kind + ' (MEASURED_PEAKS.json hbm_gbs)',
+                     'algorithmic_bytes_per_launch': alg[kern],
+                     'traffic': None if tr is None else tr * n},
+        'roofline_step': {'algorithmic_bytes': step_alg, 'achieved_gbs': step_alg / (ms / 1e3) / 1e9,
+                          'frac': step_alg / (ms / 1e3) / 1e9 / peak},
+        'e2e': {'value': world * n / (e2e_ms / 1e3), 'unit': 'vis/s', 'h2d_bytes_per_step': h2d,
+                'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_ms, 'path': 'C ABI, pinned host buffers'},
+        'gpu_launches': r['launches'],
+        'clocks': clk,
+    }
+    line.update(out)
+    if rank == 0:
+        line['err_vs_oracle_fp32c'] = oracle_errors(arl, torch, w, ctx['cf'].data, ctx)
+        if not args.no_cpu:
+            cb = CpuBaseline(w, ctx['cf'].data, 1)
+            rate, rows = cb.rate(args.cpu_seconds, 200000)
+            line['cpu_baseline'] = {'value': rate, 'unit': 'vis/s', 'cores': 1, 'kind': 'port',
+                                    'sample': '%d rows of the workload through the oracle\'s per-row complex128 '
+                                              'grid and degrid loops (%.0f s budget), %s' %
+                                              (rows, args.cpu_seconds, cpu_model())}
+    return line
+
+
+def arm_reference(args, torch, world, rank):
+    """The reference's CPU algorithm (the oracle's faithful per-row loops; the
+    reference itself is Python needing astropy, absent on the box) on all host
+    cores: one process per core, each on its own seeded row sample."""
+    if rank != 0:
+        return None
+    sim = importlib.import_module('algorithm-reference-library_gb300.simulation')
+    from oracle import arl_oracle as orc
+    w = sim.make_workload(args.workload, max_rows=400000)
+    w['name'] = args.workload
+    img = orc.image_geometry(w['npixel'], w['cellsize'], len(w['freqs']), w['npol'], w['freqs'][0],
+                             w['channel_bandwidth'])
+    if w['kernel'] == 'wproj':
+        _, cf = orc.create_awterm_cf(img, nw=w['nwplanes'], wstep=w['wstep'], oversampling=w['oversampling'],
+                                     support=w['support'])
+        cf = orc.crop_cf_planes(cf, w['plane_support'])
+    else:
+        _, cf = orc.create_pswf_cf(len(w['freqs']), w['npol'], w['npixel'], w['npixel'], w['oversampling'],
+                                   w['support'])
+    procs = os.cpu_count() or 1
+    budget = 4.0
+    cb = CpuBaseline(w, cf, procs)
+    for _ in range(args.warmup):
+        cb.rate(1.0, 2000)
+    rates = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rate, rows = cb.rate(budget, 20000)
+        rates.append(rate)
+    wall = time.perf_counter() - t0
+    cb.close()
+    value = statistics.mean(rates)
+    return {'metric': METRIC, 'value': value, 'unit': 'vis/s', 'impl': 'reference', 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': wall / args.steps * 1e3,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'c128',
+            'data': 'synthetic (seeded)',
+            'config': {'workload': workload_label(w), 'nvis_sampled_per_process': 20000},
+            'cpu_baseline': {'value': value, 'unit': 'vis/s', 'cores': procs, 'kind': 'port',
+                             'sample': 'per step, each of %d processes runs the oracle\'s per-row complex128 grid '
+                                       'and degrid loops for %.0f s on its own seeded 20000-row sample; %s' %
+                                       (procs, budget, cpu_model())},
+            'e2e': {'value': value, 'unit': 'vis/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+
+
+def main():
+    args = parse()
+    import torch
+    world, rank, local = dist_setup(torch)
+    if args.impl == 'reference':
+        line = arm_reference(args, torch, world, rank)
+    else:
+        line = arm_gb300(args, torch, world, rank, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

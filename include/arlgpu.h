@@ -1,0 +1,168 @@
+/*
+ * arlgpu.h -- C ABI of libarlgpu.so, the GB300 (sm_103a) implementation of
+ * ARL's convolutional gridding / degridding imaging path.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (ARLGPU_OK = 0).  The message of
+ *     the last failure on the calling thread is available from
+ *     arlgpu_last_error().
+ *   - All array arguments are DEVICE pointers owned by the caller unless a
+ *     parameter name ends in _host.  No entry point keeps a pointer after it
+ *     returns; the library caches only FFT plans.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *     Work is enqueued asynchronously; results are valid once the stream has
+ *     been synchronised.
+ *   - Scratch memory comes from the caller through `workspace` /
+ *     `workspace_bytes`, sized by arlgpu_plan_workspace_bytes().
+ *   - Array layouts are ARL's (row-major, C order):
+ *       uvw        [nvis][3]            float64, wavelengths
+ *       frequency  [nvis]               float64, Hz
+ *       vis        [nvis][npol]         complex (see precision)
+ *       weight     [nvis][npol]         real    (see precision)
+ *       grid       [nchan][npol][nw][ny][nx]          complex
+ *       cf         [nchan][npol][nz][O][O][S][S]      complex (strides below)
+ *       image      [nchan][npol][ny][nx]              float64
+ *   - Precision: ARLGPU_FP32C uses complex64 vis / grid / cf taps and float32
+ *     weights with compensated FP32 accumulation; ARLGPU_FP64 uses complex128 /
+ *     float64 throughout.  uvw -> pixel mapping is FP64 in both.
+ */
+#ifndef ARLGPU_H
+#define ARLGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  ARLGPU_OK = 0,
+  ARLGPU_ERR_INVALID = 1,       /* bad argument (shape, pointer, precision) */
+  ARLGPU_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+  ARLGPU_ERR_OUT_OF_GRID = 3,   /* rows whose kernel window leaves the grid */
+  ARLGPU_ERR_UNSUPPORTED = 4,   /* valid ARL input this build does not handle */
+  ARLGPU_ERR_WORKSPACE = 5,     /* workspace missing or too small */
+  ARLGPU_ERR_CUFFT = 6          /* a cuFFT call failed */
+};
+
+enum { ARLGPU_FP32C = 0, ARLGPU_FP64 = 1 };
+
+/* One linear FITS axis: world = ((pix0 + 1) - crpix) * cdelt + crval. */
+typedef struct {
+  double crval, crpix, cdelt;
+} arlgpu_axis;
+
+/* GridData geometry (ARL GridData: processing_components/griddata/operations.py:91-145). */
+typedef struct {
+  int32_t nchan, npol, nw, ny, nx;
+  arlgpu_axis u, v, w, f;       /* grid_wcs axes UU, VV, WW and FREQ */
+} arlgpu_grid_desc;
+
+/* ConvolutionFunction geometry (convolution_functions.py:62-147).  The table is
+ * [nchan][npol][nz][O][O][S][S]; chan_stride / pol_stride are element strides
+ * between channel / polarisation blocks (0 = the same kernel for all).
+ * plane_support, if not NULL, is a device array of nz even supports <= S: plane
+ * z then uses only the central plane_support[z] x plane_support[z] taps. */
+typedef struct {
+  int32_t nchan, npol, nz, oversampling, support;
+  int64_t chan_stride, pol_stride;
+  arlgpu_axis du, dv, z;        /* cf grid_wcs axes DUU, DVV and WW */
+  const int32_t *plane_support;
+} arlgpu_cf_desc;
+
+/* Library version string and the message of the last failure on this thread. */
+const char *arlgpu_version(void);
+const char *arlgpu_last_error(void);
+
+/* Number of kernels this library has launched in the process (its own kernels,
+ * not cuFFT's), for launch accounting. */
+unsigned long long arlgpu_kernel_launches(void);
+
+/* ---- a1: convolution_mapping (processing_components/griddata/gridding.py:24-96) ----
+ * Writes pu, pu_off, pv, pv_off, pwg, pwc, pfreq (int32 [nvis] each) and the
+ * number of rows whose S x S window, plane or channel falls outside the grid /
+ * cf into *n_bad_host (the rows ARL's asserts reject).  Synchronises `stream`. */
+int arlgpu_convolution_mapping(const double *uvw, const double *frequency, int64_t nvis,
+                               const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd,
+                               int32_t *pu, int32_t *pu_off, int32_t *pv, int32_t *pv_off,
+                               int32_t *pwg, int32_t *pwc, int32_t *pfreq,
+                               int64_t *n_bad_host, void *stream);
+
+/* Scratch bytes needed by arlgpu_grid / arlgpu_degrid for nvis rows. */
+int arlgpu_plan_workspace_bytes(int64_t nvis, const arlgpu_grid_desc *gd,
+                                const arlgpu_cf_desc *cd, size_t *bytes_host);
+
+/* ---- a2: grid_visibility_to_griddata (gridding.py:99-133) ----
+ * grid is zeroed, then grid[c,:,zg,v-S/2:v+S/2,u-S/2:u+S/2] += conj(cf[c,:,zc,dv,du]) * vis*weight;
+ * sumwt [nchan][npol] float64 receives the summed weights.  n_bad_dev (device
+ * int64, may be NULL) receives the count of rejected rows, which are skipped. */
+int arlgpu_grid(const double *uvw, const double *frequency, const void *vis, const void *weight,
+                int64_t nvis, int precision, const void *cf, const arlgpu_cf_desc *cd,
+                void *grid, const arlgpu_grid_desc *gd, double *sumwt, int64_t *n_bad_dev,
+                void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---- Plans: the mapping and tile binning of a set of rows, built once and
+ * shared by the planned gridder and degridder (ARL recomputes the mapping in
+ * each of grid_visibility_to_griddata and degrid_visibility_from_griddata,
+ * gridding.py:113-114,243-244).  The plan lives in `workspace`; the planned
+ * calls must be given the same nvis, gd and cd as arlgpu_plan_build. */
+int arlgpu_plan_build(const double *uvw, const double *frequency, int64_t nvis, const arlgpu_grid_desc *gd,
+                      const arlgpu_cf_desc *cd, void *workspace, size_t workspace_bytes, int64_t *n_bad_dev,
+                      void *stream);
+int arlgpu_grid_planned(const void *vis, const void *weight, int64_t nvis, int precision, const void *cf,
+                        const arlgpu_cf_desc *cd, void *grid, const arlgpu_grid_desc *gd, double *sumwt,
+                        const void *workspace, size_t workspace_bytes, void *stream);
+int arlgpu_degrid_planned(int64_t nvis, int precision, const void *cf, const arlgpu_cf_desc *cd, const void *grid,
+                          const arlgpu_grid_desc *gd, void *vis_out, const void *workspace,
+                          size_t workspace_bytes, void *stream);
+
+/* ---- a3: degrid_visibility_from_griddata (gridding.py:233-267) ----
+ * vis_out[r,p] = sum_ij grid[c,p,zg,v-S/2+j,u-S/2+i] * cf[c,p,zc,dv,du,j,i]; rejected rows get 0. */
+int arlgpu_degrid(const double *uvw, const double *frequency, int64_t nvis, int precision,
+                  const void *cf, const arlgpu_cf_desc *cd, const void *grid,
+                  const arlgpu_grid_desc *gd, void *vis_out, int64_t *n_bad_dev,
+                  void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---- a4: fft_griddata_to_image (gridding.py:270-289) + normalize_sumwt (imaging/base.py:84-101) ----
+ * image = Re/Im[ fftshift(ifft2(ifftshift(sum_w grid))) ] * gcf * nx*ny, divided by
+ * sumwt[c,p] when sumwt != NULL (zero where sumwt <= 0).  image_imag may be NULL.
+ * `fftbuf` is caller scratch of nchan*npol*ny*nx complex elements of the precision;
+ * the grid itself may be passed as fftbuf when nw == 1 and the grid may be destroyed. */
+int arlgpu_fft_grid_to_image(const void *grid, const arlgpu_grid_desc *gd, int precision,
+                             const double *gcf, const double *sumwt, double *image_real,
+                             double *image_imag, void *fftbuf, void *stream);
+
+/* ---- a5: fft_image_to_griddata (gridding.py:292-302) ----
+ * grid[c,p,z] = fftshift(fft2(ifftshift(image * gcf))) for every w-plane z. */
+int arlgpu_fft_image_to_grid(const double *image, const double *gcf, const arlgpu_grid_desc *gd,
+                             int precision, void *grid, void *stream);
+
+/* ---- a7/a8: create_pswf_convolutionfunction (griddata/kernels.py:52-97), FP64 ----
+ * cf_out: [O][O][S][S] complex128 (one plane; ARL broadcasts it over chan/pol);
+ * gcf_out: [ny][nx] float64. */
+int arlgpu_make_pswf(int32_t oversampling, int32_t support, int32_t ny, int32_t nx,
+                     void *cf_out, double *gcf_out, void *stream);
+
+/* ---- a9: create_awterm_convolutionfunction without primary beam, use_aaf=True
+ * (griddata/kernels.py:100-200), FP64 ----
+ * cf_out: [nw][O][O][S][S] complex128; image_nx / cdelt_ra_deg describe the image
+ * template; maxsupport as in ARL (512). */
+int arlgpu_make_wkernels(int32_t nw, double wstep, int32_t oversampling, int32_t support,
+                         int32_t maxsupport, int32_t image_nx, double cdelt_ra_deg,
+                         void *cf_out, void *stream);
+
+/* ---- a17: apply_gaintable, scalar gains (calibration/operations.py:134-137) ----
+ * vis[r,p] *= g[a2[r]] * conj(g[a1[r]])  (inverse: 1/g), complex128 gains [nant]. */
+int arlgpu_apply_gains(void *vis, int64_t nvis, int32_t npol, int precision, const int32_t *a1,
+                       const int32_t *a2, const void *gains, int inverse, void *stream);
+
+/* ---- a13: phaserotate_visibility, tangent plane (visibility/base.py:295-334) ----
+ * vis[r,:] *= exp(+/-2 pi i (u l + v m + w (n - 1))), n = sqrt(1 - l^2 - m^2); inverse selects +. */
+int arlgpu_phaserotate(void *vis, const double *uvw, int64_t nvis, int32_t npol, int precision,
+                       double l, double m, int inverse, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ARLGPU_H */

@@ -1,0 +1,196 @@
+"""Generate golden fixtures by running the reference's own Python code.
+
+Run in a container that has the ARL sources (default ``/root/reference``, or
+``$ARL_REFERENCE``):
+
+    python tests/golden/make_golden.py
+
+The reference cannot be imported unchanged here (no astropy; numpy 2 rejects
+the scalar assignment at ``processing_components/griddata/kernels.py:72``;
+Python 3.12 lacks ``collections.Iterable``).  Three environment shims make it
+importable without touching its sources:
+
+* ``astropy_standin.install()`` supplies a linear-axis WCS (all axes on this
+  path are linear) and inert celestial placeholders;
+* ``kernels.grdsf`` is wrapped so a length-1 input returns scalars (the value
+  is the reference's own ``grdsf``);
+* ``collections.Iterable`` is aliased to ``collections.abc.Iterable``.
+
+Everything else -- mapping, gridding and degridding loops, FFT stages, PSWF
+and w-kernel builders, invert_2d / predict_2d, the w-stack workflow -- is the
+reference's code.  Outputs go to ``tests/golden/*.npz``.
+"""
+import collections
+import collections.abc
+import os
+import sys
+
+import numpy
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get('ARL_REFERENCE', '/root/reference')
+
+sys.path.insert(0, HERE)
+import astropy_standin  # noqa: E402
+
+astropy_standin.install()
+sys.path.insert(0, REF)
+collections.Iterable = collections.abc.Iterable
+
+from data_models.memory_data_models import Visibility  # noqa: E402
+from data_models.polarisation import PolarisationFrame  # noqa: E402
+from processing_library.image.operations import create_image_from_array  # noqa: E402
+import processing_components.griddata.kernels as kernels  # noqa: E402
+from processing_components.griddata import gridding  # noqa: E402
+from processing_components.griddata.operations import create_griddata_from_image  # noqa: E402
+from processing_components.imaging.base import invert_2d, predict_2d  # noqa: E402
+
+_ref_grdsf = kernels.grdsf
+
+
+def _grdsf_scalar(nu):
+    a, b = _ref_grdsf(nu)
+    if numpy.ndim(nu) == 1 and len(nu) == 1:
+        return a[0], b[0]
+    return a, b
+
+
+kernels.grdsf = _grdsf_scalar
+
+WCS = astropy_standin.WCS
+SkyCoord = astropy_standin.SkyCoord
+
+
+def make_image(npixel, cellsize, frequency, channel_bandwidth, polframe):
+    """Template image with the WCS numbers ``create_image`` writes
+    (``processing_library/image/operations.py:31-69``)."""
+    pf = PolarisationFrame(polframe)
+    nchan = len(frequency)
+    w = WCS(naxis=4)
+    w.wcs.cdelt = [-cellsize * 180.0 / numpy.pi, cellsize * 180.0 / numpy.pi, 1.0, channel_bandwidth]
+    w.wcs.crpix = [npixel // 2 + 1, npixel // 2 + 1, 1.0, 1.0]
+    w.wcs.ctype = ["RA---SIN", "DEC--SIN", 'STOKES', 'FREQ']
+    w.wcs.crval = [0.0, -45.0, 1.0, frequency[0]]
+    w.naxis = 4
+    im = create_image_from_array(numpy.zeros([nchan, pf.npol, npixel, npixel]), w, polarisation_frame=pf)
+    return im
+
+
+def make_vis(rng, nvis, npol, umax, wmax, freqs, polframe):
+    uvw = numpy.zeros([nvis, 3])
+    uvw[:, 0] = rng.uniform(-umax, umax, nvis)
+    uvw[:, 1] = rng.uniform(-umax, umax, nvis)
+    uvw[:, 2] = rng.uniform(-wmax, wmax, nvis)
+    f = rng.choice(freqs, nvis)
+    vis = rng.normal(size=(nvis, npol)) + 1j * rng.normal(size=(nvis, npol))
+    wt = rng.uniform(0.5, 2.0, size=(nvis, npol))
+    z = numpy.zeros(nvis)
+    v = Visibility(uvw=uvw, time=z, frequency=f, channel_bandwidth=z + 1e6, vis=vis, weight=wt,
+                   imaging_weight=wt, integration_time=z + 1.0, antenna1=z.astype(int),
+                   antenna2=z.astype(int), polarisation_frame=PolarisationFrame(polframe))
+    v.phasecentre = SkyCoord(0.0, -45.0)
+    return v
+
+
+def case_2d_pswf(out):
+    rng = numpy.random.default_rng(4242)
+    N, cell, O, S = 128, 4e-3, 8, 8
+    im = make_image(N, cell, numpy.array([1e8]), 1e6, 'stokesI')
+    du = abs(1.0 / (N * cell))
+    vis = make_vis(rng, 3000, 1, (N // 2 - S // 2 - 2) * du, 50.0, numpy.array([1e8]), 'stokesI')
+    gcf, cf = kernels.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    gd = create_griddata_from_image(im)
+    maps = gridding.convolution_mapping(vis, gd, cf)
+    gd, sumwt = gridding.grid_visibility_to_griddata(vis, gd, cf)
+    grid = gd.data.copy()
+    img_re, img_im = gridding.fft_griddata_to_image(gd, gcf, imaginary=True)
+    model = numpy.zeros([1, 1, N, N])
+    for _ in range(6):
+        model[0, 0, rng.integers(N // 4, 3 * N // 4), rng.integers(N // 4, 3 * N // 4)] = rng.uniform(0.5, 3)
+    mim = create_image_from_array(model, im.wcs, im.polarisation_frame)
+    gd2 = gridding.fft_image_to_griddata(mim, create_griddata_from_image(im), gcf)
+    grid2 = gd2.data.copy()
+    newvis = gridding.degrid_visibility_from_griddata(vis, gd2, cf)
+    dirty, sumwt2 = invert_2d(vis, im, gcfcf=(gcf, cf))
+    psf, _ = invert_2d(vis, im, dopsf=True, gcfcf=(gcf, cf))
+    pvis = predict_2d(vis, mim, gcfcf=(gcf, cf))
+    numpy.savez_compressed(
+        out, N=N, cell=cell, O=O, S=S, freq0=1e8, dfreq=1e6,
+        uvw=vis.uvw, frequency=vis.frequency, vis=vis.vis, wt=vis.imaging_weight,
+        maps=numpy.stack([numpy.asarray(m) for m in (maps[0], maps[1], maps[2], maps[3], maps[4], maps[6], maps[8])]),
+        cf=cf.data, gcf=gcf.data, grid=grid, sumwt=sumwt, img_re=img_re.data, img_im=img_im.data,
+        model=model, grid_model=grid2, degrid=newvis.vis, dirty=dirty.data, sumwt_dirty=sumwt2,
+        psf=psf.data, predict=pvis.vis)
+
+
+def case_wproj_2chan_2pol(out):
+    rng = numpy.random.default_rng(4343)
+    N, cell, O, S, nw, wstep = 64, 8e-3, 4, 8, 5, 20.0
+    freqs = numpy.array([1.0e8, 1.1e8])
+    im = make_image(N, cell, freqs, 1e7, 'stokesIQ')
+    du = abs(1.0 / (N * cell))
+    vis = make_vis(rng, 1500, 2, (N // 2 - S // 2 - 2) * du, 2.4 * wstep, freqs, 'stokesIQ')
+    gcf, cf = kernels.create_awterm_convolutionfunction(im, nw=nw, wstep=wstep, oversampling=O, support=S,
+                                                        use_aaf=True, maxsupport=64)
+    gd = create_griddata_from_image(im)
+    maps = gridding.convolution_mapping(vis, gd, cf)
+    gd, sumwt = gridding.grid_visibility_to_griddata(vis, gd, cf)
+    grid = gd.data.copy()
+    img_re, img_im = gridding.fft_griddata_to_image(gd, gcf, imaginary=True)
+    rgrid = rng.normal(size=grid.shape) + 1j * rng.normal(size=grid.shape)
+    gd.data[...] = rgrid
+    newvis = gridding.degrid_visibility_from_griddata(vis, gd, cf)
+    numpy.savez_compressed(
+        out, N=N, cell=cell, O=O, S=S, nw=nw, wstep=wstep, freqs=freqs, dfreq=1e7,
+        uvw=vis.uvw, frequency=vis.frequency, vis=vis.vis, wt=vis.imaging_weight,
+        maps=numpy.stack([numpy.asarray(m) for m in (maps[0], maps[1], maps[2], maps[3], maps[4], maps[6], maps[8])]),
+        cf=cf.data, gcf=gcf.data, grid=grid, sumwt=sumwt, img_re=img_re.data, img_im=img_im.data,
+        rgrid=rgrid, degrid=newvis.vis)
+
+
+def case_wstack(out):
+    from workflows.serial.imaging.imaging_serial import invert_list_serial_workflow, \
+        predict_list_serial_workflow
+    rng = numpy.random.default_rng(4444)
+    N, cell, O, S, K = 64, 8e-3, 8, 6, 5
+    im = make_image(N, cell, numpy.array([1e8]), 1e6, 'stokesI')
+    du = abs(1.0 / (N * cell))
+    vis = make_vis(rng, 1200, 1, (N // 2 - S // 2 - 2) * du, 60.0, numpy.array([1e8]), 'stokesI')
+    gcfcf = kernels.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    (dirty, sumwt), = invert_list_serial_workflow([vis], [im], context='wstack', vis_slices=K,
+                                                  gcfcf=[gcfcf])
+    model = numpy.zeros([1, 1, N, N])
+    for _ in range(4):
+        model[0, 0, rng.integers(N // 4, 3 * N // 4), rng.integers(N // 4, 3 * N // 4)] = rng.uniform(0.5, 3)
+    mim = create_image_from_array(model, im.wcs, im.polarisation_frame)
+    (pvis,) = predict_list_serial_workflow([vis], [mim], context='wstack', vis_slices=K, gcfcf=[gcfcf])
+    numpy.savez_compressed(out, N=N, cell=cell, O=O, S=S, K=K, freq0=1e8, dfreq=1e6,
+                           uvw=vis.uvw, frequency=vis.frequency, vis=vis.vis, wt=vis.imaging_weight,
+                           cf=gcfcf[1].data, gcf=gcfcf[0].data, dirty=dirty.data, sumwt=sumwt,
+                           model=model, predict=pvis.vis)
+
+
+def case_kernels(out):
+    """Kernel values of the reference's kernel tests
+    (``tests/processing_components/test_griddata_kernels.py:33-139``) plus a small
+    w-kernel stack with its bounding boxes."""
+    im = make_image(512, 0.0005, numpy.array([1e8]), 1e6, 'stokesI')
+    _, cf8 = kernels.create_pswf_convolutionfunction(im, oversampling=8, support=6)
+    _, cf1 = kernels.create_pswf_convolutionfunction(im, oversampling=1, support=6)
+    gcf, cfw = kernels.create_awterm_convolutionfunction(im, nw=9, wstep=8.0, oversampling=8, support=16,
+                                                         use_aaf=True)
+    from processing_components.griddata.convolution_functions import \
+        calculate_bounding_box_convolutionfunction
+    bb = calculate_bounding_box_convolutionfunction(cfw, 1e-3)
+    numpy.savez_compressed(out, pswf8=cf8.data[0, 0, 0], pswf1=cf1.data[0, 0, 0], gcf=gcf.data[0, 0],
+                           wker=cfw.data[0, 0], bbox=numpy.array([[b[0], *b[1], *b[2]] for b in bb]))
+
+
+if __name__ == '__main__':
+    case_2d_pswf(os.path.join(HERE, 'ref_2d_pswf.npz'))
+    case_wproj_2chan_2pol(os.path.join(HERE, 'ref_wproj_2chan_2pol.npz'))
+    case_wstack(os.path.join(HERE, 'ref_wstack.npz'))
+    case_kernels(os.path.join(HERE, 'ref_kernels.npz'))
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith('.npz'):
+            print(f, os.path.getsize(os.path.join(HERE, f)))

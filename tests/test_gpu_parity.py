@@ -1,0 +1,330 @@
+"""Parity of the CUDA path with the oracle and with the reference's golden
+outputs.  Every call goes through libarlgpu.so (C ABI) via the package.
+
+Tolerances (max-norm error / max-norm of the reference result):
+  FP64 path   1e-12 (grid, degrid, FFT stages, kernels)
+  FP32C path  1e-5  (the ≤1e-5 relative-error target for complex64 storage
+              with compensated FP32 accumulation)
+Integer index work (convolution_mapping) must be bit-identical.
+"""
+import numpy
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+TOL = {'fp64': 1e-12, 'fp32c': 1e-5}
+
+
+def rel(a, b):
+    a = numpy.asarray(a)
+    b = numpy.asarray(b)
+    return float(numpy.max(numpy.abs(a - b)) / max(numpy.max(numpy.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope='module', autouse=True)
+def need_cuda(arl):
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    arl._native.load()
+
+
+def make_image(arl, N, cell, freqs, dfreq, polframe='stokesI'):
+    return arl.create_image(npixel=N, cellsize=cell, frequency=numpy.asarray(freqs, float),
+                            channel_bandwidth=numpy.array([dfreq]), polarisation_frame=arl.PolarisationFrame(polframe),
+                            phasecentre=arl.PhaseCentre(0.0, -45.0))
+
+
+def make_vis(arl, uvw, freq, vis, wt, polframe='stokesI'):
+    v = arl.Visibility(uvw=uvw, frequency=freq, vis=vis, weight=wt, imaging_weight=wt,
+                       polarisation_frame=arl.PolarisationFrame(polframe))
+    v.phasecentre = arl.PhaseCentre(0.0, -45.0)
+    return v
+
+
+# ---------------------------------------------------------------------------
+# Mapping: bit-exact indices
+# ---------------------------------------------------------------------------
+def test_mapping_matches_golden(arl, golden):
+    d = golden('ref_2d_pswf.npz')
+    im = make_image(arl, int(d['N']), float(d['cell']), [1e8], 1e6)
+    gd = arl.create_griddata_from_image(im)
+    _, cf = arl.create_pswf_convolutionfunction(im, oversampling=int(d['O']), support=int(d['S']))
+    vis = make_vis(arl, d['uvw'], d['frequency'], d['vis'], d['wt'])
+    m = arl.convolution_mapping(vis, gd, cf)
+    for got, want in zip((m[0], m[1], m[2], m[3], m[4], m[6], m[8]), d['maps']):
+        assert numpy.array_equal(got, want)
+
+
+def test_mapping_bit_exact_at_rounding_boundaries(arl, oracle):
+    """Rows placed exactly on (and one ulp either side of) the half-pixel and
+    sub-pixel boundaries where round-half-even / floor decide the index."""
+    N, cell, O, S = 512, 1e-3, 8, 8
+    im = make_image(arl, N, cell, [1e8], 1e6)
+    gd = arl.create_griddata_from_image(im)
+    cf = arl.create_convolutionfunction_from_image(im, oversampling=O, support=S)
+    du = gd.grid_wcs.wcs.cdelt[0]
+    rng = numpy.random.default_rng(5)
+    k = rng.integers(-200, 200, 4000).astype(float)
+    base = numpy.concatenate([(k + 0.5) * du, (k + 0.5 + rng.integers(0, O, 4000) / O) * du,
+                              rng.uniform(-200, 200, 4000) * du])
+    u = numpy.concatenate([base, numpy.nextafter(base, numpy.inf), numpy.nextafter(base, -numpy.inf)])
+    n = u.size
+    uvw = numpy.stack([u, u[::-1], rng.uniform(-100, 100, n)], axis=1)
+    freq = numpy.full(n, 1e8)
+    vis = make_vis(arl, uvw, freq, numpy.zeros((n, 1)), numpy.ones((n, 1)))
+    got = arl.convolution_mapping(vis, gd, cf)
+    img = oracle.image_geometry(N, cell)
+    want = oracle.convolution_mapping(uvw, freq, oracle.grid_axes(img), oracle.cf_axes(img, O, S))
+    for g, w in zip((got[0], got[1], got[2], got[3], got[4], got[6], got[8]), want):
+        assert numpy.array_equal(g, w)
+
+
+# ---------------------------------------------------------------------------
+# Grid / degrid / FFT against the reference's golden outputs
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
+def test_golden_2d_pswf(arl, golden, precision):
+    d = golden('ref_2d_pswf.npz')
+    tol = TOL[precision]
+    im = make_image(arl, int(d['N']), float(d['cell']), [1e8], 1e6)
+    gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=int(d['O']), support=int(d['S']))
+    assert rel(cf.data, d['cf']) < 1e-14 and rel(gcf.data, d['gcf']) < 1e-14
+    vis = make_vis(arl, d['uvw'], d['frequency'], d['vis'], d['wt'])
+    gd = arl.create_griddata_from_image(im)
+    gd, sumwt = arl.grid_visibility_to_griddata(vis, gd, cf, precision=precision)
+    assert rel(gd.data, d['grid']) < tol
+    assert rel(sumwt, d['sumwt']) < 1e-12
+    re, imag = arl.fft_griddata_to_image(gd, gcf, imaginary=True, precision=precision)
+    assert rel(re.data, d['img_re']) < tol
+    assert numpy.max(numpy.abs(imag.data - d['img_im'])) < tol * numpy.max(numpy.abs(d['img_re']))
+    mim = arl.create_image_from_array(d['model'], im.wcs, im.polarisation_frame)
+    gd2 = arl.fft_image_to_griddata(mim, arl.create_griddata_from_image(im), gcf, precision=precision)
+    assert rel(gd2.data, d['grid_model']) < tol
+    gm = arl.create_griddata_from_image(im)
+    gm.data[...] = d['grid_model']
+    newvis = arl.degrid_visibility_from_griddata(vis, gm, cf, precision=precision)
+    assert rel(newvis.vis, d['degrid']) < tol
+    dirty, sw = arl.invert_2d(vis, im, gcfcf=(gcf, cf), precision=precision)
+    assert rel(dirty.data, d['dirty']) < tol and rel(sw, d['sumwt_dirty']) < 1e-12
+    psf, _ = arl.invert_2d(vis, im, dopsf=True, gcfcf=(gcf, cf), precision=precision)
+    assert rel(psf.data, d['psf']) < tol
+    pv = arl.predict_2d(vis, mim, gcfcf=(gcf, cf), precision=precision)
+    assert rel(pv.vis, d['predict']) < tol
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
+def test_golden_wproj_2chan_2pol(arl, golden, precision):
+    d = golden('ref_wproj_2chan_2pol.npz')
+    tol = TOL[precision]
+    im = make_image(arl, int(d['N']), float(d['cell']), d['freqs'], float(d['dfreq']), 'stokesIQ')
+    gcf, cf = arl.create_awterm_convolutionfunction(im, nw=int(d['nw']), wstep=float(d['wstep']),
+                                                    oversampling=int(d['O']), support=int(d['S']), maxsupport=64)
+    assert rel(cf.data, d['cf']) < 1e-12 and rel(gcf.data, d['gcf']) < 1e-14
+    vis = make_vis(arl, d['uvw'], d['frequency'], d['vis'], d['wt'], 'stokesIQ')
+    gd = arl.create_griddata_from_image(im)
+    gd, sumwt = arl.grid_visibility_to_griddata(vis, gd, cf, precision=precision)
+    assert rel(gd.data, d['grid']) < tol and rel(sumwt, d['sumwt']) < 1e-12
+    re = arl.fft_griddata_to_image(gd, gcf, precision=precision)
+    assert rel(re.data, d['img_re']) < tol
+    gd.data[...] = d['rgrid']
+    newvis = arl.degrid_visibility_from_griddata(vis, gd, cf, precision=precision)
+    assert rel(newvis.vis, d['degrid']) < tol
+
+
+def test_kernels_match_reference(arl, golden):
+    d = golden('ref_kernels.npz')
+    im = make_image(arl, 512, 0.0005, [1e8], 1e6)
+    _, cf8 = arl.create_pswf_convolutionfunction(im, oversampling=8, support=6)
+    _, cf1 = arl.create_pswf_convolutionfunction(im, oversampling=1, support=6)
+    assert rel(cf8.data[0, 0, 0], d['pswf8']) < 1e-14 and rel(cf1.data[0, 0, 0], d['pswf1']) < 1e-14
+    gcf, cfw = arl.create_awterm_convolutionfunction(im, nw=9, wstep=8.0, oversampling=8, support=16)
+    assert rel(cfw.data[0, 0], d['wker']) < 1e-12 and rel(gcf.data[0, 0], d['gcf']) < 1e-14
+    bb = arl.calculate_bounding_box_convolutionfunction(cfw, 1e-3)
+    assert numpy.array_equal(numpy.array([[b[0], *b[1], *b[2]] for b in bb]), d['bbox'])
+
+
+# ---------------------------------------------------------------------------
+# Oracle parity on cases the fixtures do not cover
+# ---------------------------------------------------------------------------
+def _random_case(arl, oracle, rng, N, cell, O, S, nvis, nchan=1, npol=1, nz=1, zstep=1e15, distinct_chan=False):
+    freqs = 1e8 + 1e7 * numpy.arange(nchan)
+    pf = {1: 'stokesI', 2: 'stokesIQ', 4: 'stokesIQUV'}[npol]
+    im = make_image(arl, N, cell, freqs, 1e7, pf)
+    du = abs(1.0 / (N * cell))
+    lim = (N // 2 - S // 2 - 2) * du
+    uvw = numpy.stack([rng.uniform(-lim, lim, nvis), rng.uniform(-lim, lim, nvis),
+                       rng.uniform(-0.45 * nz * zstep, 0.45 * nz * zstep, nvis) if nz > 1 else
+                       rng.uniform(-50, 50, nvis)], axis=1)
+    freq = rng.choice(freqs, nvis)
+    visd = rng.normal(size=(nvis, npol)) + 1j * rng.normal(size=(nvis, npol))
+    wt = rng.uniform(0.5, 2.0, size=(nvis, npol))
+    cf = arl.create_convolutionfunction_from_image(im, nz=nz, zstep=zstep, oversampling=O, support=S)
+    base = rng.normal(size=(nz, O, O, S, S)) + 1j * rng.normal(size=(nz, O, O, S, S))
+    data = numpy.broadcast_to(base[None, None], cf.data.shape).copy()
+    if distinct_chan:
+        for c in range(nchan):
+            for p in range(npol):
+                data[c, p] *= (1.0 + 0.25 * c) * (1.0 - 0.1 * p)
+    cf.data = data
+    vis = make_vis(arl, uvw, freq, visd, wt, pf)
+    img = oracle.image_geometry(N, cell, nchan, npol, 1e8, 1e7)
+    gax = oracle.grid_axes(img)
+    cax = oracle.cf_axes(img, O, S, nz=nz, zstep=zstep)
+    maps = oracle.convolution_mapping(uvw, freq, gax, cax)
+    return im, cf, vis, maps, gax
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
+@pytest.mark.parametrize('N,O,S,npol,nchan,nz,distinct', [
+    (128, 8, 6, 1, 1, 1, False),      # ARL's default support 6
+    (128, 128, 6, 1, 1, 1, False),    # ARL invert_2d's default oversampling 128
+    (96, 4, 10, 4, 3, 1, True),       # 4 pols, per-channel / per-pol kernels
+    (128, 8, 32, 1, 2, 7, False),     # large w-kernels, several planes
+    (160, 2, 64, 2, 1, 3, False),     # support 64
+])
+def test_grid_degrid_vs_oracle(arl, oracle, precision, N, O, S, npol, nchan, nz, distinct):
+    rng = numpy.random.default_rng(N + O + S + npol)
+    im, cf, vis, maps, gax = _random_case(arl, oracle, rng, N, 4e-3, O, S, 2500, nchan, npol, nz, 20.0, distinct)
+    gd = arl.create_griddata_from_image(im)
+    gd, sumwt = arl.grid_visibility_to_griddata(vis, gd, cf, precision=precision)
+    g_ref, sw_ref = oracle.grid_vec(vis.vis, vis.imaging_weight, maps, cf.data, gax['shape'])
+    assert rel(gd.data, g_ref) < TOL[precision]
+    assert rel(sumwt, sw_ref) < 1e-12
+    rg = rng.normal(size=gax['shape']) + 1j * rng.normal(size=gax['shape'])
+    gd.data[...] = rg
+    out = arl.degrid_visibility_from_griddata(vis, gd, cf, precision=precision)
+    assert rel(out.vis, oracle.degrid_vec(rg, maps, cf.data)) < TOL[precision]
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
+def test_plane_support(arl, oracle, precision):
+    """Plane-dependent support (8 -> 32 with |w|): the GPU skips the cropped taps,
+    the oracle grids with them zeroed."""
+    rng = numpy.random.default_rng(77)
+    N, cell, O, S, nz, zstep = 192, 3e-3, 4, 32, 9, 15.0
+    im = make_image(arl, N, cell, [1e8], 1e7)
+    gcf, cf = arl.create_awterm_convolutionfunction(im, nw=nz, wstep=zstep, oversampling=O, support=S,
+                                                    maxsupport=256)
+    wpl = (numpy.arange(nz) - nz // 2) * zstep
+    arl.set_plane_support(cf, arl.support_schedule(wpl, 8, 32))
+    du = abs(1.0 / (N * cell))
+    lim = (N // 2 - S // 2 - 2) * du
+    n = 3000
+    uvw = numpy.stack([rng.uniform(-lim, lim, n), rng.uniform(-lim, lim, n), rng.uniform(-60, 60, n)], axis=1)
+    freq = numpy.full(n, 1e8)
+    vis = make_vis(arl, uvw, freq, rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1)), numpy.ones((n, 1)))
+    img = oracle.image_geometry(N, cell)
+    gax, cax = oracle.grid_axes(img), oracle.cf_axes(img, O, S, nz=nz, zstep=zstep)
+    maps = oracle.convolution_mapping(uvw, freq, gax, cax)
+    gd, _ = arl.grid_visibility_to_griddata(vis, arl.create_griddata_from_image(im), cf, precision=precision)
+    g_ref, _ = oracle.grid_vec(vis.vis, vis.imaging_weight, maps, cf.data, gax['shape'])
+    assert rel(gd.data, g_ref) < TOL[precision]
+    out = arl.degrid_visibility_from_griddata(vis, gd, cf, precision=precision)
+    assert rel(out.vis, oracle.degrid_vec(g_ref, maps, cf.data)) < TOL[precision]
+
+
+# ---------------------------------------------------------------------------
+# Edge cases and properties
+# ---------------------------------------------------------------------------
+def test_empty_rows(arl):
+    im = make_image(arl, 64, 8e-3, [1e8], 1e6)
+    gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=4, support=6)
+    vis = make_vis(arl, numpy.zeros((0, 3)), numpy.zeros(0), numpy.zeros((0, 1)), numpy.zeros((0, 1)))
+    for p in ('fp64', 'fp32c'):
+        gd, sw = arl.grid_visibility_to_griddata(vis, arl.create_griddata_from_image(im), cf, precision=p)
+        assert numpy.all(gd.data == 0) and numpy.all(sw == 0)
+        out = arl.degrid_visibility_from_griddata(vis, gd, cf, precision=p)
+        assert out.vis.shape == (0, 1)
+
+
+def test_rows_outside_grid_raise(arl):
+    im = make_image(arl, 64, 8e-3, [1e8], 1e6)
+    gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=4, support=8)
+    du = abs(1.0 / (64 * 8e-3))
+    uvw = numpy.array([[0.0, 0.0, 0.0], [31.5 * du, 0.0, 0.0], [0.0, -29.0 * du, 0.0], [0.0, 10 * du, 0.0]])
+    vis = make_vis(arl, uvw, numpy.full(4, 1e8), numpy.ones((4, 1)), numpy.ones((4, 1)))
+    with pytest.raises(AssertionError):
+        arl.grid_visibility_to_griddata(vis, arl.create_griddata_from_image(im), cf)
+    gd, _ = arl.grid_visibility_to_griddata(vis, arl.create_griddata_from_image(im), cf, check=False)
+    out = arl.degrid_visibility_from_griddata(vis, gd, cf, check=False)
+    assert out.vis[1, 0] == 0 and out.vis[2, 0] == 0 and out.vis[0, 0] != 0
+
+
+def test_adjointness(arl):
+    """<grid(v), g> = <v * wt, degrid(g)>: the gridder is the degridder's adjoint."""
+    rng = numpy.random.default_rng(11)
+    N, O, S, n = 128, 8, 8, 5000
+    im = make_image(arl, N, 4e-3, [1e8], 1e6)
+    _, cf = arl.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    du = abs(1.0 / (N * 4e-3))
+    lim = (N // 2 - S // 2 - 2) * du
+    uvw = numpy.stack([rng.uniform(-lim, lim, n), rng.uniform(-lim, lim, n), numpy.zeros(n)], axis=1)
+    v = rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1))
+    wt = rng.uniform(0.5, 2, (n, 1))
+    vis = make_vis(arl, uvw, numpy.full(n, 1e8), v, wt)
+    g = rng.normal(size=(1, 1, 1, N, N)) + 1j * rng.normal(size=(1, 1, 1, N, N))
+    for p, tol in (('fp64', 1e-12), ('fp32c', 1e-5)):
+        gd, _ = arl.grid_visibility_to_griddata(vis, arl.create_griddata_from_image(im), cf, precision=p)
+        lhs = numpy.vdot(gd.data, g)
+        gg = arl.create_griddata_from_image(im)
+        gg.data[...] = g
+        out = arl.degrid_visibility_from_griddata(vis, gg, cf, precision=p)
+        rhs = numpy.vdot(v * wt, out.vis)
+        assert abs(lhs - rhs) / abs(lhs) < tol
+
+
+def test_device_resident_path_matches_host(arl):
+    rng = numpy.random.default_rng(21)
+    N, O, S, n = 128, 8, 8, 4000
+    im = make_image(arl, N, 4e-3, [1e8], 1e6)
+    gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    du = abs(1.0 / (N * 4e-3))
+    lim = (N // 2 - S // 2 - 2) * du
+    uvw = numpy.stack([rng.uniform(-lim, lim, n), rng.uniform(-lim, lim, n), numpy.zeros(n)], axis=1)
+    vis = make_vis(arl, uvw, numpy.full(n, 1e8), rng.normal(size=(n, 1)) + 0j, numpy.ones((n, 1)))
+    dvis = arl.DeviceVisibility.from_visibility(vis, 'fp32c')
+    host_img, host_sw = arl.invert_2d(vis, im, gcfcf=(gcf, cf), precision='fp32c')
+    dev_img, dev_sw = arl.invert_2d(dvis, im, gcfcf=(gcf, cf), precision='fp32c')
+    assert isinstance(dev_img.data, torch.Tensor) and dev_img.data.is_cuda
+    assert rel(dev_img.data.cpu().numpy(), host_img.data) < 1e-6
+    gdev = arl.create_griddata_on_device(im, precision='fp32c')
+    gdev, _ = arl.grid_visibility_to_griddata(dvis, gdev, cf, precision='fp32c')
+    assert gdev.data.is_cuda
+
+
+def test_c2_full_size_properties(arl):
+    """Full C2 workload (W-projection, 64 planes, support 8 -> 32, 4 channels):
+    FP32C against the FP64 GPU path, exact weight sums, exact linearity."""
+    sim = __import__('importlib').import_module('algorithm-reference-library_gb300.simulation')
+    w = sim.make_workload('C2', device=torch.device('cuda'))
+    n = w['uvw'].shape[0]
+    im = make_image(arl, w['npixel'], w['cellsize'], w['freqs'], w['channel_bandwidth'])
+    gcf, cf = arl.create_awterm_convolutionfunction(im, nw=w['nwplanes'], wstep=w['wstep'],
+                                                    oversampling=w['oversampling'], support=w['support'],
+                                                    plane_support=w['plane_support'])
+    dev = torch.device('cuda')
+    uvw = torch.as_tensor(w['uvw'], device=dev)
+    f = torch.as_tensor(w['frequency'], device=dev)
+    v64 = w['vis'].to(dev)
+    res = {}
+    for p in ('fp64', 'fp32c'):
+        dvis = arl.DeviceVisibility(uvw, f, v64.to(arl.device.CDTYPE[p]),
+                                    torch.ones((n, 1), dtype=arl.device.RDTYPE[p], device=dev))
+        gd = arl.create_griddata_on_device(im, precision=p)
+        gd, sw = arl.grid_visibility_to_griddata(dvis, gd, cf, precision=p)
+        out = arl.degrid_visibility_from_griddata(dvis, gd, cf, precision=p)
+        res[p] = (gd.data.to(torch.complex128).cpu().numpy(), sw.cpu().numpy(),
+                  out.vis.to(torch.complex128).cpu().numpy())
+    assert rel(res['fp32c'][0], res['fp64'][0]) < 1e-5
+    assert rel(res['fp32c'][2], res['fp64'][2]) < 1e-5
+    counts = numpy.bincount(numpy.round((w['frequency'] - w['freqs'][0]) / w['channel_bandwidth']).astype(int),
+                            minlength=len(w['freqs']))
+    assert numpy.array_equal(res['fp64'][1][:, 0], counts.astype(float))
+    # Linearity: doubling the visibilities doubles the grid bit for bit.
+    dvis2 = arl.DeviceVisibility(uvw, f, (2 * v64).to(torch.complex64),
+                                 torch.ones((n, 1), dtype=torch.float32, device=dev))
+    g2, _ = arl.grid_visibility_to_griddata(dvis2, arl.create_griddata_on_device(im, precision='fp32c'), cf,
+                                            precision='fp32c')
+    g1 = res['fp32c'][0]
+    assert numpy.max(numpy.abs(g2.data.to(torch.complex128).cpu().numpy() - 2 * g1)) <= 1e-6 * numpy.abs(g1).max()

@@ -1,0 +1,104 @@
+"""Host-side logic of the package that needs no GPU: WCS, descriptors, the
+synthetic-observation generator, plane supports and w-slices."""
+import numpy
+import pytest
+
+
+def test_wcs_linear_transforms(arl, oracle):
+    w = arl.WCS(2)
+    w.wcs.crval = [0.0, 10.0]
+    w.wcs.crpix = [513.0, 3.0]
+    w.wcs.cdelt = [-1.953125, 0.25]
+    x = numpy.linspace(-900, 900, 101)
+    p = w.wcs_world2pix(x, x, 0)
+    assert numpy.array_equal(p[0], oracle.world2pix0(x, 0.0, 513.0, -1.953125))
+    assert numpy.array_equal(p[1], oracle.world2pix0(x, 10.0, 3.0, 0.25))
+    back = w.wcs_pix2world(p[0], p[1], 0)
+    assert numpy.allclose(back[0], x) and numpy.allclose(back[1], x)
+    sub = w.sub([2])
+    assert sub.axis(0) == (10.0, 3.0, 0.25)
+
+
+def test_descriptors_match_oracle_geometry(arl, oracle):
+    im = arl.create_image(npixel=256, cellsize=2e-3, frequency=numpy.array([1e8, 1.1e8]),
+                          channel_bandwidth=numpy.array([1e7, 1e7]),
+                          polarisation_frame=arl.PolarisationFrame('stokesIQ'))
+    gd = arl.create_griddata_from_image(im)
+    cf = arl.create_convolutionfunction_from_image(im, nz=5, zstep=12.5, oversampling=8, support=8)
+    g = arl.device.grid_desc(gd.grid_wcs, gd.data.shape)
+    c = arl.device.cf_desc(cf.grid_wcs, cf.data.shape, 0, 0)
+    img = oracle.image_geometry(256, 2e-3, 2, 2, 1e8, 1e7)
+    gax, cax = oracle.grid_axes(img), oracle.cf_axes(img, 8, 8, nz=5, zstep=12.5)
+    for name, ax in (('u', g.u), ('v', g.v), ('w', g.w), ('f', g.f)):
+        assert (ax.crval, ax.crpix, ax.cdelt) == gax[name], name
+    for name, ax in (('du', c.du), ('dv', c.dv), ('z', c.z)):
+        assert (ax.crval, ax.crpix, ax.cdelt) == cax[name], name
+    assert (g.nchan, g.npol, g.nw, g.ny, g.nx) == gax['shape']
+    assert (c.nchan, c.npol, c.nz, c.oversampling, c.support) == (2, 2, 5, 8, 8)
+
+
+def test_rows_follow_create_visibility_order(arl):
+    sim = arl.simulation if hasattr(arl, 'simulation') else __import__('importlib').import_module(
+        'algorithm-reference-library_gb300.simulation')
+    rng = numpy.random.default_rng(3)
+    xyz = sim.antennas_in_disk(5, 1000.0, rng)
+    ha = numpy.array([-0.1, 0.0, 0.2])
+    freqs = [1e8, 1.2e8]
+    uvw, f, a1, a2, t = sim.rows(xyz, ha, freqs)
+    # create_visibility's loops (processing_components/visibility/base.py:111-129)
+    row = 0
+    for it, h in enumerate(ha):
+        pos = sim.xyz_to_uvw(xyz, h, numpy.deg2rad(-45.0))
+        for i in range(5):
+            for j in range(i + 1, 5):
+                for ch, fr in enumerate(freqs):
+                    assert a1[row] == i and a2[row] == j and t[row] == it and f[row] == fr
+                    assert numpy.array_equal(uvw[row], (pos[j] - pos[i]) * (fr / sim.C_M_S))
+                    row += 1
+    assert row == uvw.shape[0]
+
+
+def test_uv_cut_keeps_window_inside(arl, oracle):
+    sim = __import__('importlib').import_module('algorithm-reference-library_gb300.simulation')
+    w = sim.make_workload('C1', max_rows=5000)
+    img = oracle.image_geometry(w['npixel'], w['cellsize'])
+    gax, cax = oracle.grid_axes(img), oracle.cf_axes(img, w['oversampling'], w['support'])
+    maps = oracle.convolution_mapping(w['uvw'], w['frequency'], gax, cax)
+    assert numpy.all(oracle.rows_in_grid(maps, gax['shape'], cax['shape']))
+
+
+def test_plane_support_zeroes_outside_taps(arl):
+    im = arl.create_image(npixel=64, cellsize=8e-3)
+    cf = arl.create_convolutionfunction_from_image(im, nz=3, oversampling=2, support=8)
+    cf.data[...] = 1.0
+    arl.set_plane_support(cf, [8, 4, 2])
+    assert numpy.all(cf.data[0, 0, 0] == 1.0)
+    assert cf.data[0, 0, 1].sum() == 2 * 2 * 4 * 4 and cf.data[0, 0, 1, 0, 0, 2:6, 2:6].min() == 1.0
+    assert cf.data[0, 0, 2].sum() == 2 * 2 * 2 * 2 and cf.data[0, 0, 2, 1, 1, 3:5, 3:5].min() == 1.0
+    with pytest.raises(AssertionError):
+        arl.set_plane_support(cf, [8, 3, 2])
+
+
+def test_support_schedule(arl):
+    s = arl.support_schedule(numpy.arange(-32, 32) * 10.0, 8, 32)
+    assert s.min() == 8 and s.max() == 32 and numpy.all(s % 2 == 0)
+    assert s[32] == 8 and s[0] == 32
+
+
+def test_wslice_iterator_matches_oracle(arl, oracle):
+    rng = numpy.random.default_rng(9)
+    n = 500
+    v = arl.Visibility(uvw=rng.normal(size=(n, 3)) * 50, frequency=numpy.full(n, 1e8), vis=numpy.zeros((n, 1)),
+                       weight=numpy.ones((n, 1)))
+    got = list(arl.vis_wslice_iter(v, 7))
+    want = oracle.wslice_rows(v.w, 7)
+    assert len(got) == len(want) and all(numpy.array_equal(a, b) for a, b in zip(got, want))
+
+
+def test_phasecentre_lmn(arl):
+    a = arl.PhaseCentre(10.0, -45.0)
+    assert a.separation_rad(a) == 0.0
+    b = arl.PhaseCentre(10.5, -44.0)
+    l, m, n1 = b.lmn(a)
+    assert l > 0 and m > 0 and n1 < 0
+    assert abs(l * l + m * m + (n1 + 1) ** 2 - 1.0) < 1e-14
