@@ -16,8 +16,10 @@ from .data_models import (BlockVisibility, ConvolutionFunction, GridData, Image,
 from .device import default_precision, set_default_precision  # noqa: F401
 from .gridding import (DeviceVisibility, convolution_mapping, degrid_visibility_from_griddata,  # noqa: F401
                        fft_griddata_to_image, fft_image_to_griddata, grid_visibility_to_griddata)
-from .imaging import (invert_2d, normalize_sumwt, predict_2d, shift_vis_to_image, vis_null_iter,  # noqa: F401
-                      vis_wslice_iter)
+from .imaging import (imaging_context, imaging_contexts, invert_2d, invert_list_serial_workflow,  # noqa: F401
+                      invert_wstack, invert_wstack_single, normalize_sumwt, predict_2d, predict_list_serial_workflow,
+                      predict_wstack, predict_wstack_single, shift_vis_to_image, vis_null_iter, vis_wslice_iter)
+from . import autograd  # noqa: F401
 from .kernels import (apply_bounding_box_convolutionfunction, calculate_bounding_box_convolutionfunction,  # noqa: F401
                       copy_convolutionfunction, copy_griddata, create_awterm_convolutionfunction,
                       create_box_convolutionfunction, create_convolutionfunction_from_image,

@@ -48,6 +48,9 @@ SIGNATURES = {
                                            _vp, _sz, _vp]),
     'arlgpu_degrid_planned': (ctypes.c_int, [_i64, ctypes.c_int, _vp, _P(CfDesc), _vp, _P(GridDesc), _vp, _vp, _sz,
                                              _vp]),
+    'arlgpu_plan_plane_mean_w': (ctypes.c_int, [_vp, _i64, _P(GridDesc), _P(CfDesc), _vp, _sz, _vp, _vp]),
+    'arlgpu_wstack_grid_to_image': (ctypes.c_int, [_vp, _P(GridDesc), ctypes.c_int, _vp, _vp, _f64, _vp, _vp, _vp]),
+    'arlgpu_wstack_image_to_grid': (ctypes.c_int, [_vp, _vp, _vp, _f64, _P(GridDesc), ctypes.c_int, _vp, _vp]),
     'arlgpu_degrid': (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp, _P(CfDesc), _vp, _P(GridDesc), _vp, _vp,
                                      _vp, _sz, _vp]),
     'arlgpu_fft_grid_to_image': (ctypes.c_int, [_vp, _P(GridDesc), ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -55,6 +58,8 @@ SIGNATURES = {
     'arlgpu_make_pswf': (ctypes.c_int, [_i32, _i32, _i32, _i32, _vp, _vp, _vp]),
     'arlgpu_make_wkernels': (ctypes.c_int, [_i32, _f64, _i32, _i32, _i32, _i32, _f64, _vp, _vp]),
     'arlgpu_apply_gains': (ctypes.c_int, [_vp, _i64, _i32, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, _vp]),
+    'arlgpu_gain_chi2': (ctypes.c_int, [_vp, _vp, _vp, _i64, _i32, ctypes.c_int, _vp, _vp, _vp, _i32, _vp, _vp,
+                                        _vp, _vp]),
     'arlgpu_phaserotate': (ctypes.c_int, [_vp, _vp, _i64, _i32, ctypes.c_int, _f64, _f64, ctypes.c_int, _vp]),
 }
 

@@ -85,6 +85,14 @@ __device__ __forceinline__ double floor_w2p(double x, const arlgpu_axis &a, doub
   return floor(p);
 }
 
+// Support of plane z: plane_support[z] clamped to an even value in [2, S].
+__device__ __forceinline__ int plane_sz(const Geom &g, int zc) {
+  if (!g.plane_support) return g.S;
+  int sz = g.plane_support[zc];
+  sz = sz < 2 ? 2 : (sz > g.S ? g.S : sz);
+  return sz & ~1;
+}
+
 struct Mapped {
   int32_t pu, pv, uf, vf, zg, zc, ch;
   bool ok;
@@ -113,8 +121,7 @@ __device__ __forceinline__ Mapped map_row(double u, double v, double w, double f
   m.zc = ok ? (int32_t)zc : 0;
   m.ch = ok ? (int32_t)ch : 0;
   if (ok) {
-    int sz = g.plane_support ? g.plane_support[m.zc] : g.S;
-    int h = sz >> 1;
+    int h = plane_sz(g, m.zc) >> 1;
     ok = (m.pu - h >= 0) && (m.pu + h <= g.nx) && (m.pv - h >= 0) && (m.pv + h <= g.ny);
   }
   m.ok = ok;
@@ -222,6 +229,31 @@ __global__ void k_scatter(const uint32_t *__restrict__ keys, const RowMap *__res
   }
 }
 
+// Mean w of the rows of each grid w-plane (over all channels), from a built
+// plan: block z sums uvw[sidx[r]].w over the sorted row ranges of every
+// (channel, plane z) bin run, in a fixed order.  Planes without rows get 0.
+__global__ void k_plane_mean_w(const double *__restrict__ uvw, const uint32_t *__restrict__ sidx,
+                               const uint32_t *__restrict__ off, Geom g, double *__restrict__ wmean) {
+  __shared__ double ssum[256];
+  const int z = blockIdx.x;
+  const uint32_t tiles = (uint32_t)g.ntv * g.ntu;
+  double sum = 0.0;
+  unsigned long long cnt = 0;
+  for (int c = 0; c < g.nchan; ++c) {
+    const uint32_t b0 = ((uint32_t)c * g.nw + z) * tiles;
+    const uint32_t r0 = off[b0], r1 = off[b0 + tiles];
+    for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) sum += uvw[3 * (size_t)sidx[r] + 2];
+    cnt += r1 - r0;
+  }
+  ssum[threadIdx.x] = sum;
+  __syncthreads();
+  for (int d = blockDim.x / 2; d > 0; d >>= 1) {
+    if (threadIdx.x < d) ssum[threadIdx.x] += ssum[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) wmean[z] = cnt ? ssum[0] / (double)cnt : 0.0;
+}
+
 // ---------------------------------------------------------------------------
 // Complex helpers
 // ---------------------------------------------------------------------------
@@ -321,7 +353,7 @@ k_grid(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sid
       const RowMap m = smap[r];
       const uint32_t idx = sidx[r];
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = g.plane_support ? g.plane_support[zc] : S;
+      const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
       const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);  // window origin, grid pixels
       CT vw[4];
@@ -441,7 +473,7 @@ k_degrid(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ s
       const RowMap m = smap[r];
       const uint32_t idx = sidx[r];
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = g.plane_support ? g.plane_support[zc] : S;
+      const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
       const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
       const CT *cfr = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
@@ -549,6 +581,9 @@ int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precisio
   int SG = 64;
   if ((size_t)g->npol * SG * SG * cell > 64 * 1024) SG = 32;
   if (SG - g->S < 8) SG = ((g->S + 8 + 7) / 8) * 8;
+  if ((size_t)g->npol * SG * SG * cell > 200 * 1024)
+    return fail(ARLGPU_ERR_UNSUPPORTED, "support %d with %d polarisations needs more shared memory than a CTA has",
+                g->S, g->npol);
   g->SG = SG;
   g->T = SG - g->S;
   g->ntu = (g->nx + g->T - 1) / g->T;
@@ -764,6 +799,21 @@ extern "C" int arlgpu_degrid(const double *uvw, const double *frequency, int64_t
                              size_t workspace_bytes, void *stream) {
   ARL_TRY(arlgpu_plan_build(uvw, frequency, nvis, gd, cd, workspace, workspace_bytes, n_bad_dev, stream));
   return arlgpu_degrid_planned(nvis, precision, cf, cd, grid, gd, vis_out, workspace, workspace_bytes, stream);
+}
+
+extern "C" int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const arlgpu_grid_desc *gd,
+                                        const arlgpu_cf_desc *cd, const void *workspace, size_t workspace_bytes,
+                                        double *wmean, void *stream) {
+  Geom g;
+  ARL_TRY(make_geom(gd, cd, ARLGPU_FP32C, &g));
+  ARL_TRY(check_rows(nvis));
+  if (!wmean || (nvis > 0 && !uvw)) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  PlanBufs b;
+  ARL_TRY(plan_carve(const_cast<void *>(workspace), workspace_bytes, nvis, g, &b));
+  k_plane_mean_w<<<g.nw, 256, 0, static_cast<cudaStream_t>(stream)>>>(uvw, b.sidx, b.offsets, g, wmean);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
 }
 
 extern "C" unsigned long long arlgpu_kernel_launches(void) { return g_launches.load(); }

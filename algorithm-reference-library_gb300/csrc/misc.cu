@@ -53,6 +53,69 @@ __global__ void k_gains(CT *vis, int64_t nvis, int npol, const int32_t *a1, cons
   }
 }
 
+// chi^2 = sum_r,p w |Vobs - g[a2] conj(g[a1]) M|^2 and its conjugate-Wirtinger
+// derivatives (row of baseline (a1, a2) stored at [a2, a1], the convention of
+// apply_gaintable, calibration/operations.py:134-137):
+//   d/d conj(M)     = -w conj(g2) g1 R
+//   d/d conj(g[a2]) = -w R g1 conj(M)        (summed over rows and pols)
+//   d/d conj(g[a1]) = -w conj(R) g2 M
+// with R = Vobs - g2 conj(g1) M.  Per-antenna sums go through shared memory,
+// then one global atomic per antenna and block.
+template <typename CT>
+__global__ void k_gain_chi2(const CT *__restrict__ vobs, const CT *__restrict__ m, const double *__restrict__ wt,
+                            int64_t nvis, int npol, const int32_t *__restrict__ a1, const int32_t *__restrict__ a2,
+                            const double2 *__restrict__ g, int nant, double *__restrict__ chi2,
+                            CT *__restrict__ grad_m, double2 *__restrict__ grad_g) {
+  extern __shared__ double sg[];  // 2 * nant: re, im of the per-antenna sums
+  for (int i = threadIdx.x; i < 2 * nant; i += blockDim.x) sg[i] = 0.0;
+  __syncthreads();
+  double local = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nvis; r += (int64_t)gridDim.x * blockDim.x) {
+    const int i1 = a1[r], i2 = a2[r];
+    const double2 g1 = g[i1], g2 = g[i2];
+    const double gr = g2.x * g1.x + g2.y * g1.y, gi = g2.y * g1.x - g2.x * g1.y;  // g2 conj(g1)
+    double d2r = 0.0, d2i = 0.0, d1r = 0.0, d1i = 0.0;
+    for (int p = 0; p < npol; ++p) {
+      const int64_t k = r * npol + p;
+      const double w = wt ? wt[k] : 1.0;
+      const double mr = m[k].x, mi = m[k].y;
+      const double rr = (double)vobs[k].x - (gr * mr - gi * mi);
+      const double ri = (double)vobs[k].y - (gr * mi + gi * mr);
+      local += w * (rr * rr + ri * ri);
+      if (grad_m) {
+        // -w conj(g2 conj(g1)) R
+        CT o;
+        o.x = -w * (gr * rr + gi * ri);
+        o.y = -w * (gr * ri - gi * rr);
+        grad_m[k] = o;
+      }
+      // -w R g1 conj(M)
+      const double tr = g1.x * mr + g1.y * mi, ti = g1.y * mr - g1.x * mi;  // g1 conj(M)
+      d2r -= w * (rr * tr - ri * ti);
+      d2i -= w * (rr * ti + ri * tr);
+      // -w conj(R) g2 M
+      const double ur = g2.x * mr - g2.y * mi, ui = g2.x * mi + g2.y * mr;  // g2 M
+      d1r -= w * (rr * ur + ri * ui);
+      d1i -= w * (rr * ui - ri * ur);
+    }
+    if (grad_g) {
+      atomicAdd(&sg[2 * i2], d2r);
+      atomicAdd(&sg[2 * i2 + 1], d2i);
+      atomicAdd(&sg[2 * i1], d1r);
+      atomicAdd(&sg[2 * i1 + 1], d1i);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(chi2, local);
+  __syncthreads();
+  if (grad_g)
+    for (int i = threadIdx.x; i < nant; i += blockDim.x)
+      if (sg[2 * i] != 0.0 || sg[2 * i + 1] != 0.0) {
+        atomicAdd(&grad_g[i].x, sg[2 * i]);
+        atomicAdd(&grad_g[i].y, sg[2 * i + 1]);
+      }
+}
+
 static int nblk(int64_t n) {
   int64_t b = (n + 255) / 256;
   return (int)(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
@@ -89,6 +152,36 @@ extern "C" int arlgpu_apply_gains(void *vis, int64_t nvis, int32_t npol, int pre
     k_gains<double2><<<nblk(nvis), 256, 0, st>>>(static_cast<double2 *>(vis), nvis, npol, a1, a2, g, inverse);
   else if (precision == ARLGPU_FP32C)
     k_gains<float2><<<nblk(nvis), 256, 0, st>>>(static_cast<float2 *>(vis), nvis, npol, a1, a2, g, inverse);
+  else
+    return fail(ARLGPU_ERR_INVALID, "bad precision");
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
+}
+
+extern "C" int arlgpu_gain_chi2(const void *vobs, const void *model, const double *weight, int64_t nvis, int32_t npol,
+                                int precision, const int32_t *a1, const int32_t *a2, const void *gains, int32_t nant,
+                                double *chi2, void *grad_model, void *grad_gains, void *stream) {
+  if (nvis < 0 || npol < 1 || nant < 1 || !chi2 || (nvis > 0 && (!vobs || !model || !a1 || !a2 || !gains)))
+    return fail(ARLGPU_ERR_INVALID, "bad arguments");
+  if (nant > 4096) return fail(ARLGPU_ERR_UNSUPPORTED, "more than 4096 antennas");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  ARL_CUDA(cudaMemsetAsync(chi2, 0, sizeof(double), st));
+  if (grad_gains) ARL_CUDA(cudaMemsetAsync(grad_gains, 0, sizeof(double2) * nant, st));
+  if (nvis == 0) return ARLGPU_OK;
+  const size_t smem = 2 * sizeof(double) * nant;
+  const int blocks = nblk(nvis) < 152 * 4 ? nblk(nvis) : 152 * 4;
+  const double2 *g = static_cast<const double2 *>(gains);
+  if (precision == ARLGPU_FP64)
+    k_gain_chi2<double2><<<blocks, 256, smem, st>>>(static_cast<const double2 *>(vobs),
+                                                     static_cast<const double2 *>(model), weight, nvis, npol, a1, a2, g,
+                                                     nant, chi2, static_cast<double2 *>(grad_model),
+                                                     static_cast<double2 *>(grad_gains));
+  else if (precision == ARLGPU_FP32C)
+    k_gain_chi2<float2><<<blocks, 256, smem, st>>>(static_cast<const float2 *>(vobs), static_cast<const float2 *>(model),
+                                                    weight, nvis, npol, a1, a2, g, nant, chi2,
+                                                    static_cast<float2 *>(grad_model),
+                                                    static_cast<double2 *>(grad_gains));
   else
     return fail(ARLGPU_ERR_INVALID, "bad precision");
   ARL_LAUNCH_CHECK();

@@ -1,0 +1,242 @@
+// Batched w-stacking (K9): every w-slice gridded into its own plane of one
+// [nchan][npol][K][ny][nx] grid by a single gridder launch, one batched cuFFT
+// over all planes, and one pass that applies each slice's w-beam and sums the
+// slices into the image.
+//
+// Reference behaviour:
+//   vis_wslice_iter                       processing_components/visibility/iterators.py:91-109
+//   invert_wstack_single / predict_wstack_single
+//                                         processing_components/imaging/wstack_single.py:26-96
+//   w_beam / create_w_term_like           processing_library/fourier_transforms/convolutional_gridding.py:120-188,
+//                                         processing_library/image/operations.py:364-408
+//   invert_list_serial_workflow (sum of sumwt-weighted slice images, normalisation)
+//                                         workflows/serial/imaging/imaging_serial.py:186-197
+//
+// invert: slice s contributes sumwt_s * Re(wb_s * I_s) with I_s = ifft(grid_s) gcf N^2 / sumwt_s,
+//         so the image is gcf * sum_s Re(wb_s * U_s) / sum_s sumwt_s, U_s the unnormalised
+//         centred inverse transform of grid_s.
+// predict: V = P(Re(wb) M) - i P(Im(wb) M) = P(conj(wb) M) by linearity, so plane s of the
+//          grid is fft(conj(wb_s) M gcf) and one degrid over all rows reads plane s for the
+//          rows of slice s.
+#include <cufft.h>
+
+#include "common.cuh"
+
+namespace arlgpu {
+
+void count_launch(unsigned n);
+int get_plan(int ny, int nx, int batch, long long dist, cufftType type, cufftHandle *out);
+
+// w-screen of create_w_term_like at one pixel of an n x n image centred on
+// (n/2, n/2): exp(-2 pi i w (1 - sqrt(1 - r^2))), zero for r^2 >= 1, one at
+// r^2 == 0.  The pixel part, nterm = 1 - sqrt(1 - r^2), is computed once per
+// pixel (FP64) and shared by all slices.
+struct Pix {
+  double nterm;
+  int state;  // 0: r^2 == 0 (value 1), 1: inside, 2: r^2 >= 1 (value 0)
+};
+__device__ __forceinline__ Pix wpix(int y, int x, int n, double fov) {
+  const double c = (double)(n / 2);
+  const double ly = ((double)y - c) / (double)n, mx = ((double)x - c) / (double)n;
+  const double r2 = fov * fov * (ly * ly + mx * mx);
+  Pix p;
+  p.state = r2 == 0.0 ? 0 : (r2 >= 1.0 ? 2 : 1);
+  p.nterm = p.state == 1 ? 1.0 - sqrt(1.0 - r2) : 0.0;
+  return p;
+}
+
+// FP64 path: exp(-2 pi i w nterm) with an FP64 sincos.
+__device__ __forceinline__ double2 wb64(const Pix &p, double w) {
+  if (p.state == 0) return make_double2(1.0, 0.0);
+  if (p.state == 2) return make_double2(0.0, 0.0);
+  double s, co;
+  sincos(-2.0 * M_PI * w * p.nterm, &s, &co);
+  return make_double2(co, s);
+}
+
+// FP32C path: the phase in turns t = w nterm is formed in FP64 and reduced to
+// [-1/2, 1/2] before an FP32 sincospi, so the phase error stays at FP32
+// rounding of the reduced argument (< 1e-7 rad) for any w.
+__device__ __forceinline__ double2 wb32(const Pix &p, double w) {
+  if (p.state == 0) return make_double2(1.0, 0.0);
+  if (p.state == 2) return make_double2(0.0, 0.0);
+  const double t = w * p.nterm;
+  const float f = (float)(t - rint(t));
+  float s, co;
+  sincospif(-2.f * f, &s, &co);
+  return make_double2(co, s);
+}
+
+template <typename CT> struct WB;
+template <> struct WB<float2> {
+  __device__ static __forceinline__ double2 at(const Pix &p, double w) { return wb32(p, w); }
+};
+template <> struct WB<double2> {
+  __device__ static __forceinline__ double2 at(const Pix &p, double w) { return wb64(p, w); }
+};
+
+// pre-invert: chk sign on every plane (the centred-transform trick)
+template <typename CT>
+__global__ void k_chk_planes(CT *grid, int64_t nplanes, int ny, int nx) {
+  const int64_t plane = (int64_t)ny * nx, tot = nplanes * plane;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t yx = i % plane;
+    const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
+    if ((x + y) & 1) {
+      CT v = grid[i];
+      v.x = -v.x;
+      v.y = -v.y;
+      grid[i] = v;
+    }
+  }
+}
+
+// image[b, y, x] = gcf * sum_s Re(wb_s * U_s * chk * s0) / sumwt[b]
+template <typename CT>
+__global__ void k_wstack_combine(const CT *__restrict__ grid, int nb, int K, int ny, int nx, float s0, double fov,
+                                 const double *__restrict__ wmean, const double *__restrict__ gcf,
+                                 const double *__restrict__ sumwt, double *__restrict__ image) {
+  const int64_t plane = (int64_t)ny * nx, tot = (int64_t)nb * plane;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / plane, yx = i - b * plane;
+    const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
+    const double sg = (((x + y) & 1) ? -1.0 : 1.0) * (double)s0;
+    const Pix px = wpix(y, x, nx, fov);
+    double acc = 0.0;
+    for (int s = 0; s < K; ++s) {
+      const CT u = grid[(b * K + s) * plane + yx];
+      const double2 wb = WB<CT>::at(px, wmean[s]);
+      acc += wb.x * (double)u.x - wb.y * (double)u.y;
+    }
+    const double w = sumwt[b];
+    image[i] = w > 0.0 ? acc * sg * gcf[i] / w : 0.0;
+  }
+}
+
+// grid[b, s] = chk * conj(wb_s) * image * gcf  (complex), for every slice s
+template <typename CT>
+__global__ void k_wstack_pre_predict(const double *__restrict__ image, const double *__restrict__ gcf, int nb, int K,
+                                     int ny, int nx, double fov, const double *__restrict__ wmean,
+                                     CT *__restrict__ grid) {
+  const int64_t plane = (int64_t)ny * nx, tot = (int64_t)nb * plane;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / plane, yx = i - b * plane;
+    const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
+    const double m = image[i] * gcf[i] * (((x + y) & 1) ? -1.0 : 1.0);
+    const Pix px = wpix(y, x, nx, fov);
+    for (int s = 0; s < K; ++s) {
+      const double2 wb = WB<CT>::at(px, wmean[s]);
+      CT v;
+      v.x = wb.x * m;
+      v.y = -wb.y * m;
+      grid[(b * K + s) * plane + yx] = v;
+    }
+  }
+}
+
+// post-predict: chk * s0 on every plane
+template <typename CT>
+__global__ void k_chk_scale(CT *grid, int64_t nplanes, int ny, int nx, float s0) {
+  const int64_t plane = (int64_t)ny * nx, tot = nplanes * plane;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t yx = i % plane;
+    const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
+    const float sg = (((x + y) & 1) ? -1.f : 1.f) * s0;
+    CT v = grid[i];
+    v.x *= sg;
+    v.y *= sg;
+    grid[i] = v;
+  }
+}
+
+static int nblk(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  return (int)(b < 1 ? 1 : (b > 152 * 64 ? 152 * 64 : b));
+}
+
+template <typename CT>
+static int exec(cufftHandle h, CT *d, int dir) {
+  cufftResult r = sizeof(CT) == 8
+                      ? cufftExecC2C(h, reinterpret_cast<cufftComplex *>(d), reinterpret_cast<cufftComplex *>(d), dir)
+                      : cufftExecZ2Z(h, reinterpret_cast<cufftDoubleComplex *>(d),
+                                     reinterpret_cast<cufftDoubleComplex *>(d), dir);
+  return r == CUFFT_SUCCESS ? ARLGPU_OK : fail(ARLGPU_ERR_CUFFT, "cuFFT exec failed (%d)", (int)r);
+}
+
+template <typename CT>
+static int g2i(CT *grid, const arlgpu_grid_desc *gd, const double *gcf, const double *wmean, double fov,
+               const double *sumwt, double *image, cudaStream_t st) {
+  const int nb = gd->nchan * gd->npol, K = gd->nw, ny = gd->ny, nx = gd->nx;
+  const int64_t nplanes = (int64_t)nb * K;
+  if (nplanes > 0x7fffffff) return fail(ARLGPU_ERR_UNSUPPORTED, "too many planes");
+  cufftHandle h;
+  ARL_TRY(get_plan(ny, nx, (int)nplanes, (long long)ny * nx, sizeof(CT) == 8 ? CUFFT_C2C : CUFFT_Z2Z, &h));
+  k_chk_planes<CT><<<nblk(nplanes * ny * nx), 256, 0, st>>>(grid, nplanes, ny, nx);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  cufftResult r = cufftSetStream(h, st);
+  if (r != CUFFT_SUCCESS) return fail(ARLGPU_ERR_CUFFT, "cufftSetStream failed (%d)", (int)r);
+  ARL_TRY(exec<CT>(h, grid, CUFFT_INVERSE));
+  const float s0 = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
+  k_wstack_combine<CT><<<nblk((int64_t)nb * ny * nx), 256, 0, st>>>(grid, nb, K, ny, nx, s0, fov, wmean, gcf, sumwt,
+                                                                     image);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
+}
+
+template <typename CT>
+static int i2g(const double *image, const double *gcf, const double *wmean, double fov, const arlgpu_grid_desc *gd,
+               CT *grid, cudaStream_t st) {
+  const int nb = gd->nchan * gd->npol, K = gd->nw, ny = gd->ny, nx = gd->nx;
+  const int64_t nplanes = (int64_t)nb * K;
+  if (nplanes > 0x7fffffff) return fail(ARLGPU_ERR_UNSUPPORTED, "too many planes");
+  cufftHandle h;
+  ARL_TRY(get_plan(ny, nx, (int)nplanes, (long long)ny * nx, sizeof(CT) == 8 ? CUFFT_C2C : CUFFT_Z2Z, &h));
+  k_wstack_pre_predict<CT><<<nblk((int64_t)nb * ny * nx), 256, 0, st>>>(image, gcf, nb, K, ny, nx, fov, wmean, grid);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  cufftResult r = cufftSetStream(h, st);
+  if (r != CUFFT_SUCCESS) return fail(ARLGPU_ERR_CUFFT, "cufftSetStream failed (%d)", (int)r);
+  ARL_TRY(exec<CT>(h, grid, CUFFT_FORWARD));
+  const float s0 = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
+  k_chk_scale<CT><<<nblk(nplanes * ny * nx), 256, 0, st>>>(grid, nplanes, ny, nx, s0);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
+}
+
+static int check(const arlgpu_grid_desc *gd, int precision) {
+  if (!gd) return fail(ARLGPU_ERR_INVALID, "null grid descriptor");
+  if (precision != ARLGPU_FP32C && precision != ARLGPU_FP64) return fail(ARLGPU_ERR_INVALID, "bad precision");
+  if (gd->nchan < 1 || gd->npol < 1 || gd->nw < 1 || gd->ny < 2 || gd->nx < 2)
+    return fail(ARLGPU_ERR_INVALID, "bad grid shape");
+  if (gd->ny != gd->nx || (gd->nx & 1)) return fail(ARLGPU_ERR_UNSUPPORTED, "w-stacking needs a square, even image");
+  return ARLGPU_OK;
+}
+
+}  // namespace arlgpu
+
+using namespace arlgpu;
+
+extern "C" int arlgpu_wstack_grid_to_image(void *grid, const arlgpu_grid_desc *gd, int precision, const double *gcf,
+                                           const double *wmean, double cellsize, const double *sumwt, double *image,
+                                           void *stream) {
+  ARL_TRY(check(gd, precision));
+  if (!grid || !gcf || !wmean || !sumwt || !image) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  const double fov = gd->nx * cellsize;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (precision == ARLGPU_FP64) return g2i<double2>(static_cast<double2 *>(grid), gd, gcf, wmean, fov, sumwt, image, st);
+  return g2i<float2>(static_cast<float2 *>(grid), gd, gcf, wmean, fov, sumwt, image, st);
+}
+
+extern "C" int arlgpu_wstack_image_to_grid(const double *image, const double *gcf, const double *wmean,
+                                           double cellsize, const arlgpu_grid_desc *gd, int precision, void *grid,
+                                           void *stream) {
+  ARL_TRY(check(gd, precision));
+  if (!grid || !gcf || !wmean || !image) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  const double fov = gd->nx * cellsize;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (precision == ARLGPU_FP64) return i2g<double2>(image, gcf, wmean, fov, gd, static_cast<double2 *>(grid), st);
+  return i2g<float2>(image, gcf, wmean, fov, gd, static_cast<float2 *>(grid), st);
+}

@@ -15,6 +15,8 @@ Reference behaviour:
 invert_2d keeps the grid in HBM between the gridder and the FFT: one host->device
 copy of the rows in, one device->host copy of the image out.
 """
+import ctypes
+
 import numpy
 import torch
 
@@ -162,3 +164,242 @@ def vis_wslice_iter(vis, vis_slices=1):
     wstack = boxes[1] - boxes[0] if vis_slices > 1 else 2 * wmaxabs
     for box in boxes:
         yield numpy.abs(w - box) < 0.5 * wstack
+
+
+# ---------------------------------------------------------------------------
+# W-stacking
+# ---------------------------------------------------------------------------
+def _slice_axis(w_t, vis_slices):
+    """WW grid axis (crval, crpix, cdelt) whose round-to-nearest plane index is
+    the ``vis_wslice_iter`` slice: boxes linspace(-wmax, wmax, K), a row in slice
+    s when |w - box_s| < step/2 (``visibility/iterators.py:91-109``)."""
+    wmax = float(w_t.abs().max().item()) if w_t.numel() else 0.0
+    if vis_slices > 1:
+        step = (2.0 * wmax) / (vis_slices - 1)
+    else:
+        step = 2.0 * wmax
+    if step == 0.0:
+        step = 1e15
+    return -wmax, 1.0, step
+
+
+def _wstack_setup(vis, im, vis_slices, gcfcf, precision, device, kwargs):
+    gcf, cf = gcfcf if gcfcf is not None else create_pswf_convolutionfunction(im)
+    if cf.shape[2] != 1:
+        raise NotImplementedError('batched w-stacking grids with a 2-D kernel (nz == 1); use invert_wstack_single '
+                                  'per slice for w-stacking with w-projection kernels')
+    uvw, f, v, w = _rows(vis, precision, device)
+    nchan, npol, ny, nx = im.shape
+    gwcs = _grid_wcs(im, vis_slices, 1e15)
+    crval, crpix, cdelt = _slice_axis(uvw[:, 2], vis_slices)
+    gwcs.wcs.crval[2], gwcs.wcs.crpix[2], gwcs.wcs.cdelt[2] = crval, crpix, cdelt
+    gd = dv.grid_desc(gwcs, (nchan, npol, vis_slices, ny, nx))
+    cf_t, cs, ps, psup = dv.device_cf(cf, precision, device)
+    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup)
+    ws = dv.WORKSPACE.get(dv.plan_bytes(uvw.shape[0], gd, cd), device)
+    n_bad = torch.zeros(1, dtype=torch.int64, device=device)
+    nat.call('arlgpu_plan_build', nat.ptr(uvw), nat.ptr(f), uvw.shape[0], ctypes.byref(gd), ctypes.byref(cd),
+             nat.ptr(ws), ws.numel(), nat.ptr(n_bad), nat.stream_ptr())
+    wmean = torch.empty(vis_slices, dtype=torch.float64, device=device)
+    nat.call('arlgpu_plan_plane_mean_w', nat.ptr(uvw), uvw.shape[0], ctypes.byref(gd), ctypes.byref(cd),
+             nat.ptr(ws), ws.numel(), nat.ptr(wmean), nat.stream_ptr())
+    # Rows outside every slice are dropped as vis_wslice_iter drops them (only
+    # possible for vis_slices == 1); any other rejected row is outside the grid.
+    pw = torch.round((uvw[:, 2] - crval) / cdelt + crpix - 1.0)
+    n_outside = int(((pw < 0) | (pw >= vis_slices)).sum().item())
+    nb = int(n_bad.item())
+    assert nb == n_outside, "%d visibilities fall outside the grid or convolution function" % (nb - n_outside)
+    cellsize = abs(float(im.wcs.wcs.cdelt[0])) * numpy.pi / 180.0
+    return dict(gcf=gcf, cf=cf, uvw=uvw, f=f, v=v, w=w, gd=gd, cd=cd, cf_t=cf_t, ws=ws, wmean=wmean,
+                cellsize=cellsize)
+
+
+def invert_wstack(vis, im, vis_slices, dopsf=False, normalize=True, gcfcf=None, precision=None, **kwargs):
+    """W-stack invert over all slices at once: equals ``invert_list_serial_workflow``
+    with context 'wstack' (imaging_serial.py:186-197): sum_s sumwt_s * invert_wstack_single_s,
+    normalised by sum_s sumwt_s.  One gridder launch, one batched FFT, one combine."""
+    precision = dv.resolve_precision(precision)
+    device = dv.require_cuda()
+    s = _wstack_setup(vis, im, vis_slices, gcfcf, precision, device, kwargs)
+    gd, cd = s['gd'], s['cd']
+    nchan, npol, ny, nx = im.shape
+    v = torch.ones_like(s['v']) if dopsf else s['v']
+    grid_t = torch.empty((nchan, npol, vis_slices, ny, nx), dtype=dv.CDTYPE[precision], device=device)
+    sumwt = torch.empty((nchan, npol), dtype=torch.float64, device=device)
+    nat.call('arlgpu_grid_planned', nat.ptr(v), nat.ptr(s['w']), s['uvw'].shape[0], nat.PRECISIONS[precision],
+             nat.ptr(s['cf_t']), ctypes.byref(cd), nat.ptr(grid_t), ctypes.byref(gd), nat.ptr(sumwt),
+             nat.ptr(s['ws']), s['ws'].numel(), nat.stream_ptr())
+    image = torch.empty((nchan, npol, ny, nx), dtype=torch.float64, device=device)
+    norm = sumwt if normalize else torch.ones_like(sumwt)
+    nat.call('arlgpu_wstack_grid_to_image', nat.ptr(grid_t), ctypes.byref(gd), nat.PRECISIONS[precision],
+             nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),
+             nat.stream_ptr())
+    host = not isinstance(vis, DeviceVisibility)
+    out = Image(image.cpu().numpy() if host else image, im.wcs.deepcopy(), im.polarisation_frame)
+    return out, (sumwt.cpu().numpy() if host else sumwt)
+
+
+def predict_wstack(vis, model, vis_slices, gcfcf=None, precision=None, **kwargs):
+    """W-stack predict over all slices at once: equals ``predict_list_serial_workflow``
+    with context 'wstack' (each slice's rows get predict_wstack_single's values)."""
+    precision = dv.resolve_precision(precision)
+    device = dv.require_cuda()
+    s = _wstack_setup(vis, model, vis_slices, gcfcf, precision, device, kwargs)
+    gd, cd = s['gd'], s['cd']
+    nchan, npol, ny, nx = model.shape
+    d = model.data
+    m_t = d.to(device=device, dtype=torch.float64).contiguous() if isinstance(d, torch.Tensor) else \
+        dv.to_device(numpy.asarray(d, numpy.float64), torch.float64, device)
+    grid_t = torch.empty((nchan, npol, vis_slices, ny, nx), dtype=dv.CDTYPE[precision], device=device)
+    nat.call('arlgpu_wstack_image_to_grid', nat.ptr(m_t), nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']),
+             s['cellsize'], ctypes.byref(gd), nat.PRECISIONS[precision], nat.ptr(grid_t), nat.stream_ptr())
+    out = torch.empty((s['uvw'].shape[0], npol), dtype=dv.CDTYPE[precision], device=device)
+    nat.call('arlgpu_degrid_planned', s['uvw'].shape[0], nat.PRECISIONS[precision], nat.ptr(s['cf_t']),
+             ctypes.byref(cd), nat.ptr(grid_t), ctypes.byref(gd), nat.ptr(out), nat.ptr(s['ws']), s['ws'].numel(),
+             nat.stream_ptr())
+    if isinstance(vis, DeviceVisibility):
+        return DeviceVisibility(vis.uvw, vis.frequency, out, vis.imaging_weight, vis.polarisation_frame,
+                                vis.phasecentre)
+    newvis = copy_visibility(vis, zero=True)
+    newvis.data['vis'][...] = out.cpu().numpy()
+    return newvis
+
+
+def invert_wstack_single(vis, im, dopsf, normalize=True, remove=True, gcfcf=None, precision=None, **kwargs):
+    """``wstack_single.py:67-96``: (Re(wb * I), sumwt) for one slice, wb the
+    w-beam of the slice's mean w and I the complex invert_2d image."""
+    return _single_slice_invert(vis, im, dopsf, normalize, gcfcf, precision)
+
+
+def _single_slice(vis, im, gcfcf, precision, device):
+    gcf, cf = gcfcf if gcfcf is not None else create_pswf_convolutionfunction(im)
+    if cf.shape[2] != 1:
+        raise NotImplementedError('w-stacking with w-projection kernels is outside the GB300 path')
+    uvw, f, v, w = _rows(vis, precision, device)
+    nchan, npol, ny, nx = im.shape
+    gd = dv.grid_desc(_grid_wcs(im, 1, 1e15), (nchan, npol, 1, ny, nx))
+    cf_t, cs, ps, psup = dv.device_cf(cf, precision, device)
+    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup)
+    ws = dv.WORKSPACE.get(dv.plan_bytes(uvw.shape[0], gd, cd), device)
+    n_bad = torch.zeros(1, dtype=torch.int64, device=device)
+    nat.call('arlgpu_plan_build', nat.ptr(uvw), nat.ptr(f), uvw.shape[0], ctypes.byref(gd), ctypes.byref(cd),
+             nat.ptr(ws), ws.numel(), nat.ptr(n_bad), nat.stream_ptr())
+    _assert_in_grid(n_bad)
+    wmean = torch.empty(1, dtype=torch.float64, device=device)
+    nat.call('arlgpu_plan_plane_mean_w', nat.ptr(uvw), uvw.shape[0], ctypes.byref(gd), ctypes.byref(cd),
+             nat.ptr(ws), ws.numel(), nat.ptr(wmean), nat.stream_ptr())
+    cellsize = abs(float(im.wcs.wcs.cdelt[0])) * numpy.pi / 180.0
+    return dict(gcf=gcf, cf=cf, uvw=uvw, f=f, v=v, w=w, gd=gd, cd=cd, cf_t=cf_t, ws=ws, wmean=wmean,
+                cellsize=cellsize)
+
+
+def _single_slice_invert(vis, im, dopsf, normalize, gcfcf, precision):
+    precision = dv.resolve_precision(precision)
+    device = dv.require_cuda()
+    s = _single_slice(vis, im, gcfcf, precision, device)
+    gd, cd = s['gd'], s['cd']
+    nchan, npol, ny, nx = im.shape
+    v = torch.ones_like(s['v']) if dopsf else s['v']
+    grid_t = torch.empty((nchan, npol, 1, ny, nx), dtype=dv.CDTYPE[precision], device=device)
+    sumwt = torch.empty((nchan, npol), dtype=torch.float64, device=device)
+    nat.call('arlgpu_grid_planned', nat.ptr(v), nat.ptr(s['w']), s['uvw'].shape[0], nat.PRECISIONS[precision],
+             nat.ptr(s['cf_t']), ctypes.byref(cd), nat.ptr(grid_t), ctypes.byref(gd), nat.ptr(sumwt),
+             nat.ptr(s['ws']), s['ws'].numel(), nat.stream_ptr())
+    image = torch.empty((nchan, npol, ny, nx), dtype=torch.float64, device=device)
+    norm = sumwt if normalize else torch.ones_like(sumwt)
+    nat.call('arlgpu_wstack_grid_to_image', nat.ptr(grid_t), ctypes.byref(gd), nat.PRECISIONS[precision],
+             nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),
+             nat.stream_ptr())
+    host = not isinstance(vis, DeviceVisibility)
+    out = Image(image.cpu().numpy() if host else image, im.wcs.deepcopy(), im.polarisation_frame)
+    return out, (sumwt.cpu().numpy() if host else sumwt)
+
+
+def predict_wstack_single(vis, model, remove=True, gcfcf=None, precision=None, **kwargs):
+    """``wstack_single.py:26-64``: V = predict_2d(conj(w-beam of the mean w) * model).
+    As in ARL the input's vis column is zeroed."""
+    precision = dv.resolve_precision(precision)
+    device = dv.require_cuda()
+    if isinstance(vis, Visibility):
+        vis.data['vis'][...] = 0.0
+    s = _single_slice(vis, model, gcfcf, precision, device)
+    gd, cd = s['gd'], s['cd']
+    nchan, npol, ny, nx = model.shape
+    d = model.data
+    m_t = d.to(device=device, dtype=torch.float64).contiguous() if isinstance(d, torch.Tensor) else \
+        dv.to_device(numpy.asarray(d, numpy.float64), torch.float64, device)
+    grid_t = torch.empty((nchan, npol, 1, ny, nx), dtype=dv.CDTYPE[precision], device=device)
+    nat.call('arlgpu_wstack_image_to_grid', nat.ptr(m_t), nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']),
+             s['cellsize'], ctypes.byref(gd), nat.PRECISIONS[precision], nat.ptr(grid_t), nat.stream_ptr())
+    out = torch.empty((s['uvw'].shape[0], npol), dtype=dv.CDTYPE[precision], device=device)
+    nat.call('arlgpu_degrid_planned', s['uvw'].shape[0], nat.PRECISIONS[precision], nat.ptr(s['cf_t']),
+             ctypes.byref(cd), nat.ptr(grid_t), ctypes.byref(gd), nat.ptr(out), nat.ptr(s['ws']), s['ws'].numel(),
+             nat.stream_ptr())
+    if isinstance(vis, DeviceVisibility):
+        return DeviceVisibility(vis.uvw, vis.frequency, out, vis.imaging_weight, vis.polarisation_frame,
+                                vis.phasecentre)
+    newvis = copy_visibility(vis, zero=True)
+    newvis.data['vis'][...] = out.cpu().numpy()
+    return newvis
+
+
+# ---------------------------------------------------------------------------
+# Contexts and serial workflows
+# ---------------------------------------------------------------------------
+def imaging_contexts():
+    """``workflows/shared/imaging/imaging_shared.py:21-88``, restricted to the
+    contexts on the GB300 path."""
+    return {'2d': {'predict': predict_2d, 'invert': invert_2d, 'vis_iterator': vis_null_iter},
+            'wprojection': {'predict': predict_2d, 'invert': invert_2d, 'vis_iterator': vis_null_iter},
+            'wstack': {'predict': predict_wstack_single, 'invert': invert_wstack_single,
+                       'vis_iterator': vis_wslice_iter}}
+
+
+def imaging_context(context='2d'):
+    contexts = imaging_contexts()
+    assert context in contexts.keys(), context
+    return contexts[context]
+
+
+def invert_list_serial_workflow(vis_list, template_model_imagelist, dopsf=False, normalize=True, facets=1,
+                                vis_slices=1, context='2d', gcfcf=None, precision=None, **kwargs):
+    """``imaging_serial.py:125-216`` for facets == 1: one (image, sumwt) per vis.
+    The 'wstack' context runs all slices in one batched pass."""
+    if facets != 1:
+        raise NotImplementedError('facets are outside the GB300 path')
+    if not isinstance(template_model_imagelist, (list, tuple)):
+        template_model_imagelist = [template_model_imagelist]
+    imaging_context(context)
+    if gcfcf is None:
+        gcfcf = [create_pswf_convolutionfunction(template_model_imagelist[0])]
+    out = []
+    for i, vis in enumerate(vis_list):
+        g = gcfcf[i] if len(gcfcf) > 1 else gcfcf[0]
+        im = template_model_imagelist[i]
+        if context == 'wstack':
+            if not normalize:
+                raise NotImplementedError('the serial w-stack workflow with normalize=False weights unnormalised '
+                                          'slice images by their sumwt; only normalize=True is on the GB300 path')
+            out.append(invert_wstack(vis, im, vis_slices, dopsf=dopsf, normalize=True, gcfcf=g,
+                                     precision=precision))
+        else:
+            out.append(invert_2d(vis, im, dopsf=dopsf, normalize=normalize, gcfcf=g, precision=precision))
+    return out
+
+
+def predict_list_serial_workflow(vis_list, model_imagelist, context, vis_slices=1, facets=1, gcfcf=None,
+                                 precision=None, **kwargs):
+    """``imaging_serial.py:41-122`` for facets == 1: predicted copies of each vis."""
+    if facets != 1:
+        raise NotImplementedError('facets are outside the GB300 path')
+    imaging_context(context)
+    if gcfcf is None:
+        gcfcf = [create_pswf_convolutionfunction(m) for m in model_imagelist]
+    out = []
+    for i, vis in enumerate(vis_list):
+        g = gcfcf[i] if len(gcfcf) > 1 else gcfcf[0]
+        if context == 'wstack':
+            out.append(predict_wstack(vis, model_imagelist[i], vis_slices, gcfcf=g, precision=precision))
+        else:
+            out.append(predict_2d(vis, model_imagelist[i], gcfcf=g, precision=precision))
+    return out

@@ -117,6 +117,12 @@ int arlgpu_degrid_planned(int64_t nvis, int precision, const void *cf, const arl
                           const arlgpu_grid_desc *gd, void *vis_out, const void *workspace,
                           size_t workspace_bytes, void *stream);
 
+/* Mean w of the rows that a plan assigned to each grid w-plane (the slice mean
+ * numpy.average(vis.w) of invert/predict_wstack_single, wstack_single.py:43,83);
+ * wmean: [gd->nw] float64 (0 for empty planes).  Same nvis / gd / cd as the plan. */
+int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd,
+                             const void *workspace, size_t workspace_bytes, double *wmean, void *stream);
+
 /* ---- a3: degrid_visibility_from_griddata (gridding.py:233-267) ----
  * vis_out[r,p] = sum_ij grid[c,p,zg,v-S/2+j,u-S/2+i] * cf[c,p,zc,dv,du,j,i]; rejected rows get 0. */
 int arlgpu_degrid(const double *uvw, const double *frequency, int64_t nvis, int precision,
@@ -137,6 +143,22 @@ int arlgpu_fft_grid_to_image(const void *grid, const arlgpu_grid_desc *gd, int p
  * grid[c,p,z] = fftshift(fft2(ifftshift(image * gcf))) for every w-plane z. */
 int arlgpu_fft_image_to_grid(const double *image, const double *gcf, const arlgpu_grid_desc *gd,
                              int precision, void *grid, void *stream);
+
+/* ---- a14: w-stacking, all slices at once (imaging/wstack_single.py:26-96,
+ * workflows/serial/imaging/imaging_serial.py:186-197) ----
+ * The grid holds one w-plane per slice (gd->nw = number of slices, gridded with a
+ * plan whose WW axis bins rows into slices); wmean[s] is slice s's mean w and
+ * cellsize the image cell (radians).
+ * arlgpu_wstack_grid_to_image: image = gcf * sum_s Re(wbeam(wmean[s]) * ifft_s) * nx*ny / sumwt,
+ *   i.e. the sumwt-weighted sum of the slices' invert_wstack_single images divided by
+ *   the total sumwt [nchan][npol]; the grid is used as FFT scratch and destroyed.
+ * arlgpu_wstack_image_to_grid: plane s = fft(conj(wbeam(wmean[s])) * image * gcf), so one
+ *   degrid over all rows is predict_wstack_single summed over the slices. */
+int arlgpu_wstack_grid_to_image(void *grid, const arlgpu_grid_desc *gd, int precision, const double *gcf,
+                                const double *wmean, double cellsize, const double *sumwt, double *image,
+                                void *stream);
+int arlgpu_wstack_image_to_grid(const double *image, const double *gcf, const double *wmean, double cellsize,
+                                const arlgpu_grid_desc *gd, int precision, void *grid, void *stream);
 
 /* ---- a7/a8: create_pswf_convolutionfunction (griddata/kernels.py:52-97), FP64 ----
  * cf_out: [O][O][S][S] complex128 (one plane; ARL broadcasts it over chan/pol);
@@ -161,6 +183,17 @@ int arlgpu_apply_gains(void *vis, int64_t nvis, int32_t npol, int precision, con
  * vis[r,:] *= exp(+/-2 pi i (u l + v m + w (n - 1))), n = sqrt(1 - l^2 - m^2); inverse selects +. */
 int arlgpu_phaserotate(void *vis, const double *uvw, int64_t nvis, int32_t npol, int precision,
                        double l, double m, int inverse, void *stream);
+
+/* ---- chi^2 of a gain-corrupted model and its gradients (the g_i g_j* convention
+ * of apply_gaintable, calibration/operations.py:134-137; no reference counterpart
+ * for the derivatives) ----
+ * chi2 = sum w |vobs - g[a2] conj(g[a1]) model|^2 (weight may be NULL = 1), written
+ * to the device double *chi2.  grad_model (may be NULL) = d chi2 / d conj(model)
+ * [nvis][npol] in the precision's complex type; grad_gains (may be NULL) =
+ * d chi2 / d conj(g) [nant] complex128.  gains: [nant] complex128. */
+int arlgpu_gain_chi2(const void *vobs, const void *model, const double *weight, int64_t nvis, int32_t npol,
+                     int precision, const int32_t *a1, const int32_t *a2, const void *gains, int32_t nant,
+                     double *chi2, void *grad_model, void *grad_gains, void *stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,124 @@
+"""Gradients of predict / invert / gain chi^2 through the adjoint kernels:
+torch.autograd.gradcheck, central finite differences (h = 1e-4, relative
+error <= 1e-4) and a dense-DFT reference gradient."""
+import numpy
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module', autouse=True)
+def need_cuda(arl):
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+
+
+def _setup(arl, N=48, cell=8e-3, n=400, nant=8, seed=3, wzero=False, precision='fp64'):
+    rng = numpy.random.default_rng(seed)
+    O, S = 8, 8
+    im = arl.create_image(npixel=N, cellsize=cell, frequency=numpy.array([1e8]), channel_bandwidth=numpy.array([1e6]),
+                          phasecentre=arl.PhaseCentre(0.0, -45.0))
+    gcfcf = arl.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    lim = (N // 2 - S // 2 - 2) / (N * cell)
+    uvw = numpy.stack([rng.uniform(-lim, lim, n), rng.uniform(-lim, lim, n),
+                       numpy.zeros(n) if wzero else rng.uniform(-20, 20, n)], axis=1)
+    a1 = rng.integers(0, nant - 1, n)
+    a2 = numpy.minimum(a1 + rng.integers(1, nant, n), nant - 1)
+    a2 = numpy.where(a2 == a1, a1 + 1, a2)
+    vis = arl.Visibility(uvw=uvw, frequency=numpy.full(n, 1e8), vis=numpy.zeros((n, 1)), weight=numpy.ones((n, 1)),
+                         antenna1=a1, antenna2=a2)
+    op = arl.autograd.GriddingOperator(vis, im, gcfcf, precision=precision)
+    dev = op.device
+    img = numpy.zeros((1, 1, N, N))
+    for _ in range(6):
+        img[0, 0, rng.integers(N // 4, 3 * N // 4), rng.integers(N // 4, 3 * N // 4)] = rng.uniform(0.5, 2)
+    gains = (1 + 0.1 * rng.normal(size=nant)) * numpy.exp(1j * rng.uniform(-numpy.pi, numpy.pi, nant))
+    x = torch.as_tensor(img, device=dev)
+    g = torch.as_tensor(gains, device=dev)
+    t1 = torch.as_tensor(a1.astype(numpy.int32), device=dev)
+    t2 = torch.as_tensor(a2.astype(numpy.int32), device=dev)
+    m = op.predict(x)
+    gg = (g[t2] * torch.conj(g[t1]))[:, None]
+    vobs = gg * m.to(torch.complex128) + 0.01 * torch.as_tensor(
+        rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1)), device=dev)
+    return dict(op=op, x=x, g=g, a1=t1, a2=t2, vobs=vobs, uvw=uvw, N=N, cell=cell, im=im)
+
+
+def test_predict_and_invert_gradcheck(arl):
+    s = _setup(arl, N=32, n=150)
+    op = s['op']
+    x = (0.3 * torch.randn((1, 1, 32, 32), dtype=torch.float64, device=op.device)).requires_grad_(True)
+    assert torch.autograd.gradcheck(lambda t: arl.autograd.Predict.apply(t, op), (x,), eps=1e-6, atol=1e-7,
+                                    rtol=1e-5, fast_mode=True)
+    v = (torch.randn((op.n, 1), dtype=torch.complex128, device=op.device)).requires_grad_(True)
+    assert torch.autograd.gradcheck(lambda t: arl.autograd.Invert.apply(t, op), (v,), eps=1e-6, atol=1e-7,
+                                    rtol=1e-5, fast_mode=True)
+
+
+def test_chi2_gradients_vs_finite_differences(arl):
+    s = _setup(arl)
+    op, x, g = s['op'], s['x'], s['g']
+    args = (s['vobs'], op, s['a1'], s['a2'])
+    c, gx, gg = arl.autograd.gain_chi2_step(x, g, *args)
+    h = 1e-4
+
+    def f(xx, gg_):
+        with torch.no_grad():
+            return float(arl.autograd.chi2(xx, gg_, *args))
+
+    rng = numpy.random.default_rng(0)
+    N = s['N']
+    worst = 0.0
+    scale_x = float(gx.abs().max())
+    for _ in range(12):
+        i, j = rng.integers(0, N, 2)
+        e = torch.zeros_like(x)
+        e[0, 0, i, j] = h
+        fd = (f(x + e, g) - f(x - e, g)) / (2 * h)
+        worst = max(worst, abs(fd - float(gx[0, 0, i, j])) / scale_x)
+    assert worst <= 1e-4, worst
+    scale_g = float(gg.abs().max())
+    worst = 0.0
+    for a in range(g.shape[0]):
+        for d, part in ((1.0, 'real'), (1j, 'imag')):
+            e = torch.zeros_like(g)
+            e[a] = h * d
+            fd = (f(x, g + e) - f(x, g - e)) / (2 * h)
+            an = float(getattr(gg[a], part))
+            worst = max(worst, abs(fd - an) / scale_g)
+    assert worst <= 1e-4, worst
+
+
+def test_chi2_fp32c_gradients_close_to_fp64(arl):
+    s64 = _setup(arl, precision='fp64')
+    s32 = _setup(arl, precision='fp32c')
+    r64 = arl.autograd.gain_chi2_step(s64['x'], s64['g'], s64['vobs'], s64['op'], s64['a1'], s64['a2'])
+    r32 = arl.autograd.gain_chi2_step(s32['x'], s32['g'], s32['vobs'], s32['op'], s32['a1'], s32['a2'])
+    for a, b in zip(r32, r64):
+        assert float((a.to(b.dtype) - b).abs().max() / b.abs().max()) < 1e-4
+
+
+def test_image_gradient_vs_dense_dft(arl):
+    """Gridded chi^2 gradient against a dense direct-Fourier-transform predict on
+    a 64 x 64 image (w = 0 so both model the same 2-D transform).  The gridding
+    approximation (PSWF support 8, oversampling 8) bounds the agreement."""
+    s = _setup(arl, N=64, cell=6e-3, n=500, wzero=True)
+    op, x, g = s['op'], s['x'], s['g']
+    _, gx, _ = arl.autograd.gain_chi2_step(x, g, s['vobs'], op, s['a1'], s['a2'])
+    N, cell = s['N'], s['cell']
+    dev = op.device
+    l = -(torch.arange(N, dtype=torch.float64, device=dev) - N // 2) * cell
+    m = (torch.arange(N, dtype=torch.float64, device=dev) - N // 2) * cell
+    L = l[None, :].expand(N, N).reshape(-1)
+    M = m[:, None].expand(N, N).reshape(-1)
+    uvw = torch.as_tensor(s['uvw'], device=dev)
+    A = torch.exp(-2j * numpy.pi * (uvw[:, 0:1] * L[None, :] + uvw[:, 1:2] * M[None, :]))
+    xx = x.detach().reshape(-1).clone().requires_grad_(True)
+    gains = g[s['a2']] * torch.conj(g[s['a1']])
+    r = s['vobs'][:, 0] - gains * (A @ xx.to(torch.complex128))
+    (r.abs() ** 2).sum().backward()
+    gd = xx.grad.reshape(1, 1, N, N)
+    inner = slice(N // 4, 3 * N // 4)
+    err = float((gx - gd)[..., inner, inner].abs().max() / gd[..., inner, inner].abs().max())
+    assert err < 2e-2, err

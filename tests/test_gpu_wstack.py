@@ -1,0 +1,91 @@
+"""W-stacking on the GPU against the reference's serial w-stack workflow
+(golden fixture) and the oracle."""
+import numpy
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+TOL = {'fp64': 1e-10, 'fp32c': 1e-5}  # outputs pass through an FFT
+
+
+def rel(a, b):
+    return float(numpy.max(numpy.abs(numpy.asarray(a) - b)) / numpy.max(numpy.abs(b)))
+
+
+@pytest.fixture(scope='module', autouse=True)
+def need_cuda(arl):
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+
+
+def _case(arl, d):
+    im = arl.create_image(npixel=int(d['N']), cellsize=float(d['cell']), frequency=numpy.array([1e8]),
+                          channel_bandwidth=numpy.array([1e6]), phasecentre=arl.PhaseCentre(0.0, -45.0))
+    gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=int(d['O']), support=int(d['S']))
+    vis = arl.Visibility(uvw=d['uvw'], frequency=d['frequency'], vis=d['vis'], weight=d['wt'], imaging_weight=d['wt'])
+    vis.phasecentre = arl.PhaseCentre(0.0, -45.0)
+    return im, gcf, cf, vis
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
+def test_wstack_workflow_matches_reference(arl, golden, precision):
+    d = golden('ref_wstack.npz')
+    im, gcf, cf, vis = _case(arl, d)
+    K = int(d['K'])
+    (dirty, sumwt), = arl.imaging.invert_list_serial_workflow([vis], [im], context='wstack', vis_slices=K,
+                                                               gcfcf=[(gcf, cf)], precision=precision)
+    assert rel(dirty.data, d['dirty']) < TOL[precision]
+    assert numpy.allclose(sumwt, d['sumwt'], rtol=1e-12)
+    model = arl.create_image_from_array(d['model'], im.wcs, im.polarisation_frame)
+    (pv,) = arl.imaging.predict_list_serial_workflow([vis], [model], context='wstack', vis_slices=K,
+                                                      gcfcf=[(gcf, cf)], precision=precision)
+    assert rel(pv.vis, d['predict']) < TOL[precision]
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
+def test_wstack_single_matches_oracle(arl, oracle, golden, precision):
+    d = golden('ref_wstack.npz')
+    im, gcf, cf, vis = _case(arl, d)
+    N, cell = int(d['N']), float(d['cell'])
+    img = oracle.image_geometry(N, cell)
+    cax = oracle.cf_axes(img, int(d['O']), int(d['S']))
+    ocf = oracle.create_pswf_cf(1, 1, N, N, int(d['O']), int(d['S']))[1]
+    ogcf = oracle.pswf_gcf(N)[None, None]
+    # one slice: all rows, w-beam of their mean w
+    uvw = d['uvw'].copy()
+    wav = numpy.average(uvw[:, 2])
+    uvw[:, 2] -= wav
+    ref, sw = oracle.invert_2d(uvw, d['frequency'], d['vis'], d['wt'], img, ogcf, ocf, cax)
+    wb = oracle.w_term_image(N, cell, wav)
+    want = wb.real * ref.real - wb.imag * ref.imag
+    got, gsw = arl.imaging.invert_wstack_single(vis, im, False, gcfcf=(gcf, cf), precision=precision)
+    assert rel(got.data, want) < TOL[precision]
+    model = arl.create_image_from_array(d['model'], im.wcs, im.polarisation_frame)
+    vr = oracle.predict_2d(uvw, d['frequency'], wb.real * d['model'], img, ogcf, ocf, cax)
+    vi = oracle.predict_2d(uvw, d['frequency'], wb.imag * d['model'], img, ogcf, ocf, cax)
+    pv = arl.imaging.predict_wstack_single(vis, model, gcfcf=(gcf, cf), precision=precision)
+    assert rel(pv.vis, vr - 1j * vi) < TOL[precision]
+
+
+def test_wstack_many_slices_vs_oracle(arl, oracle):
+    """12 slices, 2 channels imaged together (MFS through one wide image channel)."""
+    rng = numpy.random.default_rng(8)
+    N, cell, O, S, K, n = 96, 6e-3, 8, 8, 12, 4000
+    im = arl.create_image(npixel=N, cellsize=cell, frequency=numpy.array([1.05e8]), channel_bandwidth=numpy.array([1e8]),
+                          phasecentre=arl.PhaseCentre(0.0, -45.0))
+    gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    lim = (N // 2 - S // 2 - 2) / (N * cell)
+    uvw = numpy.stack([rng.uniform(-lim, lim, n), rng.uniform(-lim, lim, n), rng.uniform(-300, 300, n)], axis=1)
+    freq = rng.choice([1.0e8, 1.1e8], n)
+    v = rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1))
+    wt = numpy.ones((n, 1))
+    vis = arl.Visibility(uvw=uvw, frequency=freq, vis=v, weight=wt, imaging_weight=wt)
+    vis.phasecentre = arl.PhaseCentre(0.0, -45.0)
+    img = oracle.image_geometry(N, cell, 1, 1, 1.05e8, 1e8)
+    cax = oracle.cf_axes(img, O, S)
+    ocf = oracle.create_pswf_cf(1, 1, N, N, O, S)[1]
+    want, wsw = oracle.invert_wstack(uvw, freq, v, wt, img, oracle.pswf_gcf(N)[None, None], ocf, cax, K, cell)
+    for p in ('fp64', 'fp32c'):
+        got, sw = arl.imaging.invert_wstack(vis, im, K, gcfcf=(gcf, cf), precision=p)
+        assert rel(got.data, want) < TOL[p]
+        assert numpy.allclose(sw, wsw)
