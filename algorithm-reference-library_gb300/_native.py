@@ -43,13 +43,16 @@ SIGNATURES = {
     'arlgpu_grid': (ctypes.c_int, [_vp, _vp, _vp, _vp, _i64, ctypes.c_int, _vp, _P(CfDesc), _vp, _P(GridDesc),
                                    _vp, _vp, _vp, _sz, _vp]),
     'arlgpu_kernel_launches': (ctypes.c_ulonglong, []),
+    'arlgpu_set_tuning': (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    'arlgpu_get_tuning': (ctypes.c_int, [ctypes.c_char_p, _P(ctypes.c_int)]),
     'arlgpu_plan_build': (ctypes.c_int, [_vp, _vp, _i64, _P(GridDesc), _P(CfDesc), _vp, _sz, _vp, _vp]),
     'arlgpu_grid_planned': (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp, _P(CfDesc), _vp, _P(GridDesc), _vp,
                                            _vp, _sz, _vp]),
     'arlgpu_degrid_planned': (ctypes.c_int, [_i64, ctypes.c_int, _vp, _P(CfDesc), _vp, _P(GridDesc), _vp, _vp, _sz,
                                              _vp]),
     'arlgpu_plan_plane_mean_w': (ctypes.c_int, [_vp, _i64, _P(GridDesc), _P(CfDesc), _vp, _sz, _vp, _vp]),
-    'arlgpu_wstack_grid_to_image': (ctypes.c_int, [_vp, _P(GridDesc), ctypes.c_int, _vp, _vp, _f64, _vp, _vp, _vp]),
+    'arlgpu_wstack_grid_to_image': (ctypes.c_int, [_vp, _P(GridDesc), ctypes.c_int, _vp, _vp, _f64, _vp, _vp, _vp,
+                                                   _vp]),
     'arlgpu_wstack_image_to_grid': (ctypes.c_int, [_vp, _vp, _vp, _f64, _P(GridDesc), ctypes.c_int, _vp, _vp]),
     'arlgpu_degrid': (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp, _P(CfDesc), _vp, _P(GridDesc), _vp, _vp,
                                      _vp, _sz, _vp]),

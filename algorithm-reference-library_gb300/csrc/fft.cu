@@ -64,31 +64,27 @@ template <typename CT> __device__ __forceinline__ CT cmk(double a, double b);
 template <> __device__ __forceinline__ float2 cmk<float2>(double a, double b) { return make_float2((float)a, (float)b); }
 template <> __device__ __forceinline__ double2 cmk<double2>(double a, double b) { return make_double2(a, b); }
 
-// buf[b, y, x] = chk * sum_z grid[b, z, y, x]
+// buf[b, y, x] = chk * sum_z grid[b, z, y, x], summed and stored in FP64
 template <typename CT>
-__global__ void k_pre_g2i(const CT *__restrict__ grid, int nb, int nw, int ny, int nx, CT *__restrict__ buf) {
+__global__ void k_pre_g2i(const CT *__restrict__ grid, int nb, int nw, int ny, int nx, double2 *__restrict__ buf) {
   const int64_t plane = (int64_t)ny * nx;
   const int64_t total = (int64_t)nb * plane;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / plane, yx = i - b * plane;
     const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
     const CT *src = grid + b * nw * plane + yx;
-    CT s = src[0];
+    double sx = src[0].x, sy = src[0].y;
     for (int z = 1; z < nw; ++z) {
-      CT t = src[z * plane];
-      s.x += t.x;
-      s.y += t.y;
+      sx += (double)src[z * plane].x;
+      sy += (double)src[z * plane].y;
     }
-    const float sg = chk_sign(y, x);
-    s.x *= sg;
-    s.y *= sg;
-    buf[i] = s;
+    const double sg = chk_sign(y, x);
+    buf[i] = make_double2(sx * sg, sy * sg);
   }
 }
 
 // image = part(buf * chk * s) * gcf  [/ sumwt]
-template <typename CT>
-__global__ void k_post_g2i(const CT *__restrict__ buf, int nb, int ny, int nx, float s, const double *__restrict__ gcf,
+__global__ void k_post_g2i(const double2 *__restrict__ buf, int nb, int ny, int nx, float s, const double *__restrict__ gcf,
                            const double *__restrict__ sumwt, double *__restrict__ im_re, double *__restrict__ im_im) {
   const int64_t plane = (int64_t)ny * nx;
   const int64_t total = (int64_t)nb * plane;
@@ -97,8 +93,8 @@ __global__ void k_post_g2i(const CT *__restrict__ buf, int nb, int ny, int nx, f
     const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
     const double sg = (double)(chk_sign(y, x) * s);
     const double g = gcf[i];
-    double re = (double)buf[i].x * sg * g;
-    double im = (double)buf[i].y * sg * g;
+    double re = buf[i].x * sg * g;
+    double im = buf[i].y * sg * g;
     if (sumwt) {
       const double w = sumwt[b];
       if (w > 0.0) {
@@ -163,21 +159,25 @@ int exec_c2c<double2>(cufftHandle h, double2 *data, int dir) {
   return r == CUFFT_SUCCESS ? ARLGPU_OK : cufft_fail(r, "cufftExecZ2Z");
 }
 
+// The inverse transform runs in FP64 for both precisions: the grid correction
+// multiplies the transform's rounding error by up to max(gcf) / min(gcf)
+// (~6e4 at the edge of a PSWF-corrected image), so an FP32 transform would
+// leave ~1e-3 relative errors in the image whatever the gridder's accuracy.
 template <typename CT>
 static int g2i(const CT *grid, const arlgpu_grid_desc *gd, const double *gcf, const double *sumwt, double *re,
-               double *im, CT *buf, cudaStream_t st) {
+               double *im, double2 *buf, cudaStream_t st) {
   const int nb = gd->nchan * gd->npol, ny = gd->ny, nx = gd->nx;
   const int64_t total = (int64_t)nb * ny * nx;
   cufftHandle h;
-  ARL_TRY(get_plan(ny, nx, nb, (long long)ny * nx, sizeof(CT) == 8 ? CUFFT_C2C : CUFFT_Z2Z, &h));
+  ARL_TRY(get_plan(ny, nx, nb, (long long)ny * nx, CUFFT_Z2Z, &h));
   k_pre_g2i<CT><<<grid_blocks(total), 256, 0, st>>>(grid, nb, gd->nw, ny, nx, buf);
   count_launch(1);
   ARL_LAUNCH_CHECK();
   cufftResult r = cufftSetStream(h, st);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
-  ARL_TRY(exec_c2c<CT>(h, buf, CUFFT_INVERSE));
+  ARL_TRY(exec_c2c<double2>(h, buf, CUFFT_INVERSE));
   const float s = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
-  k_post_g2i<CT><<<grid_blocks(total), 256, 0, st>>>(buf, nb, ny, nx, s, gcf, sumwt, re, im);
+  k_post_g2i<<<grid_blocks(total), 256, 0, st>>>(buf, nb, ny, nx, s, gcf, sumwt, re, im);
   count_launch(1);
   ARL_LAUNCH_CHECK();
   return ARLGPU_OK;
@@ -225,7 +225,7 @@ extern "C" int arlgpu_fft_grid_to_image(const void *grid, const arlgpu_grid_desc
     return g2i<double2>(static_cast<const double2 *>(grid), gd, gcf, sumwt, image_real, image_imag,
                         static_cast<double2 *>(fftbuf), st);
   return g2i<float2>(static_cast<const float2 *>(grid), gd, gcf, sumwt, image_real, image_imag,
-                     static_cast<float2 *>(fftbuf), st);
+                     static_cast<double2 *>(fftbuf), st);
 }
 
 extern "C" int arlgpu_fft_image_to_grid(const double *image, const double *gcf, const arlgpu_grid_desc *gd,

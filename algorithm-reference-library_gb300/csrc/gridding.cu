@@ -44,6 +44,11 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
 const char *last_error() { return g_last_error.c_str(); }
 
 static std::atomic<unsigned long long> g_launches{0};
+
+// Kernel-variant choices (set by the autotuner through arlgpu_set_tuning).
+static std::atomic<int> g_tune_grid_kernel{0};    // 0: shared atomics + TwoSum, 1: band owner
+static std::atomic<int> g_tune_degrid_kernel{0};  // 0: warp per row, 1: batched rows
+static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automatic)
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------
@@ -429,6 +434,190 @@ k_grid(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sid
   }
 }
 
+// Per-cell compensated accumulation by the cell's single owner thread (no
+// atomics): Kahan for FP32, a plain add for FP64.
+template <typename R> struct OwnerAcc;
+template <> struct OwnerAcc<float> {
+  __device__ static __forceinline__ void add(float2 *sum, float2 *comp, float2 v) {
+    float2 s = *sum, c = *comp;
+    float y = v.x - c.x, t = s.x + y;
+    c.x = (t - s.x) - y;
+    s.x = t;
+    y = v.y - c.y;
+    t = s.y + y;
+    c.y = (t - s.y) - y;
+    s.y = t;
+    *sum = s;
+    *comp = c;
+  }
+};
+template <> struct OwnerAcc<double> {
+  __device__ static __forceinline__ void add(double2 *sum, double2 *, double2 v) {
+    double2 s = *sum;
+    s.x += v.x;
+    s.y += v.y;
+    *sum = s;
+  }
+};
+
+// Row data staged in shared memory for a batch of rows.
+template <typename CT> struct StagedRow {
+  RowMap m;
+  CT vw[4];
+};
+
+// K3 (band-owner variant): one CTA per chunk of sorted rows.  For each bin run
+// the (T + S)^2 subgrid lives in shared memory and warp w owns subgrid rows
+// [w B, w B + B), B = SG / NW.  Every warp walks every row of the run (their
+// metadata staged once per batch in shared memory) and adds only the window
+// taps that fall in its band, so each cell has exactly one writer: a plain
+// read-modify-write with a per-cell Kahan term, in a fixed row order.  Bin
+// runs with few rows skip the subgrid and add their taps to the grid directly.
+template <typename R, int NW>
+__global__ void __launch_bounds__(NW * 32)
+k_grid_band(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
+            const uint32_t *__restrict__ off, uint32_t chunk,
+            const typename VisT<R>::C *__restrict__ vis, const typename VisT<R>::W *__restrict__ wt,
+            const typename Cplx<R>::T *__restrict__ cf, typename Cplx<R>::T *__restrict__ grid,
+            double *__restrict__ sumwt) {
+  using CT = typename Cplx<R>::T;
+  constexpr int BATCH = NW * 32;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int SG = g.SG, SG2 = SG * SG, npol = g.npol;
+  StagedRow<CT> *rows = reinterpret_cast<StagedRow<CT> *>(smraw);
+  CT *sub = reinterpret_cast<CT *>(smraw + sizeof(StagedRow<CT>) * BATCH);
+  CT *comp = sub + (size_t)npol * SG2;
+  const uint32_t nvalid = off[g.nbins];
+  const uint32_t c0 = blockIdx.x * chunk;
+  if (c0 >= nvalid) return;
+  const uint32_t c1 = min(c0 + chunk, nvalid);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int S = g.S, O = g.O;
+  const int B = SG / NW, band0 = warp * B;
+  const int64_t plane_elems = (int64_t)g.ny * g.nx;
+
+  uint32_t pos = c0;
+  while (pos < c1) {
+    const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    if (!sg.direct) {
+      for (int k = threadIdx.x; k < npol * SG2 * SmemAcc<R>::kWords; k += blockDim.x) sub[k] = czero<CT>();
+    }
+    double wsum[4] = {0.0, 0.0, 0.0, 0.0};
+    for (uint32_t rb = pos; rb < sg.end; rb += BATCH) {
+      const int nb = (int)min((uint32_t)BATCH, sg.end - rb);
+      __syncthreads();  // previous batch fully consumed (and subgrid zeroed)
+      if ((int)threadIdx.x < nb) {
+        StagedRow<CT> st;
+        st.m = smap[rb + threadIdx.x];
+        const uint32_t idx = sidx[rb + threadIdx.x];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          if (p < npol) {
+            const CT v = vis[(size_t)idx * npol + p];
+            const R w = wt[(size_t)idx * npol + p];
+            st.vw[p].x = v.x * w;
+            st.vw[p].y = v.y * w;
+            wsum[p] += (double)w;
+          }
+        }
+        rows[threadIdx.x] = st;
+      }
+      __syncthreads();
+      for (int k = 0; k < nb; ++k) {
+        const RowMap m = rows[k].m;
+        const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+        const int sz = plane_sz(g, zc);
+        const int toff = (S - sz) >> 1;
+        const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
+        const CT *cfr = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                        ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+        if (sg.direct) {
+          if ((k % NW) != warp) continue;
+          const int n = sz * sz, q = 32 / sz, rr = 32 - q * sz;
+          int j = lane / sz, i = lane - j * sz;
+          for (int t = lane; t < n; t += 32) {
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+              if (p < npol) {
+                const CT vw = rows[k].vw[p];
+                const CT tp = cfr[p * g.cf_pol_stride + j * S + i];
+                CT c;
+                c.x = tp.x * vw.x + tp.y * vw.y;
+                c.y = tp.x * vw.y - tp.y * vw.x;
+                red_global<CT>(grid + ((int64_t)(sg.ch * npol + p) * g.nw + sg.zg) * plane_elems +
+                                   (int64_t)(wv + j) * g.nx + (wu + i),
+                               c);
+              }
+            }
+            i += rr;
+            j += q;
+            if (i >= sz) {
+              i -= sz;
+              ++j;
+            }
+          }
+          continue;
+        }
+        const int lv = wv - sg.v0, lu = wu - sg.u0;
+        const int j0 = max(lv, band0) - lv, j1 = min(lv + sz, band0 + B) - lv;
+        if (j0 >= j1) continue;
+        const int n = (j1 - j0) * sz, q = 32 / sz, rr = 32 - q * sz;
+        int j = j0 + lane / sz, i = lane - (lane / sz) * sz;
+        for (int t = lane; t < n; t += 32) {
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            if (p < npol) {
+              const CT vw = rows[k].vw[p];
+              const CT tp = cfr[p * g.cf_pol_stride + j * S + i];
+              CT c;  // conj(tap) * vw
+              c.x = tp.x * vw.x + tp.y * vw.y;
+              c.y = tp.x * vw.y - tp.y * vw.x;
+              const int cell = p * SG2 + (lv + j) * SG + (lu + i);
+              OwnerAcc<R>::add(sub + cell, comp + cell, c);
+            }
+          }
+          i += rr;
+          j += q;
+          if (i >= sz) {
+            i -= sz;
+            ++j;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    // Weight sums: each row was staged by exactly one thread.
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      if (p < npol) {
+        double s = wsum[p];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0 && s != 0.0) atomicAdd(&sumwt[sg.ch * npol + p], s);
+      }
+    }
+    __syncthreads();
+    if (!sg.direct) {
+      for (int k = threadIdx.x; k < npol * SG2; k += blockDim.x) {
+        CT val = sub[k];
+        if (SmemAcc<R>::kWords == 2) {
+          CT e = comp[k];
+          val.x -= e.x;
+          val.y -= e.y;
+        }
+        if (val.x == (R)0 && val.y == (R)0) continue;
+        const int p = k / SG2, rem = k - p * SG2, y = rem / SG, x = rem - y * SG;
+        const int gy = sg.v0 + y, gx = sg.u0 + x;
+        if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
+        red_global<CT>(grid + ((int64_t)(sg.ch * npol + p) * g.nw + sg.zg) * plane_elems +
+                           (int64_t)gy * g.nx + gx,
+                       val);
+      }
+      __syncthreads();
+    }
+    pos = sg.end;
+  }
+}
+
 template <typename R, int NW>
 __global__ void __launch_bounds__(NW * 32)
 k_degrid(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
@@ -526,6 +715,134 @@ k_degrid(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ s
   }
 }
 
+// K4 (batched variant): as k_degrid, but each warp loads the metadata of 32
+// rows at once (one row per lane, so 32 independent loads are in flight),
+// broadcasts them with shuffles, and runs the tap loop two taps at a time with
+// independent accumulators.
+template <typename R, int NW>
+__global__ void __launch_bounds__(NW * 32)
+k_degrid_batch(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
+               const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
+               const typename Cplx<R>::T *__restrict__ cf, const typename Cplx<R>::T *__restrict__ grid,
+               typename VisT<R>::C *__restrict__ vis_out) {
+  using CT = typename Cplx<R>::T;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int SG = g.SG, SG2 = SG * SG, npol = g.npol;
+  CT *sub = reinterpret_cast<CT *>(smraw);
+  const uint32_t nvalid = off[g.nbins];
+  const uint32_t c0 = blockIdx.x * chunk;
+  if (c0 >= (uint32_t)nvis) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (c0 + chunk > nvalid) {
+    const uint32_t b = max(c0, nvalid), e = min(c0 + chunk, (uint32_t)nvis);
+    for (uint32_t r = b + threadIdx.x; r < e; r += blockDim.x)
+      for (int p = 0; p < npol; ++p) vis_out[(size_t)sidx[r] * npol + p] = czero<CT>();
+    if (c0 >= nvalid) return;
+  }
+  const uint32_t c1 = min(c0 + chunk, nvalid);
+  const int S = g.S, O = g.O;
+  const int64_t plane_elems = (int64_t)g.ny * g.nx;
+
+  uint32_t pos = c0;
+  while (pos < c1) {
+    const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    const CT *gplane = grid + (int64_t)(sg.ch * npol) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems;
+    if (!sg.direct) {
+      for (int k = threadIdx.x; k < npol * SG2; k += blockDim.x) {
+        const int p = k / SG2, rem = k - p * SG2, y = rem / SG, x = rem - y * SG;
+        const int gy = sg.v0 + y, gx = sg.u0 + x;
+        CT val = czero<CT>();
+        if (gy >= 0 && gy < g.ny && gx >= 0 && gx < g.nx)
+          val = gplane[(int64_t)p * g.nw * plane_elems + (int64_t)gy * g.nx + gx];
+        sub[k] = val;
+      }
+      __syncthreads();
+    }
+    for (uint32_t rb = pos + 32 * warp; rb < sg.end; rb += 32 * NW) {
+      const int nb = (int)min(32u, sg.end - rb);
+      RowMap mine;
+      uint32_t myidx = 0;
+      if (lane < nb) {
+        mine = smap[rb + lane];
+        myidx = sidx[rb + lane];
+      }
+      for (int k = 0; k < nb; ++k) {
+        const int pu = __shfl_sync(0xffffffffu, mine.pu, k);
+        const int pv = __shfl_sync(0xffffffffu, mine.pv, k);
+        const uint32_t subf = __shfl_sync(0xffffffffu, mine.sub, k);
+        const uint32_t idx = __shfl_sync(0xffffffffu, myidx, k);
+        const int uf = subf & 0xff, vf = (subf >> 8) & 0xff, zc = subf >> 16;
+        const int sz = plane_sz(g, zc);
+        const int toff = (S - sz) >> 1;
+        const int wu = pu - (sz >> 1), wv = pv - (sz >> 1);
+        const CT *cfr = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                        ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+        const int n = sz * sz, q = 32 / sz, rr = 32 - q * sz;
+        const int lv = wv - sg.v0, lu = wu - sg.u0;
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          if (p >= npol) break;
+          const CT *cp = cfr + p * g.cf_pol_stride;
+          R ax = 0, ay = 0, bx = 0, by = 0;
+          int j = lane / sz, i = lane - j * sz;
+          int t = lane;
+          for (; t + 32 < n; t += 64) {
+            int j2 = j + q, i2 = i + rr;
+            if (i2 >= sz) {
+              i2 -= sz;
+              ++j2;
+            }
+            const CT t1 = cp[j * S + i], t2 = cp[j2 * S + i2];
+            CT g1, g2;
+            if (sg.direct) {
+              const CT *gp = gplane + (int64_t)p * g.nw * plane_elems;
+              g1 = gp[(int64_t)(wv + j) * g.nx + (wu + i)];
+              g2 = gp[(int64_t)(wv + j2) * g.nx + (wu + i2)];
+            } else {
+              g1 = sub[p * SG2 + (lv + j) * SG + (lu + i)];
+              g2 = sub[p * SG2 + (lv + j2) * SG + (lu + i2)];
+            }
+            ax += g1.x * t1.x - g1.y * t1.y;
+            ay += g1.x * t1.y + g1.y * t1.x;
+            bx += g2.x * t2.x - g2.y * t2.y;
+            by += g2.x * t2.y + g2.y * t2.x;
+            j = j2 + q;
+            i = i2 + rr;
+            if (i >= sz) {
+              i -= sz;
+              ++j;
+            }
+          }
+          if (t < n) {
+            const CT t1 = cp[j * S + i];
+            CT g1;
+            if (sg.direct)
+              g1 = gplane[(int64_t)p * g.nw * plane_elems + (int64_t)(wv + j) * g.nx + (wu + i)];
+            else
+              g1 = sub[p * SG2 + (lv + j) * SG + (lu + i)];
+            ax += g1.x * t1.x - g1.y * t1.y;
+            ay += g1.x * t1.y + g1.y * t1.x;
+          }
+          ax += bx;
+          ay += by;
+          for (int o = 16; o > 0; o >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o);
+          }
+          if (lane == 0) {
+            CT out;
+            out.x = ax;
+            out.y = ay;
+            vis_out[(size_t)idx * npol + p] = out;
+          }
+        }
+      }
+    }
+    if (!sg.direct) __syncthreads();
+    pos = sg.end;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
@@ -578,9 +895,13 @@ int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precisio
   // Subgrid edge: 64 cells when npol planes of it (with the FP32 compensation
   // words) fit in 64 KiB of shared memory, else 32.
   const size_t cell = precision == ARLGPU_FP64 ? 16 : 16;  // c128, or c64 sum + c64 comp
-  int SG = 64;
-  if ((size_t)g->npol * SG * SG * cell > 64 * 1024) SG = 32;
+  int SG = g_tune_subgrid.load();
+  if (SG <= 0) {
+    SG = 64;
+    if ((size_t)g->npol * SG * SG * cell > 64 * 1024) SG = 32;
+  }
   if (SG - g->S < 8) SG = ((g->S + 8 + 7) / 8) * 8;
+  SG = (SG + 7) & ~7;  // a multiple of the band-owner warp count
   if ((size_t)g->npol * SG * SG * cell > 200 * 1024)
     return fail(ARLGPU_ERR_UNSUPPORTED, "support %d with %d polarisations needs more shared memory than a CTA has",
                 g->S, g->npol);
@@ -664,6 +985,11 @@ static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const voi
                        const void *cf, void *grid, double *sumwt, cudaStream_t st) {
   size_t smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T) * SmemAcc<R>::kWords;
   auto kern = k_grid<R, kWarps>;
+  if (g_tune_grid_kernel.load() == 1) {
+    kern = k_grid_band<R, kWarps>;
+    smem += sizeof(StagedRow<typename Cplx<R>::T>) * kWarps * 32;
+  }
+  if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   unsigned blocks = (unsigned)((nvis + kChunk - 1) / kChunk);
   if (blocks == 0) return ARLGPU_OK;
@@ -682,6 +1008,7 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
                          void *vis_out, cudaStream_t st) {
   size_t smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T);
   auto kern = k_degrid<R, kWarps>;
+  if (g_tune_degrid_kernel.load() == 1) kern = k_degrid_batch<R, kWarps>;
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   unsigned blocks = (unsigned)((nvis + kChunk - 1) / kChunk);
   if (blocks == 0) return ARLGPU_OK;
@@ -813,6 +1140,26 @@ extern "C" int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const a
   k_plane_mean_w<<<g.nw, 256, 0, static_cast<cudaStream_t>(stream)>>>(uvw, b.sidx, b.offsets, g, wmean);
   ARL_LAUNCH_CHECK();
   count_launch(1);
+  return ARLGPU_OK;
+}
+
+extern "C" int arlgpu_set_tuning(const char *key, int value) {
+  if (!key) return fail(ARLGPU_ERR_INVALID, "null key");
+  const std::string k(key);
+  if (k == "grid_kernel" && (value == 0 || value == 1)) g_tune_grid_kernel = value;
+  else if (k == "degrid_kernel" && (value == 0 || value == 1)) g_tune_degrid_kernel = value;
+  else if (k == "subgrid" && (value == 0 || (value >= 16 && value <= 128))) g_tune_subgrid = value;
+  else return fail(ARLGPU_ERR_INVALID, "unknown tuning key or value: %s = %d", key, value);
+  return ARLGPU_OK;
+}
+
+extern "C" int arlgpu_get_tuning(const char *key, int *value) {
+  if (!key || !value) return fail(ARLGPU_ERR_INVALID, "null argument");
+  const std::string k(key);
+  if (k == "grid_kernel") *value = g_tune_grid_kernel;
+  else if (k == "degrid_kernel") *value = g_tune_degrid_kernel;
+  else if (k == "subgrid") *value = g_tune_subgrid;
+  else return fail(ARLGPU_ERR_INVALID, "unknown tuning key: %s", key);
   return ARLGPU_OK;
 }
 

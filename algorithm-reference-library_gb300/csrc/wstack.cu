@@ -75,25 +75,23 @@ template <> struct WB<double2> {
   __device__ static __forceinline__ double2 at(const Pix &p, double w) { return wb64(p, w); }
 };
 
-// pre-invert: chk sign on every plane (the centred-transform trick)
+// pre-invert: every plane into the FP64 FFT buffer with the chk sign (the
+// centred-transform trick)
 template <typename CT>
-__global__ void k_chk_planes(CT *grid, int64_t nplanes, int ny, int nx) {
+__global__ void k_chk_planes(const CT *grid, int64_t nplanes, int ny, int nx, double2 *buf) {
   const int64_t plane = (int64_t)ny * nx, tot = nplanes * plane;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t yx = i % plane;
     const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
-    if ((x + y) & 1) {
-      CT v = grid[i];
-      v.x = -v.x;
-      v.y = -v.y;
-      grid[i] = v;
-    }
+    const double sg = ((x + y) & 1) ? -1.0 : 1.0;
+    buf[i] = make_double2(sg * (double)grid[i].x, sg * (double)grid[i].y);
   }
 }
 
-// image[b, y, x] = gcf * sum_s Re(wb_s * U_s * chk * s0) / sumwt[b]
+// image[b, y, x] = gcf * sum_s Re(wb_s * U_s * chk * s0) / sumwt[b]; U_s in FP64,
+// the w-beam in the precision of the path (CT)
 template <typename CT>
-__global__ void k_wstack_combine(const CT *__restrict__ grid, int nb, int K, int ny, int nx, float s0, double fov,
+__global__ void k_wstack_combine(const double2 *__restrict__ grid, int nb, int K, int ny, int nx, float s0, double fov,
                                  const double *__restrict__ wmean, const double *__restrict__ gcf,
                                  const double *__restrict__ sumwt, double *__restrict__ image) {
   const int64_t plane = (int64_t)ny * nx, tot = (int64_t)nb * plane;
@@ -104,9 +102,9 @@ __global__ void k_wstack_combine(const CT *__restrict__ grid, int nb, int K, int
     const Pix px = wpix(y, x, nx, fov);
     double acc = 0.0;
     for (int s = 0; s < K; ++s) {
-      const CT u = grid[(b * K + s) * plane + yx];
+      const double2 u = grid[(b * K + s) * plane + yx];
       const double2 wb = WB<CT>::at(px, wmean[s]);
-      acc += wb.x * (double)u.x - wb.y * (double)u.y;
+      acc += wb.x * u.x - wb.y * u.y;
     }
     const double w = sumwt[b];
     image[i] = w > 0.0 ? acc * sg * gcf[i] / w : 0.0;
@@ -163,22 +161,24 @@ static int exec(cufftHandle h, CT *d, int dir) {
   return r == CUFFT_SUCCESS ? ARLGPU_OK : fail(ARLGPU_ERR_CUFFT, "cuFFT exec failed (%d)", (int)r);
 }
 
+// The inverse transforms run in FP64 for both precisions (the grid correction
+// amplifies transform rounding by up to max(gcf) / min(gcf)).
 template <typename CT>
-static int g2i(CT *grid, const arlgpu_grid_desc *gd, const double *gcf, const double *wmean, double fov,
-               const double *sumwt, double *image, cudaStream_t st) {
+static int g2i(const CT *grid, const arlgpu_grid_desc *gd, const double *gcf, const double *wmean, double fov,
+               const double *sumwt, double *image, double2 *buf, cudaStream_t st) {
   const int nb = gd->nchan * gd->npol, K = gd->nw, ny = gd->ny, nx = gd->nx;
   const int64_t nplanes = (int64_t)nb * K;
   if (nplanes > 0x7fffffff) return fail(ARLGPU_ERR_UNSUPPORTED, "too many planes");
   cufftHandle h;
-  ARL_TRY(get_plan(ny, nx, (int)nplanes, (long long)ny * nx, sizeof(CT) == 8 ? CUFFT_C2C : CUFFT_Z2Z, &h));
-  k_chk_planes<CT><<<nblk(nplanes * ny * nx), 256, 0, st>>>(grid, nplanes, ny, nx);
+  ARL_TRY(get_plan(ny, nx, (int)nplanes, (long long)ny * nx, CUFFT_Z2Z, &h));
+  k_chk_planes<CT><<<nblk(nplanes * ny * nx), 256, 0, st>>>(grid, nplanes, ny, nx, buf);
   ARL_LAUNCH_CHECK();
   count_launch(1);
   cufftResult r = cufftSetStream(h, st);
   if (r != CUFFT_SUCCESS) return fail(ARLGPU_ERR_CUFFT, "cufftSetStream failed (%d)", (int)r);
-  ARL_TRY(exec<CT>(h, grid, CUFFT_INVERSE));
+  ARL_TRY(exec<double2>(h, buf, CUFFT_INVERSE));
   const float s0 = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
-  k_wstack_combine<CT><<<nblk((int64_t)nb * ny * nx), 256, 0, st>>>(grid, nb, K, ny, nx, s0, fov, wmean, gcf, sumwt,
+  k_wstack_combine<CT><<<nblk((int64_t)nb * ny * nx), 256, 0, st>>>(buf, nb, K, ny, nx, s0, fov, wmean, gcf, sumwt,
                                                                      image);
   ARL_LAUNCH_CHECK();
   count_launch(1);
@@ -219,15 +219,17 @@ static int check(const arlgpu_grid_desc *gd, int precision) {
 
 using namespace arlgpu;
 
-extern "C" int arlgpu_wstack_grid_to_image(void *grid, const arlgpu_grid_desc *gd, int precision, const double *gcf,
-                                           const double *wmean, double cellsize, const double *sumwt, double *image,
-                                           void *stream) {
+extern "C" int arlgpu_wstack_grid_to_image(const void *grid, const arlgpu_grid_desc *gd, int precision,
+                                           const double *gcf, const double *wmean, double cellsize,
+                                           const double *sumwt, double *image, void *fftbuf, void *stream) {
   ARL_TRY(check(gd, precision));
-  if (!grid || !gcf || !wmean || !sumwt || !image) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  if (!grid || !gcf || !wmean || !sumwt || !image || !fftbuf) return fail(ARLGPU_ERR_INVALID, "null array argument");
   const double fov = gd->nx * cellsize;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (precision == ARLGPU_FP64) return g2i<double2>(static_cast<double2 *>(grid), gd, gcf, wmean, fov, sumwt, image, st);
-  return g2i<float2>(static_cast<float2 *>(grid), gd, gcf, wmean, fov, sumwt, image, st);
+  double2 *buf = static_cast<double2 *>(fftbuf);
+  if (precision == ARLGPU_FP64)
+    return g2i<double2>(static_cast<const double2 *>(grid), gd, gcf, wmean, fov, sumwt, image, buf, st);
+  return g2i<float2>(static_cast<const float2 *>(grid), gd, gcf, wmean, fov, sumwt, image, buf, st);
 }
 
 extern "C" int arlgpu_wstack_image_to_grid(const double *image, const double *gcf, const double *wmean,

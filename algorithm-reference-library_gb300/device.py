@@ -185,13 +185,14 @@ def degrid(uvw, freq, grid_t, cf_t, cd, gd, precision, out=None, n_bad=None, str
 
 
 def fft_grid_to_image(grid_t, gd, gcf_t, precision, sumwt=None, imaginary=False, buf=None, stream=None):
-    """Image (and imaginary part) [nchan, npol, ny, nx] float64 from a device grid."""
+    """Image (and imaginary part) [nchan, npol, ny, nx] float64 from a device grid.
+    ``buf`` is complex128 FFT scratch (a complex128 grid with nw == 1 may be reused)."""
     dev = grid_t.device
     shape = (gd.nchan, gd.npol, gd.ny, gd.nx)
     re = torch.empty(shape, dtype=torch.float64, device=dev)
     im = torch.empty(shape, dtype=torch.float64, device=dev) if imaginary else None
-    if buf is None:
-        buf = torch.empty(shape, dtype=CDTYPE[precision], device=dev)
+    if buf is None or buf.dtype != torch.complex128:
+        buf = torch.empty(shape, dtype=torch.complex128, device=dev)
     nat.call('arlgpu_fft_grid_to_image', nat.ptr(grid_t), ctypes.byref(gd), nat.PRECISIONS[precision],
              nat.ptr(gcf_t), nat.ptr(sumwt), nat.ptr(re), nat.ptr(im), nat.ptr(buf), nat.stream_ptr(stream))
     return re, im

@@ -231,9 +231,10 @@ def invert_wstack(vis, im, vis_slices, dopsf=False, normalize=True, gcfcf=None, 
              nat.ptr(s['ws']), s['ws'].numel(), nat.stream_ptr())
     image = torch.empty((nchan, npol, ny, nx), dtype=torch.float64, device=device)
     norm = sumwt if normalize else torch.ones_like(sumwt)
+    fftbuf = grid_t if precision == 'fp64' else torch.empty(grid_t.shape, dtype=torch.complex128, device=device)
     nat.call('arlgpu_wstack_grid_to_image', nat.ptr(grid_t), ctypes.byref(gd), nat.PRECISIONS[precision],
              nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),
-             nat.stream_ptr())
+             nat.ptr(fftbuf), nat.stream_ptr())
     host = not isinstance(vis, DeviceVisibility)
     out = Image(image.cpu().numpy() if host else image, im.wcs.deepcopy(), im.polarisation_frame)
     return out, (sumwt.cpu().numpy() if host else sumwt)
@@ -307,9 +308,10 @@ def _single_slice_invert(vis, im, dopsf, normalize, gcfcf, precision):
              nat.ptr(s['ws']), s['ws'].numel(), nat.stream_ptr())
     image = torch.empty((nchan, npol, ny, nx), dtype=torch.float64, device=device)
     norm = sumwt if normalize else torch.ones_like(sumwt)
+    fftbuf = grid_t if precision == 'fp64' else torch.empty(grid_t.shape, dtype=torch.complex128, device=device)
     nat.call('arlgpu_wstack_grid_to_image', nat.ptr(grid_t), ctypes.byref(gd), nat.PRECISIONS[precision],
              nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),
-             nat.stream_ptr())
+             nat.ptr(fftbuf), nat.stream_ptr())
     host = not isinstance(vis, DeviceVisibility)
     out = Image(image.cpu().numpy() if host else image, im.wcs.deepcopy(), im.polarisation_frame)
     return out, (sumwt.cpu().numpy() if host else sumwt)

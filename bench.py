@@ -50,6 +50,7 @@ def parse():
     ap.add_argument('--no-fp64', action='store_true', help='skip the FP64 comparison arm')
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline')
     ap.add_argument('--cpu-seconds', type=float, default=12.0, help='CPU-baseline time budget')
+    ap.add_argument('--no-tune', action='store_true', help='keep the library\'s default kernel variants')
     return ap.parse_args()
 
 
@@ -80,11 +81,13 @@ def barrier(torch, world):
             tdist.barrier()
 
 
-def max_over_ranks(torch, world, x):
+def max_over_ranks(torch, world, x, device=None):
     if world == 1:
         return x
     import torch.distributed as tdist
-    t = torch.tensor([x], dtype=torch.float64, device='cuda' if torch.cuda.is_available() else 'cpu')
+    if device is None:
+        device = 'cuda' if torch.cuda.is_available() else 'cpu'
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
     return float(t.item())
 
@@ -415,6 +418,14 @@ def arm_gb300(args, torch, world, rank, local):
     w = sim.make_workload(args.workload, device=device)
     w['name'] = args.workload
     n = w['uvw'].shape[0]
+    tuned = None
+    if not args.no_tune:
+        # Autotune on this workload before any timing (untimed set-up).
+        c0 = build_context(arl, torch, w, 'fp32c', device)
+        best, table = arl.tune.autotune(c0['uvw'], c0['freq'], c0['vis'], c0['wt'], c0['cf_t'], c0['cd'], c0['gd'],
+                                        'fp32c')
+        tuned = {'choice': best, 'ms_per_step': {'%d/%d/%d' % k: round(v, 4) for k, v in table.items()}}
+        del c0
     ctx = build_context(arl, torch, w, 'fp32c', device)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
     clocks = Clocks(local)
@@ -477,6 +488,7 @@ def arm_gb300(args, torch, world, rank, local):
                 'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_ms, 'path': 'C ABI, pinned host buffers'},
         'gpu_launches': r['launches'],
         'clocks': clk,
+        'autotune': tuned,
     }
     line.update(out)
     if rank == 0:

@@ -79,6 +79,16 @@ const char *arlgpu_last_error(void);
  * not cuFFT's), for launch accounting. */
 unsigned long long arlgpu_kernel_launches(void);
 
+/* Kernel-variant selection (the autotuner's knobs; process-wide):
+ *   "grid_kernel"   0 = shared-memory atomics with TwoSum compensation (default),
+ *                   1 = band owner: each warp owns a band of the subgrid, plain
+ *                       read-modify-write with a per-cell Kahan term
+ *   "degrid_kernel" 0 = one warp per row (default), 1 = 32-row batches per warp
+ *   "subgrid"       subgrid edge in cells (16..128), 0 = automatic
+ * No reference counterpart (ARL has one Python loop per function). */
+int arlgpu_set_tuning(const char *key, int value);
+int arlgpu_get_tuning(const char *key, int *value);
+
 /* ---- a1: convolution_mapping (processing_components/griddata/gridding.py:24-96) ----
  * Writes pu, pu_off, pv, pv_off, pwg, pwc, pfreq (int32 [nvis] each) and the
  * number of rows whose S x S window, plane or channel falls outside the grid /
@@ -133,8 +143,10 @@ int arlgpu_degrid(const double *uvw, const double *frequency, int64_t nvis, int 
 /* ---- a4: fft_griddata_to_image (gridding.py:270-289) + normalize_sumwt (imaging/base.py:84-101) ----
  * image = Re/Im[ fftshift(ifft2(ifftshift(sum_w grid))) ] * gcf * nx*ny, divided by
  * sumwt[c,p] when sumwt != NULL (zero where sumwt <= 0).  image_imag may be NULL.
- * `fftbuf` is caller scratch of nchan*npol*ny*nx complex elements of the precision;
- * the grid itself may be passed as fftbuf when nw == 1 and the grid may be destroyed. */
+ * `fftbuf` is caller scratch of nchan*npol*ny*nx complex128 elements: the transform
+ * runs in FP64 for both precisions, because the grid correction multiplies its
+ * rounding error by up to max(gcf)/min(gcf).  With precision FP64 and nw == 1 the
+ * grid itself may be passed as fftbuf (it is then destroyed). */
 int arlgpu_fft_grid_to_image(const void *grid, const arlgpu_grid_desc *gd, int precision,
                              const double *gcf, const double *sumwt, double *image_real,
                              double *image_imag, void *fftbuf, void *stream);
@@ -151,12 +163,13 @@ int arlgpu_fft_image_to_grid(const double *image, const double *gcf, const arlgp
  * cellsize the image cell (radians).
  * arlgpu_wstack_grid_to_image: image = gcf * sum_s Re(wbeam(wmean[s]) * ifft_s) * nx*ny / sumwt,
  *   i.e. the sumwt-weighted sum of the slices' invert_wstack_single images divided by
- *   the total sumwt [nchan][npol]; the grid is used as FFT scratch and destroyed.
+ *   the total sumwt [nchan][npol].  fftbuf: nchan*npol*nw*ny*nx complex128 scratch (the
+ *   transforms run in FP64); with precision FP64 it may be the grid itself.
  * arlgpu_wstack_image_to_grid: plane s = fft(conj(wbeam(wmean[s])) * image * gcf), so one
  *   degrid over all rows is predict_wstack_single summed over the slices. */
-int arlgpu_wstack_grid_to_image(void *grid, const arlgpu_grid_desc *gd, int precision, const double *gcf,
+int arlgpu_wstack_grid_to_image(const void *grid, const arlgpu_grid_desc *gd, int precision, const double *gcf,
                                 const double *wmean, double cellsize, const double *sumwt, double *image,
-                                void *stream);
+                                void *fftbuf, void *stream);
 int arlgpu_wstack_image_to_grid(const double *image, const double *gcf, const double *wmean, double cellsize,
                                 const arlgpu_grid_desc *gd, int precision, void *grid, void *stream);
 

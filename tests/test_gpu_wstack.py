@@ -4,6 +4,8 @@ import numpy
 import pytest
 import torch
 
+from helpers import assert_image
+
 pytestmark = pytest.mark.gpu
 TOL = {'fp64': 1e-10, 'fp32c': 1e-5}  # outputs pass through an FFT
 
@@ -34,8 +36,8 @@ def test_wstack_workflow_matches_reference(arl, golden, precision):
     K = int(d['K'])
     (dirty, sumwt), = arl.imaging.invert_list_serial_workflow([vis], [im], context='wstack', vis_slices=K,
                                                                gcfcf=[(gcf, cf)], precision=precision)
-    assert rel(dirty.data, d['dirty']) < TOL[precision]
-    assert numpy.allclose(sumwt, d['sumwt'], rtol=1e-12)
+    assert_image(dirty.data, d['dirty'], d['gcf'], precision)
+    assert numpy.allclose(sumwt, d['sumwt'], rtol=1e-12 if precision == 'fp64' else 1e-6)
     model = arl.create_image_from_array(d['model'], im.wcs, im.polarisation_frame)
     (pv,) = arl.imaging.predict_list_serial_workflow([vis], [model], context='wstack', vis_slices=K,
                                                       gcfcf=[(gcf, cf)], precision=precision)
@@ -59,7 +61,7 @@ def test_wstack_single_matches_oracle(arl, oracle, golden, precision):
     wb = oracle.w_term_image(N, cell, wav)
     want = wb.real * ref.real - wb.imag * ref.imag
     got, gsw = arl.imaging.invert_wstack_single(vis, im, False, gcfcf=(gcf, cf), precision=precision)
-    assert rel(got.data, want) < TOL[precision]
+    assert_image(got.data, want, ogcf, precision)
     model = arl.create_image_from_array(d['model'], im.wcs, im.polarisation_frame)
     vr = oracle.predict_2d(uvw, d['frequency'], wb.real * d['model'], img, ogcf, ocf, cax)
     vi = oracle.predict_2d(uvw, d['frequency'], wb.imag * d['model'], img, ogcf, ocf, cax)
@@ -87,5 +89,5 @@ def test_wstack_many_slices_vs_oracle(arl, oracle):
     want, wsw = oracle.invert_wstack(uvw, freq, v, wt, img, oracle.pswf_gcf(N)[None, None], ocf, cax, K, cell)
     for p in ('fp64', 'fp32c'):
         got, sw = arl.imaging.invert_wstack(vis, im, K, gcfcf=(gcf, cf), precision=p)
-        assert rel(got.data, want) < TOL[p]
-        assert numpy.allclose(sw, wsw)
+        assert_image(got.data, want, oracle.pswf_gcf(N), p)
+        assert numpy.allclose(sw, wsw, rtol=1e-12 if p == 'fp64' else 1e-6)
