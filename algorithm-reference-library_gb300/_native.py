@@ -106,7 +106,10 @@ def call(name, *args):
 
 
 def ptr(t):
-    """Device pointer of a torch tensor (or None)."""
+    """Device pointer of a torch tensor (or None).  The caller must hold a
+    reference to the tensor until the library call that uses the pointer has
+    returned: a tensor dropped earlier can have its memory handed to the next
+    allocation before the call's kernels are even queued."""
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 

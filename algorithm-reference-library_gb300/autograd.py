@@ -61,7 +61,9 @@ class GriddingOperator:
         g = torch.empty((self.shape[0], self.shape[1], 1, self.shape[2], self.shape[3]),
                         dtype=dv.CDTYPE[self.precision], device=self.device)
         sw = torch.empty((self.shape[0], self.shape[1]), dtype=torch.float64, device=self.device)
-        nat.call('arlgpu_grid_planned', nat.ptr(v.contiguous()), nat.ptr(w.contiguous()), self.n,
+        v = v.contiguous()
+        w = w.contiguous()
+        nat.call('arlgpu_grid_planned', nat.ptr(v), nat.ptr(w), self.n,
                  nat.PRECISIONS[self.precision], nat.ptr(self.cf_t), ctypes.byref(self.cd), nat.ptr(g),
                  ctypes.byref(self.gd), nat.ptr(sw), nat.ptr(self.ws), self.ws.numel(), nat.stream_ptr())
         return g, sw
@@ -145,7 +147,9 @@ class GainChi2(torch.autograd.Function):
         grad_m = torch.empty_like(model) if ctx.needs_input_grad[0] else None
         grad_g = torch.empty(gains.shape, dtype=torch.complex128, device=dev) if ctx.needs_input_grad[1] else None
         g = gains.detach().to(torch.complex128).contiguous()
-        nat.call('arlgpu_gain_chi2', nat.ptr(vobs.to(model.dtype).contiguous()), nat.ptr(model.contiguous()),
+        vo = vobs.to(model.dtype).contiguous()
+        mo = model.contiguous()
+        nat.call('arlgpu_gain_chi2', nat.ptr(vo), nat.ptr(mo),
                  nat.ptr(weight), model.shape[0], model.shape[1], nat.PRECISIONS[prec], nat.ptr(a1), nat.ptr(a2),
                  nat.ptr(g), g.shape[0], nat.ptr(chi2), nat.ptr(grad_m), nat.ptr(grad_g), nat.stream_ptr())
         ctx.save_for_backward(*(t for t in (grad_m, grad_g) if t is not None))

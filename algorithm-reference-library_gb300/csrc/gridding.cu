@@ -46,9 +46,10 @@ const char *last_error() { return g_last_error.c_str(); }
 static std::atomic<unsigned long long> g_launches{0};
 
 // Kernel-variant choices (set by the autotuner through arlgpu_set_tuning).
-static std::atomic<int> g_tune_grid_kernel{0};    // 0: shared atomics + TwoSum, 1: band owner
-static std::atomic<int> g_tune_degrid_kernel{0};  // 0: warp per row, 1: batched rows
+static std::atomic<int> g_tune_grid_kernel{2};    // 0: atomics + TwoSum, 1: band owner, 2: lean, 3: uncompensated
+static std::atomic<int> g_tune_degrid_kernel{2};  // 0: warp per row, 1: batched rows, 2: lean
 static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automatic)
+static std::atomic<int> g_tune_chunk{512};        // sorted rows per gridder / degridder CTA
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------
@@ -103,28 +104,74 @@ struct Mapped {
   bool ok;
 };
 
+// round(world2pix0(x)) through one FMA, falling back to the exact sequence
+// when the fast value lies within tol of a half-integer.  Both the fast and
+// NumPy's value are within a few ulps of x / cdelt + crpix - 1; tol is ~45 ulps.
+__device__ __forceinline__ double round_w2p_fma(double x, const arlgpu_axis &a, double rcp) {
+  const double p = fma(__dsub_rn(x, a.crval), rcp, a.crpix - 1.0);
+  const double r = rint(p);
+  if (0.5 - fabs(p - r) < 1e-14 * (fabs(p) + fabs(a.crpix) + 2.0)) return rint(w2p_exact(x, a));
+  return r;
+}
+
+// Exact NumPy sequence for the u (or v) axis: (pixel, sub-pixel offset).
+__device__ __forceinline__ void map_axis_exact(double x, const arlgpu_axis &ga, double rcp_g, const arlgpu_axis &ca,
+                                               double rcp_c, double *pix, double *sub) {
+  *pix = round_w2p(x, ga, rcp_g);
+  *sub = floor_w2p(__dsub_rn(x, p2w(*pix, ga)), ca, rcp_c);
+}
+
+// The seven mapped indices of one row, as doubles, before any range check.
+struct RawMap {
+  double pu, pv, uf, vf, zg, zc, ch;
+};
+
+__device__ __forceinline__ RawMap map_raw(double u, double v, double w, double f, const Geom &g) {
+  RawMap r;
+  bool exact = !g.fast_uv;
+  if (!exact) {
+    // One-FMA fast path (valid when crval == 0 on UU, VV, DUU, DVV and the cf's
+    // DUU / DVV cdelt is the grid cdelt / O; the host checks this).  With
+    // P = u / cdelt + crpix - 1, the nearest pixel is rint(P) and the sub-pixel
+    // index is floor((P - pixel) O + O // 2); both fast values are within
+    // ~O |P| 1e-16 of NumPy's, so any result within 1e-14 O (|P| + 2) of a
+    // rounding boundary goes to the exact sequence instead.
+    const double Pu = fma(u, g.rcp_gu, g.gu.crpix - 1.0), Pv = fma(v, g.rcp_gv, g.gv.crpix - 1.0);
+    r.pu = rint(Pu);
+    r.pv = rint(Pv);
+    const double Qu = fma(Pu - r.pu, (double)g.O, g.cdu.crpix - 1.0);
+    const double Qv = fma(Pv - r.pv, (double)g.O, g.cdv.crpix - 1.0);
+    r.uf = floor(Qu);
+    r.vf = floor(Qv);
+    const double tu = 1e-14 * (fabs(Pu) + 2.0), tv = 1e-14 * (fabs(Pv) + 2.0);
+    const double tqu = tu * g.O, tqv = tv * g.O;
+    exact = (0.5 - fabs(Pu - r.pu) < tu) || (0.5 - fabs(Pv - r.pv) < tv) || (Qu - r.uf < tqu) ||
+            (r.uf + 1.0 - Qu < tqu) || (Qv - r.vf < tqv) || (r.vf + 1.0 - Qv < tqv);
+  }
+  if (exact) {
+    map_axis_exact(u, g.gu, g.rcp_gu, g.cdu, g.rcp_cdu, &r.pu, &r.uf);
+    map_axis_exact(v, g.gv, g.rcp_gv, g.cdv, g.rcp_cdv, &r.pv, &r.vf);
+  }
+  r.zg = round_w2p_fma(w, g.gw, g.rcp_gw);
+  r.zc = round_w2p_fma(w, g.cz, g.rcp_cz);
+  r.ch = round_w2p_fma(f, g.gf, g.rcp_gf);
+  return r;
+}
+
 __device__ __forceinline__ Mapped map_row(double u, double v, double w, double f, const Geom &g) {
   Mapped m;
-  double pu = round_w2p(u, g.gu, g.rcp_gu);
-  double pv = round_w2p(v, g.gv, g.rcp_gv);
-  double du = __dsub_rn(u, p2w(pu, g.gu));
-  double dv = __dsub_rn(v, p2w(pv, g.gv));
-  double uf = floor_w2p(du, g.cdu, g.rcp_cdu);
-  double vf = floor_w2p(dv, g.cdv, g.rcp_cdv);
-  double zg = round_w2p(w, g.gw, g.rcp_gw);
-  double zc = round_w2p(w, g.cz, g.rcp_cz);
-  double ch = round_w2p(f, g.gf, g.rcp_gf);
+  const RawMap r = map_raw(u, v, w, f, g);
   // Range checks in double so huge values cannot wrap when narrowed.
-  bool ok = pu >= 0.0 && pu < g.nx && pv >= 0.0 && pv < g.ny && uf >= 0.0 && uf < g.O &&
-            vf >= 0.0 && vf < g.O && zg >= 0.0 && zg < g.nw && zc >= 0.0 && zc < g.nz &&
-            ch >= 0.0 && ch < g.nchan && ch < g.cf_nchan;
-  m.pu = ok ? (int32_t)pu : -1;
-  m.pv = ok ? (int32_t)pv : -1;
-  m.uf = ok ? (int32_t)uf : 0;
-  m.vf = ok ? (int32_t)vf : 0;
-  m.zg = ok ? (int32_t)zg : 0;
-  m.zc = ok ? (int32_t)zc : 0;
-  m.ch = ok ? (int32_t)ch : 0;
+  bool ok = r.pu >= 0.0 && r.pu < g.nx && r.pv >= 0.0 && r.pv < g.ny && r.uf >= 0.0 && r.uf < g.O &&
+            r.vf >= 0.0 && r.vf < g.O && r.zg >= 0.0 && r.zg < g.nw && r.zc >= 0.0 && r.zc < g.nz &&
+            r.ch >= 0.0 && r.ch < g.nchan && r.ch < g.cf_nchan;
+  m.pu = ok ? (int32_t)r.pu : -1;
+  m.pv = ok ? (int32_t)r.pv : -1;
+  m.uf = ok ? (int32_t)r.uf : 0;
+  m.vf = ok ? (int32_t)r.vf : 0;
+  m.zg = ok ? (int32_t)r.zg : 0;
+  m.zc = ok ? (int32_t)r.zc : 0;
+  m.ch = ok ? (int32_t)r.ch : 0;
   if (ok) {
     int h = plane_sz(g, m.zc) >> 1;
     ok = (m.pu - h >= 0) && (m.pu + h <= g.nx) && (m.pv - h >= 0) && (m.pv + h <= g.ny);
@@ -163,26 +210,24 @@ __global__ void k_map(const double *__restrict__ uvw, const double *__restrict__
   }
 }
 
-// Exact-mapping export for arlgpu_convolution_mapping.
+// Mapping export for arlgpu_convolution_mapping: the same indices the plan
+// uses (map_raw), clamped only to fit int32.
 __global__ void k_map_export(const double *__restrict__ uvw, const double *__restrict__ freq, int64_t nvis,
                              Geom g, int32_t *pu, int32_t *puo, int32_t *pv, int32_t *pvo, int32_t *pwg,
                              int32_t *pwc, int32_t *pf, unsigned long long *nbad) {
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nvis;
        r += (int64_t)gridDim.x * blockDim.x) {
-    double u = uvw[3 * r], v = uvw[3 * r + 1], w = uvw[3 * r + 2], f = freq[r];
-    double dpu = round_w2p(u, g.gu, g.rcp_gu);
-    double dpv = round_w2p(v, g.gv, g.rcp_gv);
-    double uf = floor_w2p(__dsub_rn(u, p2w(dpu, g.gu)), g.cdu, g.rcp_cdu);
-    double vf = floor_w2p(__dsub_rn(v, p2w(dpv, g.gv)), g.cdv, g.rcp_cdv);
-    pu[r] = (int32_t)fmax(fmin(dpu, 2e9), -2e9);
-    pv[r] = (int32_t)fmax(fmin(dpv, 2e9), -2e9);
-    puo[r] = (int32_t)fmax(fmin(uf, 2e9), -2e9);
-    pvo[r] = (int32_t)fmax(fmin(vf, 2e9), -2e9);
-    pwg[r] = (int32_t)fmax(fmin(round_w2p(w, g.gw, g.rcp_gw), 2e9), -2e9);
-    pwc[r] = (int32_t)fmax(fmin(round_w2p(w, g.cz, g.rcp_cz), 2e9), -2e9);
-    pf[r] = (int32_t)fmax(fmin(round_w2p(f, g.gf, g.rcp_gf), 2e9), -2e9);
-    Mapped m = map_row(u, v, w, f, g);
-    if (!m.ok) atomicAdd(nbad, 1ull);
+    const double u = uvw[3 * r], v = uvw[3 * r + 1], w = uvw[3 * r + 2], f = freq[r];
+    const RawMap m = map_raw(u, v, w, f, g);
+    auto c = [](double x) { return (int32_t)fmax(fmin(x, 2e9), -2e9); };
+    pu[r] = c(m.pu);
+    pv[r] = c(m.pv);
+    puo[r] = c(m.uf);
+    pvo[r] = c(m.vf);
+    pwg[r] = c(m.zg);
+    pwc[r] = c(m.zc);
+    pf[r] = c(m.ch);
+    if (!map_row(u, v, w, f, g).ok) atomicAdd(nbad, 1ull);
   }
 }
 
@@ -295,6 +340,17 @@ template <> struct SmemAcc<float> {
 template <> struct SmemAcc<double> {
   static constexpr int kWords = 1;
   __device__ static __forceinline__ void add(double2 *sum, double2 *, double2 v) {
+    atomicAdd(&sum->x, v.x);
+    atomicAdd(&sum->y, v.y);
+  }
+};
+
+// Uncompensated shared-memory accumulation (grid_kernel 3, kept only to
+// measure what the compensation costs; not part of the FP32C contract).
+template <typename R> struct PlainAcc {
+  static constexpr int kWords = 1;
+  __device__ static __forceinline__ void add(typename Cplx<R>::T *sum, typename Cplx<R>::T *,
+                                             typename Cplx<R>::T v) {
     atomicAdd(&sum->x, v.x);
     atomicAdd(&sum->y, v.y);
   }
@@ -843,6 +899,268 @@ k_degrid_batch(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restri
   }
 }
 
+// Per-row set-up shared by the lean kernels: the sub-kernel base pointer and
+// the 32-bit tap / subgrid offsets of this lane's first tap, plus the offset
+// steps for "32 taps further" (q rows and rr columns, with a row wrap).
+struct RowWalk {
+  int n, sz;     // taps in the window, window edge
+  int i, ko, so; // column of the current tap, its tap-table and subgrid offsets
+  int q, rr;     // 32 = q * sz + rr
+  int dko, dso;  // offset steps without a wrap
+  int wko, wso;  // extra step when the column wraps
+};
+
+__device__ __forceinline__ RowWalk row_walk(int sz, int S, int SG, int lv, int lu, int lane) {
+  RowWalk w;
+  w.sz = sz;
+  w.n = sz * sz;
+  w.q = 32 / sz;
+  w.rr = 32 - w.q * sz;
+  const int j = lane / sz;
+  w.i = lane - j * sz;
+  w.ko = j * S + w.i;
+  w.so = (lv + j) * SG + lu + w.i;
+  w.dko = w.q * S + w.rr;
+  w.dso = w.q * SG + w.rr;
+  w.wko = S - sz;
+  w.wso = SG - sz;
+  return w;
+}
+
+__device__ __forceinline__ void row_step(RowWalk &w) {
+  w.i += w.rr;
+  w.ko += w.dko;
+  w.so += w.dso;
+  if (w.i >= w.sz) {
+    w.i -= w.sz;
+    w.ko += w.wko;
+    w.so += w.wso;
+  }
+}
+
+// K3 (lean variant): warp per row, compensated shared-memory atomics as in
+// k_grid, specialised on the polarisation count, with 32-bit incremental
+// offsets into the tap table and the subgrid.
+template <typename R, int NPOL, int NW, typename ACC = SmemAcc<R>>
+__global__ void __launch_bounds__(NW * 32)
+k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
+            const uint32_t *__restrict__ off, uint32_t chunk,
+            const typename VisT<R>::C *__restrict__ vis, const typename VisT<R>::W *__restrict__ wt,
+            const typename Cplx<R>::T *__restrict__ cf, typename Cplx<R>::T *__restrict__ grid,
+            double *__restrict__ sumwt) {
+  using CT = typename Cplx<R>::T;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int SG = g.SG, SG2 = SG * SG;
+  CT *sub = reinterpret_cast<CT *>(smraw);
+  CT *comp = sub + (size_t)NPOL * SG2;
+  const uint32_t nvalid = off[g.nbins];
+  const uint32_t c0 = blockIdx.x * chunk;
+  if (c0 >= nvalid) return;
+  const uint32_t c1 = min(c0 + chunk, nvalid);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int S = g.S, O = g.O;
+  const int ps = (int)g.cf_pol_stride;
+  const int64_t plane_elems = (int64_t)g.ny * g.nx;
+
+  uint32_t pos = c0;
+  while (pos < c1) {
+    const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    if (!sg.direct) {
+      for (int k = threadIdx.x; k < NPOL * SG2 * ACC::kWords; k += blockDim.x) sub[k] = czero<CT>();
+      __syncthreads();
+    }
+    double wsum[NPOL];
+#pragma unroll
+    for (int p = 0; p < NPOL; ++p) wsum[p] = 0.0;
+    for (uint32_t r = pos + warp; r < sg.end; r += NW) {
+      const RowMap m = smap[r];
+      const uint32_t idx = sidx[r];
+      const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+      const int sz = plane_sz(g, zc);
+      const int toff = (S - sz) >> 1;
+      const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
+      CT vw[NPOL];
+#pragma unroll
+      for (int p = 0; p < NPOL; ++p) {
+        const CT v = vis[(size_t)idx * NPOL + p];
+        const R w = wt[(size_t)idx * NPOL + p];
+        vw[p].x = v.x * w;
+        vw[p].y = v.y * w;
+        if (lane == 0) wsum[p] += (double)w;
+      }
+      const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                     ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+      if (sg.direct) {
+        RowWalk wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
+        CT *gb = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
+                 (int64_t)wv * g.nx + wu;
+        for (int t = lane; t < wk.n; t += 32) {
+#pragma unroll
+          for (int p = 0; p < NPOL; ++p) {
+            const CT tp = kb[p * ps + wk.ko];
+            CT c;
+            c.x = tp.x * vw[p].x + tp.y * vw[p].y;
+            c.y = tp.x * vw[p].y - tp.y * vw[p].x;
+            red_global<CT>(gb + (int64_t)p * g.nw * plane_elems + wk.so, c);
+          }
+          row_step(wk);
+        }
+        continue;
+      }
+      RowWalk wk = row_walk(sz, S, SG, wv - sg.v0, wu - sg.u0, lane);
+      for (int t = lane; t < wk.n; t += 32) {
+#pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          const CT tp = kb[p * ps + wk.ko];
+          CT c;  // conj(tap) * vw
+          c.x = tp.x * vw[p].x + tp.y * vw[p].y;
+          c.y = tp.x * vw[p].y - tp.y * vw[p].x;
+          ACC::add(sub + p * SG2 + wk.so, comp + p * SG2 + wk.so, c);
+        }
+        row_step(wk);
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NPOL; ++p) {
+      double s = wsum[p];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0 && s != 0.0) atomicAdd(&sumwt[sg.ch * NPOL + p], s);
+    }
+    if (!sg.direct) {
+      __syncthreads();
+      for (int k = threadIdx.x; k < NPOL * SG2; k += blockDim.x) {
+        CT val = sub[k];
+        if (ACC::kWords == 2) {
+          CT e = comp[k];
+          val.x += e.x;
+          val.y += e.y;
+        }
+        if (val.x == (R)0 && val.y == (R)0) continue;
+        const int p = k / SG2, rem = k - p * SG2, y = rem / SG, x = rem - y * SG;
+        const int gy = sg.v0 + y, gx = sg.u0 + x;
+        if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
+        red_global<CT>(grid + ((int64_t)(sg.ch * NPOL + p) * g.nw + sg.zg) * plane_elems + (int64_t)gy * g.nx + gx,
+                       val);
+      }
+      __syncthreads();
+    }
+    pos = sg.end;
+  }
+}
+
+// K4 (lean variant): warp per row, specialised on the polarisation count,
+// 32-bit incremental offsets, two taps per iteration with independent sums.
+template <typename R, int NPOL, int NW>
+__global__ void __launch_bounds__(NW * 32)
+k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
+              const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
+              const typename Cplx<R>::T *__restrict__ cf, const typename Cplx<R>::T *__restrict__ grid,
+              typename VisT<R>::C *__restrict__ vis_out) {
+  using CT = typename Cplx<R>::T;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int SG = g.SG, SG2 = SG * SG;
+  CT *sub = reinterpret_cast<CT *>(smraw);
+  const uint32_t nvalid = off[g.nbins];
+  const uint32_t c0 = blockIdx.x * chunk;
+  if (c0 >= (uint32_t)nvis) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (c0 + chunk > nvalid) {
+    const uint32_t b = max(c0, nvalid), e = min(c0 + chunk, (uint32_t)nvis);
+    for (uint32_t r = b + threadIdx.x; r < e; r += blockDim.x)
+      for (int p = 0; p < NPOL; ++p) vis_out[(size_t)sidx[r] * NPOL + p] = czero<CT>();
+    if (c0 >= nvalid) return;
+  }
+  const uint32_t c1 = min(c0 + chunk, nvalid);
+  const int S = g.S, O = g.O;
+  const int ps = (int)g.cf_pol_stride;
+  const int64_t plane_elems = (int64_t)g.ny * g.nx;
+
+  uint32_t pos = c0;
+  while (pos < c1) {
+    const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    const CT *gplane = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems;
+    if (!sg.direct) {
+      for (int k = threadIdx.x; k < NPOL * SG2; k += blockDim.x) {
+        const int p = k / SG2, rem = k - p * SG2, y = rem / SG, x = rem - y * SG;
+        const int gy = sg.v0 + y, gx = sg.u0 + x;
+        CT val = czero<CT>();
+        if (gy >= 0 && gy < g.ny && gx >= 0 && gx < g.nx)
+          val = gplane[(int64_t)p * g.nw * plane_elems + (int64_t)gy * g.nx + gx];
+        sub[k] = val;
+      }
+      __syncthreads();
+    }
+    for (uint32_t r = pos + warp; r < sg.end; r += NW) {
+      const RowMap m = smap[r];
+      const uint32_t idx = sidx[r];
+      const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+      const int sz = plane_sz(g, zc);
+      const int toff = (S - sz) >> 1;
+      const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
+      const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                     ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+      const CT *src;
+      int pstride;
+      RowWalk wk;
+      if (sg.direct) {
+        src = gplane + (int64_t)wv * g.nx + wu;
+        pstride = 0;  // unused: direct mode indexes planes through gplane below
+        wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
+      } else {
+        src = sub;
+        pstride = SG2;
+        wk = row_walk(sz, S, SG, wv - sg.v0, wu - sg.u0, lane);
+      }
+      R ax[NPOL], ay[NPOL], bx[NPOL], by[NPOL];
+#pragma unroll
+      for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = bx[p] = by[p] = 0;
+      int t = lane;
+      for (; t + 32 < wk.n; t += 64) {
+        const int ko1 = wk.ko, so1 = wk.so;
+        row_step(wk);
+        const int ko2 = wk.ko, so2 = wk.so;
+        row_step(wk);
+#pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          const CT *sp = sg.direct ? src + (int64_t)p * g.nw * plane_elems : src + p * pstride;
+          const CT t1 = kb[p * ps + ko1], t2 = kb[p * ps + ko2];
+          const CT g1 = sp[so1], g2 = sp[so2];
+          ax[p] += g1.x * t1.x - g1.y * t1.y;
+          ay[p] += g1.x * t1.y + g1.y * t1.x;
+          bx[p] += g2.x * t2.x - g2.y * t2.y;
+          by[p] += g2.x * t2.y + g2.y * t2.x;
+        }
+      }
+      if (t < wk.n) {
+#pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          const CT *sp = sg.direct ? src + (int64_t)p * g.nw * plane_elems : src + p * pstride;
+          const CT t1 = kb[p * ps + wk.ko];
+          const CT g1 = sp[wk.so];
+          ax[p] += g1.x * t1.x - g1.y * t1.y;
+          ay[p] += g1.x * t1.y + g1.y * t1.x;
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < NPOL; ++p) {
+        R sx = ax[p] + bx[p], sy = ay[p] + by[p];
+        for (int o = 16; o > 0; o >>= 1) {
+          sx += __shfl_xor_sync(0xffffffffu, sx, o);
+          sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        }
+        if (lane == p) {
+          CT out;
+          out.x = sx;
+          out.y = sy;
+          vis_out[(size_t)idx * NPOL + p] = out;
+        }
+      }
+    }
+    if (!sg.direct) __syncthreads();
+    pos = sg.end;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
@@ -892,12 +1210,23 @@ int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precisio
   g->rcp_cdv = rcp(cd->dv.cdelt);
   g->rcp_cz = rcp(cd->z.cdelt);
   g->plane_support = cd->plane_support;
+  {
+    // The fast u/v mapping needs zero crvals, integer crpixes and the cf's
+    // sub-pixel cdelt equal to the grid cdelt / O (ARL builds both from one
+    // image, so this is the usual case).
+    auto integral = [](double x) { return x == (double)(long long)x; };
+    g->fast_uv = gd->u.crval == 0.0 && gd->v.crval == 0.0 && cd->du.crval == 0.0 && cd->dv.crval == 0.0 &&
+                 integral(gd->u.crpix) && integral(gd->v.crpix) && integral(cd->du.crpix) &&
+                 integral(cd->dv.crpix) && cd->du.cdelt == gd->u.cdelt / cd->oversampling &&
+                 cd->dv.cdelt == gd->v.cdelt / cd->oversampling && fabs(gd->u.crpix) < 1e9 &&
+                 fabs(gd->v.crpix) < 1e9;
+  }
   // Subgrid edge: 64 cells when npol planes of it (with the FP32 compensation
   // words) fit in 64 KiB of shared memory, else 32.
   const size_t cell = precision == ARLGPU_FP64 ? 16 : 16;  // c128, or c64 sum + c64 comp
   int SG = g_tune_subgrid.load();
   if (SG <= 0) {
-    SG = 64;
+    SG = 48;  // the C2 autotuning optimum for supports 8..32
     if ((size_t)g->npol * SG * SG * cell > 64 * 1024) SG = 32;
   }
   if (SG - g->S < 8) SG = ((g->S + 8 + 7) / 8) * 8;
@@ -978,7 +1307,7 @@ int plan_build(const double *uvw, const double *freq, int64_t nvis, const Geom &
 }
 
 static constexpr int kWarps = 8;
-static constexpr uint32_t kChunk = 512;
+static inline uint32_t chunk_rows() { return (uint32_t)g_tune_chunk.load(); }
 
 template <typename R>
 static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const void *vis, const void *wt,
@@ -988,12 +1317,22 @@ static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const voi
   if (g_tune_grid_kernel.load() == 1) {
     kern = k_grid_band<R, kWarps>;
     smem += sizeof(StagedRow<typename Cplx<R>::T>) * kWarps * 32;
+  } else if (g_tune_grid_kernel.load() == 2) {
+    kern = g.npol == 1 ? k_grid_lean<R, 1, kWarps> : g.npol == 2 ? k_grid_lean<R, 2, kWarps>
+                                                                  : k_grid_lean<R, 4, kWarps>;
+    if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean gridder handles 1, 2 or 4 polarisations");
+  } else if (g_tune_grid_kernel.load() == 3) {
+    kern = g.npol == 1 ? k_grid_lean<R, 1, kWarps, PlainAcc<R>>
+                       : g.npol == 2 ? k_grid_lean<R, 2, kWarps, PlainAcc<R>> : k_grid_lean<R, 4, kWarps, PlainAcc<R>>;
+    if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean gridder handles 1, 2 or 4 polarisations");
+    smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T);
   }
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  unsigned blocks = (unsigned)((nvis + kChunk - 1) / kChunk);
+  const uint32_t chunk = chunk_rows();
+  unsigned blocks = (unsigned)((nvis + chunk - 1) / chunk);
   if (blocks == 0) return ARLGPU_OK;
-  kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, kChunk,
+  kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk,
                                           static_cast<const typename VisT<R>::C *>(vis),
                                           static_cast<const typename VisT<R>::W *>(wt),
                                           static_cast<const typename Cplx<R>::T *>(cf),
@@ -1008,11 +1347,18 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
                          void *vis_out, cudaStream_t st) {
   size_t smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T);
   auto kern = k_degrid<R, kWarps>;
-  if (g_tune_degrid_kernel.load() == 1) kern = k_degrid_batch<R, kWarps>;
+  if (g_tune_degrid_kernel.load() == 1) {
+    kern = k_degrid_batch<R, kWarps>;
+  } else if (g_tune_degrid_kernel.load() == 2) {
+    if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
+    kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps> : g.npol == 2 ? k_degrid_lean<R, 2, kWarps>
+                                                                    : k_degrid_lean<R, 4, kWarps>;
+  }
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  unsigned blocks = (unsigned)((nvis + kChunk - 1) / kChunk);
+  const uint32_t chunk = chunk_rows();
+  unsigned blocks = (unsigned)((nvis + chunk - 1) / chunk);
   if (blocks == 0) return ARLGPU_OK;
-  kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, kChunk, nvis,
+  kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk, nvis,
                                           static_cast<const typename Cplx<R>::T *>(cf),
                                           static_cast<const typename Cplx<R>::T *>(grid),
                                           static_cast<typename VisT<R>::C *>(vis_out));
@@ -1146,9 +1492,10 @@ extern "C" int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const a
 extern "C" int arlgpu_set_tuning(const char *key, int value) {
   if (!key) return fail(ARLGPU_ERR_INVALID, "null key");
   const std::string k(key);
-  if (k == "grid_kernel" && (value == 0 || value == 1)) g_tune_grid_kernel = value;
-  else if (k == "degrid_kernel" && (value == 0 || value == 1)) g_tune_degrid_kernel = value;
+  if (k == "grid_kernel" && value >= 0 && value <= 3) g_tune_grid_kernel = value;
+  else if (k == "degrid_kernel" && value >= 0 && value <= 2) g_tune_degrid_kernel = value;
   else if (k == "subgrid" && (value == 0 || (value >= 16 && value <= 128))) g_tune_subgrid = value;
+  else if (k == "chunk" && value >= 32 && value <= (1 << 20)) g_tune_chunk = value;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key or value: %s = %d", key, value);
   return ARLGPU_OK;
 }
@@ -1159,6 +1506,7 @@ extern "C" int arlgpu_get_tuning(const char *key, int *value) {
   if (k == "grid_kernel") *value = g_tune_grid_kernel;
   else if (k == "degrid_kernel") *value = g_tune_degrid_kernel;
   else if (k == "subgrid") *value = g_tune_subgrid;
+  else if (k == "chunk") *value = g_tune_chunk;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key: %s", key);
   return ARLGPU_OK;
 }

@@ -203,7 +203,9 @@ def fft_image_to_grid(image_t, gcf_t, gd, precision, out=None, stream=None):
     dev = image_t.device
     if out is None:
         out = torch.empty((gd.nchan, gd.npol, gd.nw, gd.ny, gd.nx), dtype=CDTYPE[precision], device=dev)
-    nat.call('arlgpu_fft_image_to_grid', nat.ptr(image_t.contiguous()), nat.ptr(gcf_t.contiguous()),
+    image_t = image_t.contiguous()
+    gcf_t = gcf_t.contiguous()
+    nat.call('arlgpu_fft_image_to_grid', nat.ptr(image_t), nat.ptr(gcf_t),
              ctypes.byref(gd), nat.PRECISIONS[precision], nat.ptr(out), nat.stream_ptr(stream))
     return out
 

@@ -232,8 +232,9 @@ def invert_wstack(vis, im, vis_slices, dopsf=False, normalize=True, gcfcf=None, 
     image = torch.empty((nchan, npol, ny, nx), dtype=torch.float64, device=device)
     norm = sumwt if normalize else torch.ones_like(sumwt)
     fftbuf = grid_t if precision == 'fp64' else torch.empty(grid_t.shape, dtype=torch.complex128, device=device)
+    gcf_d = _gcf_t(s['gcf'], device)
     nat.call('arlgpu_wstack_grid_to_image', nat.ptr(grid_t), ctypes.byref(gd), nat.PRECISIONS[precision],
-             nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),
+             nat.ptr(gcf_d), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),
              nat.ptr(fftbuf), nat.stream_ptr())
     host = not isinstance(vis, DeviceVisibility)
     out = Image(image.cpu().numpy() if host else image, im.wcs.deepcopy(), im.polarisation_frame)
@@ -252,7 +253,8 @@ def predict_wstack(vis, model, vis_slices, gcfcf=None, precision=None, **kwargs)
     m_t = d.to(device=device, dtype=torch.float64).contiguous() if isinstance(d, torch.Tensor) else \
         dv.to_device(numpy.asarray(d, numpy.float64), torch.float64, device)
     grid_t = torch.empty((nchan, npol, vis_slices, ny, nx), dtype=dv.CDTYPE[precision], device=device)
-    nat.call('arlgpu_wstack_image_to_grid', nat.ptr(m_t), nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']),
+    gcf_d = _gcf_t(s['gcf'], device)
+    nat.call('arlgpu_wstack_image_to_grid', nat.ptr(m_t), nat.ptr(gcf_d), nat.ptr(s['wmean']),
              s['cellsize'], ctypes.byref(gd), nat.PRECISIONS[precision], nat.ptr(grid_t), nat.stream_ptr())
     out = torch.empty((s['uvw'].shape[0], npol), dtype=dv.CDTYPE[precision], device=device)
     nat.call('arlgpu_degrid_planned', s['uvw'].shape[0], nat.PRECISIONS[precision], nat.ptr(s['cf_t']),
@@ -309,8 +311,9 @@ def _single_slice_invert(vis, im, dopsf, normalize, gcfcf, precision):
     image = torch.empty((nchan, npol, ny, nx), dtype=torch.float64, device=device)
     norm = sumwt if normalize else torch.ones_like(sumwt)
     fftbuf = grid_t if precision == 'fp64' else torch.empty(grid_t.shape, dtype=torch.complex128, device=device)
+    gcf_d = _gcf_t(s['gcf'], device)
     nat.call('arlgpu_wstack_grid_to_image', nat.ptr(grid_t), ctypes.byref(gd), nat.PRECISIONS[precision],
-             nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),
+             nat.ptr(gcf_d), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),
              nat.ptr(fftbuf), nat.stream_ptr())
     host = not isinstance(vis, DeviceVisibility)
     out = Image(image.cpu().numpy() if host else image, im.wcs.deepcopy(), im.polarisation_frame)
@@ -331,7 +334,8 @@ def predict_wstack_single(vis, model, remove=True, gcfcf=None, precision=None, *
     m_t = d.to(device=device, dtype=torch.float64).contiguous() if isinstance(d, torch.Tensor) else \
         dv.to_device(numpy.asarray(d, numpy.float64), torch.float64, device)
     grid_t = torch.empty((nchan, npol, 1, ny, nx), dtype=dv.CDTYPE[precision], device=device)
-    nat.call('arlgpu_wstack_image_to_grid', nat.ptr(m_t), nat.ptr(_gcf_t(s['gcf'], device)), nat.ptr(s['wmean']),
+    gcf_d = _gcf_t(s['gcf'], device)
+    nat.call('arlgpu_wstack_image_to_grid', nat.ptr(m_t), nat.ptr(gcf_d), nat.ptr(s['wmean']),
              s['cellsize'], ctypes.byref(gd), nat.PRECISIONS[precision], nat.ptr(grid_t), nat.stream_ptr())
     out = torch.empty((s['uvw'].shape[0], npol), dtype=dv.CDTYPE[precision], device=device)
     nat.call('arlgpu_degrid_planned', s['uvw'].shape[0], nat.PRECISIONS[precision], nat.ptr(s['cf_t']),

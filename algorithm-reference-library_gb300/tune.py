@@ -14,9 +14,10 @@ import torch
 from . import _native as nat
 from . import device as dv
 
-GRID_KERNELS = (0, 1)      # shared atomics + TwoSum, band owner + Kahan
-DEGRID_KERNELS = (0, 1)    # warp per row, 32-row batches
-SUBGRIDS = (32, 48, 64, 96)
+GRID_KERNELS = (0, 1, 2)     # shared atomics + TwoSum, band owner + Kahan, lean atomics
+DEGRID_KERNELS = (0, 1, 2)   # warp per row, 32-row batches, lean warp per row
+SUBGRIDS = (32, 48, 64)
+CHUNKS = (512, 2048)
 
 
 def set_tuning(**kw):
@@ -28,7 +29,7 @@ def set_tuning(**kw):
 def get_tuning():
     lib = nat.load()
     out = {}
-    for k in ('grid_kernel', 'degrid_kernel', 'subgrid'):
+    for k in ('grid_kernel', 'degrid_kernel', 'subgrid', 'chunk'):
         v = ctypes.c_int()
         nat.check(lib.arlgpu_get_tuning(k.encode(), ctypes.byref(v)))
         out[k] = v.value
@@ -100,18 +101,36 @@ def stage_times(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps=3):
     return tuple(acc)
 
 
-def autotune(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps=2, subgrids=SUBGRIDS, grid_kernels=GRID_KERNELS,
-             degrid_kernels=DEGRID_KERNELS):
-    """Pick the fastest (grid_kernel, degrid_kernel, subgrid) for these rows;
-    returns (best setting, {setting: ms per step})."""
+def autotune(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps=2, subgrids=SUBGRIDS, chunks=CHUNKS,
+             grid_kernels=GRID_KERNELS, degrid_kernels=DEGRID_KERNELS):
+    """Pick the fastest (subgrid, chunk) and, for it, the fastest gridder and
+    degridder variants, timing plan, grid and degrid separately on these rows.
+    Returns (best setting, {setting string: (plan, grid, degrid) ms})."""
     results = {}
-    for sg, gk, dk in itertools.product(subgrids, grid_kernels, degrid_kernels):
-        try:
-            set_tuning(grid_kernel=gk, degrid_kernel=dk, subgrid=sg)
-            ms = _time_step(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps)
-        except nat.ArlGpuError:
+    best, best_ms = None, float('inf')
+    for sg, ch in itertools.product(subgrids, chunks):
+        g_ms, d_ms, plan = {}, {}, None
+        for k in sorted(set(grid_kernels) | set(degrid_kernels)):
+            try:
+                set_tuning(subgrid=sg, chunk=ch, grid_kernel=k if k in grid_kernels else grid_kernels[0],
+                           degrid_kernel=k if k in degrid_kernels else degrid_kernels[0])
+                t = stage_times(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps)
+            except nat.ArlGpuError:
+                continue
+            plan = t[0] if plan is None else min(plan, t[0])
+            if k in grid_kernels:
+                g_ms[k] = t[1]
+            if k in degrid_kernels:
+                d_ms[k] = t[2]
+            results['sg%d/chunk%d/kernel%d' % (sg, ch, k)] = tuple(round(x, 4) for x in t)
+        if not g_ms or not d_ms:
             continue
-        results[(gk, dk, sg)] = ms
-    best = min(results, key=results.get)
-    set_tuning(grid_kernel=best[0], degrid_kernel=best[1], subgrid=best[2])
-    return dict(grid_kernel=best[0], degrid_kernel=best[1], subgrid=best[2]), results
+        gk = min(g_ms, key=g_ms.get)
+        dk = min(d_ms, key=d_ms.get)
+        total = plan + g_ms[gk] + d_ms[dk]
+        if total < best_ms:
+            best_ms = total
+            best = dict(grid_kernel=gk, degrid_kernel=dk, subgrid=sg, chunk=ch)
+    set_tuning(**best)
+    best['ms_per_step'] = round(best_ms, 4)
+    return best, results

@@ -51,6 +51,9 @@ def parse():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline')
     ap.add_argument('--cpu-seconds', type=float, default=12.0, help='CPU-baseline time budget')
     ap.add_argument('--no-tune', action='store_true', help='keep the library\'s default kernel variants')
+    ap.add_argument('--profile-rows', type=int, default=0,
+                    help='profiling case for ncu: the workload subsampled to this many rows, --warmup + --steps '
+                         'untimed steps with the library defaults, no other arms')
     return ap.parse_args()
 
 
@@ -424,7 +427,7 @@ def arm_gb300(args, torch, world, rank, local):
         c0 = build_context(arl, torch, w, 'fp32c', device)
         best, table = arl.tune.autotune(c0['uvw'], c0['freq'], c0['vis'], c0['wt'], c0['cf_t'], c0['cd'], c0['gd'],
                                         'fp32c')
-        tuned = {'choice': best, 'ms_per_step': {'%d/%d/%d' % k: round(v, 4) for k, v in table.items()}}
+        tuned = {'choice': best, 'stage_ms_plan_grid_degrid': table}
         del c0
     ctx = build_context(arl, torch, w, 'fp32c', device)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
@@ -547,9 +550,30 @@ def arm_reference(args, torch, world, rank):
             'e2e': {'value': value, 'unit': 'vis/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
 
 
+def profile_case(args, torch):
+    """Small untimed case for ncu captures (one GPU): warmup + steps plan /
+    grid / degrid calls on a row subsample, with the library's default
+    kernel variants."""
+    arl = importlib.import_module('algorithm-reference-library_gb300')
+    sim = importlib.import_module('algorithm-reference-library_gb300.simulation')
+    device = torch.device('cuda', 0)
+    w = sim.make_workload(args.workload, max_rows=args.profile_rows, device=device)
+    w['name'] = args.workload
+    ctx = build_context(arl, torch, w, 'fp32c', device)
+    st = torch.cuda.current_stream()
+    for _ in range(args.warmup + args.steps):
+        run_step(arl, ctx, st)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_case': args.workload, 'rows': ctx['n'], 'steps': args.warmup + args.steps,
+                      'tuning': arl.tune.get_tuning()}))
+
+
 def main():
     args = parse()
     import torch
+    if args.profile_rows:
+        profile_case(args, torch)
+        return
     world, rank, local = dist_setup(torch)
     if args.impl == 'reference':
         line = arm_reference(args, torch, world, rank)

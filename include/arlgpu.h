@@ -80,11 +80,16 @@ const char *arlgpu_last_error(void);
 unsigned long long arlgpu_kernel_launches(void);
 
 /* Kernel-variant selection (the autotuner's knobs; process-wide):
- *   "grid_kernel"   0 = shared-memory atomics with TwoSum compensation (default),
+ *   "grid_kernel"   0 = shared-memory atomics with TwoSum compensation,
  *                   1 = band owner: each warp owns a band of the subgrid, plain
- *                       read-modify-write with a per-cell Kahan term
- *   "degrid_kernel" 0 = one warp per row (default), 1 = 32-row batches per warp
- *   "subgrid"       subgrid edge in cells (16..128), 0 = automatic
+ *                       read-modify-write with a per-cell Kahan term,
+ *                   2 = as 0, specialised on npol with 32-bit incremental offsets (default),
+ *                   3 = as 2 without the compensation (measurement only: FP32C
+ *                       promises compensated sums, so the autotuner never picks it)
+ *   "degrid_kernel" 0 = one warp per row, 1 = 32-row batches per warp,
+ *                   2 = one warp per row, specialised on npol, two taps per step (default)
+ *   "subgrid"       subgrid edge in cells (16..128), 0 = automatic (48, or 32 when 4 pols)
+ *   "chunk"         sorted rows per gridder / degridder CTA (32..2^20, default 512)
  * No reference counterpart (ARL has one Python loop per function). */
 int arlgpu_set_tuning(const char *key, int value);
 int arlgpu_get_tuning(const char *key, int *value);

@@ -80,11 +80,19 @@ def test_mapping_bit_exact_at_rounding_boundaries(arl, oracle):
     uvw = numpy.stack([u, u[::-1], rng.uniform(-100, 100, n)], axis=1)
     freq = numpy.full(n, 1e8)
     vis = make_vis(arl, uvw, freq, numpy.zeros((n, 1)), numpy.ones((n, 1)))
-    got = arl.convolution_mapping(vis, gd, cf)
     img = oracle.image_geometry(N, cell)
-    want = oracle.convolution_mapping(uvw, freq, oracle.grid_axes(img), oracle.cf_axes(img, O, S))
-    for g, w in zip((got[0], got[1], got[2], got[3], got[4], got[6], got[8]), want):
-        assert numpy.array_equal(g, w)
+    gax, cax = oracle.grid_axes(img), oracle.cf_axes(img, O, S)
+    # As built (the one-FMA fast path applies), then with the cf's sub-pixel
+    # cdelt nudged by one ulp (the library must take the exact path).
+    for nudge in (False, True):
+        if nudge:
+            for ax, key in ((2, 'du'), (3, 'dv')):
+                cf.grid_wcs.wcs.cdelt[ax] = numpy.nextafter(cf.grid_wcs.wcs.cdelt[ax], numpy.inf)
+                cax[key] = (cax[key][0], cax[key][1], float(cf.grid_wcs.wcs.cdelt[ax]))
+        got = arl.convolution_mapping(vis, gd, cf)
+        want = oracle.convolution_mapping(uvw, freq, gax, cax)
+        for g, w in zip((got[0], got[1], got[2], got[3], got[4], got[6], got[8]), want):
+            assert numpy.array_equal(g, w)
 
 
 # ---------------------------------------------------------------------------
@@ -341,3 +349,27 @@ def test_c2_full_size_properties(arl):
                                             precision='fp32c')
     g1 = res['fp32c'][0]
     assert numpy.max(numpy.abs(g2.data.to(torch.complex128).cpu().numpy() - 2 * g1)) <= 1e-6 * numpy.abs(g1).max()
+
+
+@pytest.mark.parametrize('grid_kernel,degrid_kernel,subgrid,chunk', [
+    (0, 0, 48, 512), (1, 1, 0, 512), (2, 2, 32, 2048), (2, 2, 0, 512), (3, 0, 0, 512)])
+@pytest.mark.parametrize('npol', [1, 2, 4])
+def test_kernel_variants_vs_oracle(arl, oracle, grid_kernel, degrid_kernel, subgrid, chunk, npol):
+    """Every gridder / degridder variant, against the oracle (grid_kernel 3 is
+    the uncompensated measurement variant: FP32 sums, same 1e-5 bound here)."""
+    before = arl.tune.get_tuning()
+    try:
+        arl.tune.set_tuning(grid_kernel=grid_kernel, degrid_kernel=degrid_kernel, subgrid=subgrid, chunk=chunk)
+        for precision in ('fp64', 'fp32c'):
+            rng = numpy.random.default_rng(7 + npol)
+            im, cf, vis, maps, gax = _random_case(arl, oracle, rng, 128, 4e-3, 8, 12, 4000, 2, npol, 3, 20.0, True)
+            arl.set_plane_support(cf, [8, 12, 10])
+            gd, sumwt = arl.grid_visibility_to_griddata(vis, arl.create_griddata_from_image(im), cf,
+                                                        precision=precision)
+            g_ref, sw_ref = oracle.grid_vec(vis.vis, vis.imaging_weight, maps, cf.data, gax['shape'])
+            assert rel(gd.data, g_ref) < TOL[precision]
+            assert rel(sumwt, sw_ref) < TOLW[precision]
+            out = arl.degrid_visibility_from_griddata(vis, gd, cf, precision=precision)
+            assert rel(out.vis, oracle.degrid_vec(g_ref, maps, cf.data)) < TOL[precision]
+    finally:
+        arl.tune.set_tuning(**before)

@@ -41,13 +41,15 @@ def test_apply_gains(arl, oracle):
     g = (1 + 0.1 * rng.normal(size=nant)) * numpy.exp(1j * rng.uniform(-3, 3, nant))
     v = rng.normal(size=(n, 4)) + 1j * rng.normal(size=(n, 4))
     dev = torch.device('cuda')
+    # Device copies held in names until the library calls below have returned.
+    t1 = torch.as_tensor(a1, device=dev)
+    t2 = torch.as_tensor(a2, device=dev)
+    tg = torch.as_tensor(g, device=dev)
     for prec, tol in (('fp64', 1e-13), ('fp32c', 1e-6)):
         for inverse in (False, True):
             t = torch.as_tensor(v, device=dev).to(arl.device.CDTYPE[prec]).contiguous()
             arl._native.call('arlgpu_apply_gains', arl._native.ptr(t), n, 4, arl._native.PRECISIONS[prec],
-                             arl._native.ptr(torch.as_tensor(a1, device=dev)),
-                             arl._native.ptr(torch.as_tensor(a2, device=dev)),
-                             arl._native.ptr(torch.as_tensor(g, device=dev)), int(inverse),
+                             arl._native.ptr(t1), arl._native.ptr(t2), arl._native.ptr(tg), int(inverse),
                              arl._native.stream_ptr())
             gg = 1.0 / g if inverse else g
             assert rel(t.cpu().numpy(), oracle.apply_gains(v, a1, a2, gg)) < tol
