@@ -43,6 +43,8 @@ SIGNATURES = {
     'arlgpu_grid': (ctypes.c_int, [_vp, _vp, _vp, _vp, _i64, ctypes.c_int, _vp, _P(CfDesc), _vp, _P(GridDesc),
                                    _vp, _vp, _vp, _sz, _vp]),
     'arlgpu_kernel_launches': (ctypes.c_ulonglong, []),
+    'arlgpu_grid_noalloc': (ctypes.c_int, [_vp, _vp, _vp, _vp, _i64, ctypes.c_int, _vp, _P(CfDesc), _vp,
+                                           _P(GridDesc), _vp, _vp, _vp]),
     'arlgpu_set_tuning': (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     'arlgpu_get_tuning': (ctypes.c_int, [ctypes.c_char_p, _P(ctypes.c_int)]),
     'arlgpu_plan_build': (ctypes.c_int, [_vp, _vp, _i64, _P(GridDesc), _P(CfDesc), _vp, _sz, _vp, _vp]),
