@@ -354,6 +354,25 @@ template <typename R> struct PlainAcc {
     atomicAdd(&sum->x, v.x);
     atomicAdd(&sum->y, v.y);
   }
+  // Planar layout: one real value into its own plane.
+  __device__ static __forceinline__ void add1(R *sum, R *, R v) { atomicAdd(sum, v); }
+};
+
+// Planar (re / im in separate planes) compensated accumulation of one real
+// value: FP32 adds the atomic's rounding error (TwoSum on the value the atomic
+// replaced) to a compensation plane; FP64 adds directly.
+template <typename R> struct PlanarAcc;
+template <> struct PlanarAcc<float> {
+  static constexpr int kWords = 2;
+  __device__ static __forceinline__ void add1(float *sum, float *comp, float v) {
+    const float o = atomicAdd(sum, v);
+    const float s = o + v, bp = s - o;
+    atomicAdd(comp, (o - (s - bp)) + (v - bp));
+  }
+};
+template <> struct PlanarAcc<double> {
+  static constexpr int kWords = 1;
+  __device__ static __forceinline__ void add1(double *sum, double *, double v) { atomicAdd(sum, v); }
 };
 
 template <typename R> struct VisT;
@@ -941,7 +960,7 @@ __device__ __forceinline__ void row_step(RowWalk &w) {
 // K3 (lean variant): warp per row, compensated shared-memory atomics as in
 // k_grid, specialised on the polarisation count, with 32-bit incremental
 // offsets into the tap table and the subgrid.
-template <typename R, int NPOL, int NW, typename ACC = SmemAcc<R>>
+template <typename R, int NPOL, int NW, typename ACC = PlanarAcc<R>>
 __global__ void __launch_bounds__(NW * 32)
 k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
             const uint32_t *__restrict__ off, uint32_t chunk,
@@ -951,8 +970,10 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   using CT = typename Cplx<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int SG = g.SG, SG2 = SG * SG;
-  CT *sub = reinterpret_cast<CT *>(smraw);
-  CT *comp = sub + (size_t)NPOL * SG2;
+  // Planar subgrid: plane (p, c) at sub + (2 p + c) SG2, c = 0 real, 1 imaginary;
+  // FP32 keeps the compensation planes after all value planes.
+  R *sub = reinterpret_cast<R *>(smraw);
+  R *comp = sub + (size_t)2 * NPOL * SG2;
   const uint32_t nvalid = off[g.nbins];
   const uint32_t c0 = blockIdx.x * chunk;
   if (c0 >= nvalid) return;
@@ -966,15 +987,26 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
     if (!sg.direct) {
-      for (int k = threadIdx.x; k < NPOL * SG2 * ACC::kWords; k += blockDim.x) sub[k] = czero<CT>();
+      for (int k = threadIdx.x; k < 2 * NPOL * SG2 * ACC::kWords; k += blockDim.x) sub[k] = (R)0;
       __syncthreads();
     }
     double wsum[NPOL];
 #pragma unroll
     for (int p = 0; p < NPOL; ++p) wsum[p] = 0.0;
-    for (uint32_t r = pos + warp; r < sg.end; r += NW) {
-      const RowMap m = smap[r];
-      const uint32_t idx = sidx[r];
+    uint32_t r = pos + warp;
+    RowMap mnext;
+    uint32_t inext = 0;
+    if (r < sg.end) {
+      mnext = smap[r];
+      inext = sidx[r];
+    }
+    for (; r < sg.end; r += NW) {
+      const RowMap m = mnext;
+      const uint32_t idx = inext;
+      if (r + NW < sg.end) {  // next row's metadata in flight during this row
+        mnext = smap[r + NW];
+        inext = sidx[r + NW];
+      }
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
       const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
@@ -1015,7 +1047,8 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
           CT c;  // conj(tap) * vw
           c.x = tp.x * vw[p].x + tp.y * vw[p].y;
           c.y = tp.x * vw[p].y - tp.y * vw[p].x;
-          ACC::add(sub + p * SG2 + wk.so, comp + p * SG2 + wk.so, c);
+          ACC::add1(sub + 2 * p * SG2 + wk.so, comp + 2 * p * SG2 + wk.so, c.x);
+          ACC::add1(sub + (2 * p + 1) * SG2 + wk.so, comp + (2 * p + 1) * SG2 + wk.so, c.y);
         }
         row_step(wk);
       }
@@ -1029,11 +1062,13 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
     if (!sg.direct) {
       __syncthreads();
       for (int k = threadIdx.x; k < NPOL * SG2; k += blockDim.x) {
-        CT val = sub[k];
+        const int pp = k / SG2, cell = k - pp * SG2;
+        CT val;
+        val.x = sub[2 * pp * SG2 + cell];
+        val.y = sub[(2 * pp + 1) * SG2 + cell];
         if (ACC::kWords == 2) {
-          CT e = comp[k];
-          val.x += e.x;
-          val.y += e.y;
+          val.x += comp[2 * pp * SG2 + cell];
+          val.y += comp[(2 * pp + 1) * SG2 + cell];
         }
         if (val.x == (R)0 && val.y == (R)0) continue;
         const int p = k / SG2, rem = k - p * SG2, y = rem / SG, x = rem - y * SG;
@@ -1090,9 +1125,22 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       }
       __syncthreads();
     }
-    for (uint32_t r = pos + warp; r < sg.end; r += NW) {
-      const RowMap m = smap[r];
-      const uint32_t idx = sidx[r];
+    // Rows of this warp: r = pos + warp, pos + warp + NW, ...; the metadata of
+    // the next row is loaded while the current one is computed.
+    uint32_t r = pos + warp;
+    RowMap mnext;
+    uint32_t inext = 0;
+    if (r < sg.end) {
+      mnext = smap[r];
+      inext = sidx[r];
+    }
+    for (; r < sg.end; r += NW) {
+      const RowMap m = mnext;
+      const uint32_t idx = inext;
+      if (r + NW < sg.end) {
+        mnext = smap[r + NW];
+        inext = sidx[r + NW];
+      }
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
       const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
@@ -1100,50 +1148,56 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
                      ((int64_t)(vf * O + uf) * S + toff) * S + toff;
       const CT *src;
-      int pstride;
+      int64_t pstride;
       RowWalk wk;
       if (sg.direct) {
         src = gplane + (int64_t)wv * g.nx + wu;
-        pstride = 0;  // unused: direct mode indexes planes through gplane below
+        pstride = (int64_t)g.nw * plane_elems;
         wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
       } else {
         src = sub;
         pstride = SG2;
         wk = row_walk(sz, S, SG, wv - sg.v0, wu - sg.u0, lane);
       }
-      R ax[NPOL], ay[NPOL], bx[NPOL], by[NPOL];
+      R ax[NPOL], ay[NPOL];
 #pragma unroll
-      for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = bx[p] = by[p] = 0;
-      int t = lane;
-      for (; t + 32 < wk.n; t += 64) {
-        const int ko1 = wk.ko, so1 = wk.so;
-        row_step(wk);
-        const int ko2 = wk.ko, so2 = wk.so;
-        row_step(wk);
+      for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = 0;
+      // Four taps per lane per iteration: all eight loads are issued before
+      // the multiply-adds that use them.
+      for (int t = lane; t < wk.n; t += 128) {
+        int ko[4], so[4];
+        bool on[4];
 #pragma unroll
-        for (int p = 0; p < NPOL; ++p) {
-          const CT *sp = sg.direct ? src + (int64_t)p * g.nw * plane_elems : src + p * pstride;
-          const CT t1 = kb[p * ps + ko1], t2 = kb[p * ps + ko2];
-          const CT g1 = sp[so1], g2 = sp[so2];
-          ax[p] += g1.x * t1.x - g1.y * t1.y;
-          ay[p] += g1.x * t1.y + g1.y * t1.x;
-          bx[p] += g2.x * t2.x - g2.y * t2.y;
-          by[p] += g2.x * t2.y + g2.y * t2.x;
+        for (int u = 0; u < 4; ++u) {
+          on[u] = t + 32 * u < wk.n;
+          ko[u] = wk.ko;
+          so[u] = wk.so;
+          row_step(wk);
         }
-      }
-      if (t < wk.n) {
 #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
-          const CT *sp = sg.direct ? src + (int64_t)p * g.nw * plane_elems : src + p * pstride;
-          const CT t1 = kb[p * ps + wk.ko];
-          const CT g1 = sp[wk.so];
-          ax[p] += g1.x * t1.x - g1.y * t1.y;
-          ay[p] += g1.x * t1.y + g1.y * t1.x;
+          const CT *sp = src + p * pstride;
+          CT tp[4], gv[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (on[u]) {
+              tp[u] = kb[p * ps + ko[u]];
+              gv[u] = sp[so[u]];
+            } else {
+              tp[u] = czero<CT>();
+              gv[u] = czero<CT>();
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            ax[p] += gv[u].x * tp[u].x - gv[u].y * tp[u].y;
+            ay[p] += gv[u].x * tp[u].y + gv[u].y * tp[u].x;
+          }
         }
       }
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) {
-        R sx = ax[p] + bx[p], sy = ay[p] + by[p];
+        R sx = ax[p], sy = ay[p];
         for (int o = 16; o > 0; o >>= 1) {
           sx += __shfl_xor_sync(0xffffffffu, sx, o);
           sy += __shfl_xor_sync(0xffffffffu, sy, o);
@@ -1327,6 +1381,7 @@ static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const voi
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean gridder handles 1, 2 or 4 polarisations");
     smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T);
   }
+  // The lean variants' planar subgrid has the same size as the interleaved one.
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t chunk = chunk_rows();
