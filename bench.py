@@ -151,15 +151,19 @@ def measured_hbm():
         return FALLBACK_HBM_GBS, 'fallback'
 
 
-def traffic_per_row(kernel):
-    """DRAM bytes per row of `kernel` from the committed ncu summary, or None."""
-    path = os.path.join(ROOT, 'profiles', 'ncu_dram_per_row.txt')
+def launch_traffic(kernel, nrows):
+    """DRAM bytes of one `kernel` launch over nrows rows from the committed ncu
+    summary (profiles/ncu_dram.txt: kernel, rows captured, bytes), scaled by
+    rows when the capture ran on a row subsample; None when absent."""
+    path = os.path.join(ROOT, 'profiles', 'ncu_dram.txt')
     try:
         for line in open(path):
             parts = line.split()
-            if len(parts) >= 3 and parts[0] == kernel and parts[1] == 'dram_bytes_per_row':
-                return float(parts[2])
-    except OSError:
+            if len(parts) == 3 and parts[0] == kernel:
+                rows, b = float(parts[1]), float(parts[2])
+                return {'bytes': b * nrows / rows, 'captured_rows': int(rows),
+                        'scaled': rows != nrows}
+    except (OSError, ValueError):
         pass
     return None
 
@@ -470,7 +474,7 @@ def arm_gb300(args, torch, world, rank, local):
     kms = r[kern + '_ms']
     peak, peak_kind = measured_hbm()
     achieved = alg[kern] / (kms / 1e3) / 1e9
-    tr = traffic_per_row('k_' + kern)
+    tr = launch_traffic('k_' + kern, n)
     step_alg = n * (24 + 8 * npol + 4 * npol + 4) + grid_bytes + n * (24 + 4 + 8 * npol) + grid_bytes
     line = {
         'metric': METRIC, 'value': value, 'unit': 'vis/s', 'n_gpus': world, 'steps': args.steps,
@@ -484,7 +488,10 @@ def arm_gb300(args, torch, world, rank, local):
         'roofline': {'bound': 'hbm', 'kernel': 'k_' + kern, 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                      'frac': achieved / peak, 'peak_source': peak_kind + ' (MEASURED_PEAKS.json hbm_gbs)',
                      'algorithmic_bytes_per_launch': alg[kern],
-                     'traffic': None if tr is None else tr * n},
+                     'traffic': None if tr is None else tr['bytes'],
+                     'traffic_source': None if tr is None else
+                     ('ncu dram__bytes_read.sum + dram__bytes_write.sum, %d-row capture%s' %
+                      (tr['captured_rows'], ', scaled by rows' if tr['scaled'] else ''))},
         'roofline_step': {'algorithmic_bytes': step_alg, 'achieved_gbs': step_alg / (ms / 1e3) / 1e9,
                           'frac': step_alg / (ms / 1e3) / 1e9 / peak},
         'e2e': {'value': world * n / (e2e_ms / 1e3), 'unit': 'vis/s', 'h2d_bytes_per_step': h2d,
