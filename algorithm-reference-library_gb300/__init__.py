@@ -19,12 +19,13 @@ from .gridding import (DeviceVisibility, convolution_mapping, degrid_visibility_
 from .imaging import (imaging_context, imaging_contexts, invert_2d, invert_list_serial_workflow,  # noqa: F401
                       invert_wstack, invert_wstack_single, normalize_sumwt, predict_2d, predict_list_serial_workflow,
                       predict_wstack, predict_wstack_single, shift_vis_to_image, vis_null_iter, vis_wslice_iter)
-from . import autograd, tune  # noqa: F401
+from . import autograd, simulation, tune  # noqa: F401
 from .kernels import (apply_bounding_box_convolutionfunction, calculate_bounding_box_convolutionfunction,  # noqa: F401
                       copy_convolutionfunction, copy_griddata, create_awterm_convolutionfunction,
                       create_box_convolutionfunction, create_convolutionfunction_from_image,
                       create_griddata_from_image, create_griddata_on_device, create_pswf_convolutionfunction,
                       set_plane_support, support_schedule)
 from .wcs import WCS  # noqa: F401
+from .wstack import WStackImager  # noqa: F401
 
 __version__ = '0.1.0'

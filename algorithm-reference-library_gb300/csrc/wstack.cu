@@ -20,6 +20,8 @@
 //          rows of slice s.
 #include <cufft.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace arlgpu {
@@ -88,26 +90,35 @@ __global__ void k_chk_planes(const CT *grid, int64_t nplanes, int ny, int nx, do
   }
 }
 
-// image[b, y, x] = gcf * sum_s Re(wb_s * U_s * chk * s0) / sumwt[b]; U_s in FP64,
-// the w-beam in the precision of the path (CT)
+// image[b, y, x] (+)= gcf * sum_s Re(wb_s * U_s * chk * s0) / sumwt[b] over the
+// slices of flattened planes [p0, p1) (plane index b * K + s); buf holds those
+// planes' FP64 transforms.  The group holding slice 0 of image b writes it,
+// later groups add to it.  U_s in FP64, the w-beam in the precision of the
+// path (CT).
 template <typename CT>
-__global__ void k_wstack_combine(const double2 *__restrict__ grid, int nb, int K, int ny, int nx, float s0, double fov,
-                                 const double *__restrict__ wmean, const double *__restrict__ gcf,
-                                 const double *__restrict__ sumwt, double *__restrict__ image) {
-  const int64_t plane = (int64_t)ny * nx, tot = (int64_t)nb * plane;
+__global__ void k_wstack_combine(const double2 *__restrict__ buf, int64_t p0, int64_t p1, int K, int ny, int nx,
+                                 float s0, double fov, const double *__restrict__ wmean,
+                                 const double *__restrict__ gcf, const double *__restrict__ sumwt,
+                                 double *__restrict__ image) {
+  const int64_t plane = (int64_t)ny * nx;
+  const int64_t b0 = p0 / K, b1 = (p1 - 1) / K;
+  const int64_t tot = (b1 - b0 + 1) * plane;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = i / plane, yx = i - b * plane;
+    const int64_t b = b0 + i / plane, yx = i % plane;
     const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
     const double sg = (((x + y) & 1) ? -1.0 : 1.0) * (double)s0;
     const Pix px = wpix(y, x, nx, fov);
+    const int sa = (int)max((int64_t)0, p0 - b * K), sb = (int)min((int64_t)K, p1 - b * K);
     double acc = 0.0;
-    for (int s = 0; s < K; ++s) {
-      const double2 u = grid[(b * K + s) * plane + yx];
+    for (int s = sa; s < sb; ++s) {
+      const double2 u = buf[(b * K + s - p0) * plane + yx];
       const double2 wb = WB<CT>::at(px, wmean[s]);
       acc += wb.x * u.x - wb.y * u.y;
     }
+    const int64_t o = b * plane + yx;
     const double w = sumwt[b];
-    image[i] = w > 0.0 ? acc * sg * gcf[i] / w : 0.0;
+    const double v = w > 0.0 ? acc * sg * gcf[o] / w : 0.0;
+    image[o] = sa == 0 ? v : image[o] + v;
   }
 }
 
@@ -161,27 +172,47 @@ static int exec(cufftHandle h, CT *d, int dir) {
   return r == CUFFT_SUCCESS ? ARLGPU_OK : fail(ARLGPU_ERR_CUFFT, "cuFFT exec failed (%d)", (int)r);
 }
 
+// Planes per cuFFT call: batches of at most kGroupBytes of complex128, so the
+// FFT scratch (fftbuf) and cuFFT's own work area stay bounded for large grids
+// (an 8192^2 plane is 1 GiB in complex128).
+constexpr int64_t kGroupBytes = (int64_t)2 << 30;
+
+int64_t group_planes(int64_t nplanes, int ny, int nx) {
+  int64_t g = kGroupBytes / ((int64_t)ny * nx * (int64_t)sizeof(double2));
+  if (g < 1) g = 1;
+  return g < nplanes ? g : nplanes;
+}
+
 // The inverse transforms run in FP64 for both precisions (the grid correction
-// amplifies transform rounding by up to max(gcf) / min(gcf)).
+// amplifies transform rounding by up to max(gcf) / min(gcf)).  Planes go
+// through the FP64 buffer a group at a time; with precision FP64 and the grid
+// passed as fftbuf, each group is transformed where it lies in the grid.
 template <typename CT>
 static int g2i(const CT *grid, const arlgpu_grid_desc *gd, const double *gcf, const double *wmean, double fov,
-               const double *sumwt, double *image, double2 *buf, cudaStream_t st) {
+               const double *sumwt, double *image, double2 *fftbuf, cudaStream_t st) {
   const int nb = gd->nchan * gd->npol, K = gd->nw, ny = gd->ny, nx = gd->nx;
-  const int64_t nplanes = (int64_t)nb * K;
+  const int64_t nplanes = (int64_t)nb * K, plane = (int64_t)ny * nx;
   if (nplanes > 0x7fffffff) return fail(ARLGPU_ERR_UNSUPPORTED, "too many planes");
-  cufftHandle h;
-  ARL_TRY(get_plan(ny, nx, (int)nplanes, (long long)ny * nx, CUFFT_Z2Z, &h));
-  k_chk_planes<CT><<<nblk(nplanes * ny * nx), 256, 0, st>>>(grid, nplanes, ny, nx, buf);
-  ARL_LAUNCH_CHECK();
-  count_launch(1);
-  cufftResult r = cufftSetStream(h, st);
-  if (r != CUFFT_SUCCESS) return fail(ARLGPU_ERR_CUFFT, "cufftSetStream failed (%d)", (int)r);
-  ARL_TRY(exec<double2>(h, buf, CUFFT_INVERSE));
+  const bool inplace = (const void *)grid == (const void *)fftbuf;
+  const int64_t G = group_planes(nplanes, ny, nx);
   const float s0 = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
-  k_wstack_combine<CT><<<nblk((int64_t)nb * ny * nx), 256, 0, st>>>(buf, nb, K, ny, nx, s0, fov, wmean, gcf, sumwt,
-                                                                     image);
-  ARL_LAUNCH_CHECK();
-  count_launch(1);
+  for (int64_t p0 = 0; p0 < nplanes; p0 += G) {
+    const int64_t np = std::min(G, nplanes - p0);
+    double2 *buf = inplace ? fftbuf + p0 * plane : fftbuf;
+    cufftHandle h;
+    ARL_TRY(get_plan(ny, nx, (int)np, (long long)plane, CUFFT_Z2Z, &h));
+    k_chk_planes<CT><<<nblk(np * plane), 256, 0, st>>>(grid + p0 * plane, np, ny, nx, buf);
+    ARL_LAUNCH_CHECK();
+    count_launch(1);
+    cufftResult r = cufftSetStream(h, st);
+    if (r != CUFFT_SUCCESS) return fail(ARLGPU_ERR_CUFFT, "cufftSetStream failed (%d)", (int)r);
+    ARL_TRY(exec<double2>(h, buf, CUFFT_INVERSE));
+    const int64_t nbt = (p0 + np - 1) / K - p0 / K + 1;
+    k_wstack_combine<CT><<<nblk(nbt * plane), 256, 0, st>>>(buf, p0, p0 + np, K, ny, nx, s0, fov, wmean, gcf,
+                                                             sumwt, image);
+    ARL_LAUNCH_CHECK();
+    count_launch(1);
+  }
   return ARLGPU_OK;
 }
 
@@ -189,20 +220,24 @@ template <typename CT>
 static int i2g(const double *image, const double *gcf, const double *wmean, double fov, const arlgpu_grid_desc *gd,
                CT *grid, cudaStream_t st) {
   const int nb = gd->nchan * gd->npol, K = gd->nw, ny = gd->ny, nx = gd->nx;
-  const int64_t nplanes = (int64_t)nb * K;
+  const int64_t nplanes = (int64_t)nb * K, plane = (int64_t)ny * nx;
   if (nplanes > 0x7fffffff) return fail(ARLGPU_ERR_UNSUPPORTED, "too many planes");
-  cufftHandle h;
-  ARL_TRY(get_plan(ny, nx, (int)nplanes, (long long)ny * nx, sizeof(CT) == 8 ? CUFFT_C2C : CUFFT_Z2Z, &h));
-  k_wstack_pre_predict<CT><<<nblk((int64_t)nb * ny * nx), 256, 0, st>>>(image, gcf, nb, K, ny, nx, fov, wmean, grid);
+  k_wstack_pre_predict<CT><<<nblk((int64_t)nb * plane), 256, 0, st>>>(image, gcf, nb, K, ny, nx, fov, wmean, grid);
   ARL_LAUNCH_CHECK();
   count_launch(1);
-  cufftResult r = cufftSetStream(h, st);
-  if (r != CUFFT_SUCCESS) return fail(ARLGPU_ERR_CUFFT, "cufftSetStream failed (%d)", (int)r);
-  ARL_TRY(exec<CT>(h, grid, CUFFT_FORWARD));
+  const int64_t G = group_planes(nplanes, ny, nx);
   const float s0 = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
-  k_chk_scale<CT><<<nblk(nplanes * ny * nx), 256, 0, st>>>(grid, nplanes, ny, nx, s0);
-  ARL_LAUNCH_CHECK();
-  count_launch(1);
+  for (int64_t p0 = 0; p0 < nplanes; p0 += G) {
+    const int64_t np = std::min(G, nplanes - p0);
+    cufftHandle h;
+    ARL_TRY(get_plan(ny, nx, (int)np, (long long)plane, sizeof(CT) == 8 ? CUFFT_C2C : CUFFT_Z2Z, &h));
+    cufftResult r = cufftSetStream(h, st);
+    if (r != CUFFT_SUCCESS) return fail(ARLGPU_ERR_CUFFT, "cufftSetStream failed (%d)", (int)r);
+    ARL_TRY(exec<CT>(h, grid + p0 * plane, CUFFT_FORWARD));
+    k_chk_scale<CT><<<nblk(np * plane), 256, 0, st>>>(grid + p0 * plane, np, ny, nx, s0);
+    ARL_LAUNCH_CHECK();
+    count_launch(1);
+  }
   return ARLGPU_OK;
 }
 
@@ -230,6 +265,14 @@ extern "C" int arlgpu_wstack_grid_to_image(const void *grid, const arlgpu_grid_d
   if (precision == ARLGPU_FP64)
     return g2i<double2>(static_cast<const double2 *>(grid), gd, gcf, wmean, fov, sumwt, image, buf, st);
   return g2i<float2>(static_cast<const float2 *>(grid), gd, gcf, wmean, fov, sumwt, image, buf, st);
+}
+
+extern "C" int arlgpu_wstack_fftbuf_bytes(const arlgpu_grid_desc *gd, size_t *bytes) {
+  ARL_TRY(check(gd, ARLGPU_FP64));
+  if (!bytes) return fail(ARLGPU_ERR_INVALID, "null bytes");
+  const int64_t nplanes = (int64_t)gd->nchan * gd->npol * gd->nw;
+  *bytes = (size_t)group_planes(nplanes, gd->ny, gd->nx) * gd->ny * gd->nx * sizeof(double2);
+  return ARLGPU_OK;
 }
 
 extern "C" int arlgpu_wstack_image_to_grid(const double *image, const double *gcf, const double *wmean,

@@ -25,6 +25,7 @@ from . import device as dv
 from .data_models import Image, Visibility, copy_visibility, create_empty_image_like, create_visibility_from_rows
 from .gridding import DeviceVisibility, _assert_in_grid, _gcf_t, _rows
 from .kernels import create_pswf_convolutionfunction, _grid_wcs
+from .wstack import WStackImager, invert_to_host, slice_axis as _slice_axis
 
 
 def get_parameter(kwargs, key, default=None):
@@ -169,103 +170,36 @@ def vis_wslice_iter(vis, vis_slices=1):
 # ---------------------------------------------------------------------------
 # W-stacking
 # ---------------------------------------------------------------------------
-def _slice_axis(w_t, vis_slices):
-    """WW grid axis (crval, crpix, cdelt) whose round-to-nearest plane index is
-    the ``vis_wslice_iter`` slice: boxes linspace(-wmax, wmax, K), a row in slice
-    s when |w - box_s| < step/2 (``visibility/iterators.py:91-109``)."""
-    wmax = float(w_t.abs().max().item()) if w_t.numel() else 0.0
-    if vis_slices > 1:
-        step = (2.0 * wmax) / (vis_slices - 1)
-    else:
-        step = 2.0 * wmax
-    if step == 0.0:
-        step = 1e15
-    return -wmax, 1.0, step
-
-
-def _wstack_setup(vis, im, vis_slices, gcfcf, precision, device, kwargs):
-    gcf, cf = gcfcf if gcfcf is not None else create_pswf_convolutionfunction(im)
-    if cf.shape[2] != 1:
-        raise NotImplementedError('batched w-stacking grids with a 2-D kernel (nz == 1); use invert_wstack_single '
-                                  'per slice for w-stacking with w-projection kernels')
-    uvw, f, v, w = _rows(vis, precision, device)
-    nchan, npol, ny, nx = im.shape
-    gwcs = _grid_wcs(im, vis_slices, 1e15)
-    crval, crpix, cdelt = _slice_axis(uvw[:, 2], vis_slices)
-    gwcs.wcs.crval[2], gwcs.wcs.crpix[2], gwcs.wcs.cdelt[2] = crval, crpix, cdelt
-    gd = dv.grid_desc(gwcs, (nchan, npol, vis_slices, ny, nx))
-    cf_t, cs, ps, psup = dv.device_cf(cf, precision, device)
-    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup)
-    ws = dv.WORKSPACE.get(dv.plan_bytes(uvw.shape[0], gd, cd), device)
-    n_bad = torch.zeros(1, dtype=torch.int64, device=device)
-    nat.call('arlgpu_plan_build', nat.ptr(uvw), nat.ptr(f), uvw.shape[0], ctypes.byref(gd), ctypes.byref(cd),
-             nat.ptr(ws), ws.numel(), nat.ptr(n_bad), nat.stream_ptr())
-    wmean = torch.empty(vis_slices, dtype=torch.float64, device=device)
-    nat.call('arlgpu_plan_plane_mean_w', nat.ptr(uvw), uvw.shape[0], ctypes.byref(gd), ctypes.byref(cd),
-             nat.ptr(ws), ws.numel(), nat.ptr(wmean), nat.stream_ptr())
-    # Rows outside every slice are dropped as vis_wslice_iter drops them (only
-    # possible for vis_slices == 1); any other rejected row is outside the grid.
-    pw = torch.round((uvw[:, 2] - crval) / cdelt + crpix - 1.0)
-    n_outside = int(((pw < 0) | (pw >= vis_slices)).sum().item())
-    nb = int(n_bad.item())
-    assert nb == n_outside, "%d visibilities fall outside the grid or convolution function" % (nb - n_outside)
-    cellsize = abs(float(im.wcs.wcs.cdelt[0])) * numpy.pi / 180.0
-    return dict(gcf=gcf, cf=cf, uvw=uvw, f=f, v=v, w=w, gd=gd, cd=cd, cf_t=cf_t, ws=ws, wmean=wmean,
-                cellsize=cellsize)
-
-
 def invert_wstack(vis, im, vis_slices, dopsf=False, normalize=True, gcfcf=None, precision=None, **kwargs):
     """W-stack invert over all slices at once: equals ``invert_list_serial_workflow``
     with context 'wstack' (imaging_serial.py:186-197): sum_s sumwt_s * invert_wstack_single_s,
-    normalised by sum_s sumwt_s.  One gridder launch, one batched FFT, one combine."""
-    precision = dv.resolve_precision(precision)
-    device = dv.require_cuda()
-    s = _wstack_setup(vis, im, vis_slices, gcfcf, precision, device, kwargs)
-    gd, cd = s['gd'], s['cd']
-    nchan, npol, ny, nx = im.shape
-    v = torch.ones_like(s['v']) if dopsf else s['v']
-    grid_t = torch.empty((nchan, npol, vis_slices, ny, nx), dtype=dv.CDTYPE[precision], device=device)
-    sumwt = torch.empty((nchan, npol), dtype=torch.float64, device=device)
-    nat.call('arlgpu_grid_planned', nat.ptr(v), nat.ptr(s['w']), s['uvw'].shape[0], nat.PRECISIONS[precision],
-             nat.ptr(s['cf_t']), ctypes.byref(cd), nat.ptr(grid_t), ctypes.byref(gd), nat.ptr(sumwt),
-             nat.ptr(s['ws']), s['ws'].numel(), nat.stream_ptr())
-    image = torch.empty((nchan, npol, ny, nx), dtype=torch.float64, device=device)
-    norm = sumwt if normalize else torch.ones_like(sumwt)
-    fftbuf = grid_t if precision == 'fp64' else torch.empty(grid_t.shape, dtype=torch.complex128, device=device)
-    gcf_d = _gcf_t(s['gcf'], device)
-    nat.call('arlgpu_wstack_grid_to_image', nat.ptr(grid_t), ctypes.byref(gd), nat.PRECISIONS[precision],
-             nat.ptr(gcf_d), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),
-             nat.ptr(fftbuf), nat.stream_ptr())
-    host = not isinstance(vis, DeviceVisibility)
-    out = Image(image.cpu().numpy() if host else image, im.wcs.deepcopy(), im.polarisation_frame)
-    return out, (sumwt.cpu().numpy() if host else sumwt)
+    normalised by sum_s sumwt_s.  One gridder launch, batched FFTs, one combine."""
+    imager = WStackImager(vis, im, vis_slices, gcfcf=gcfcf, precision=precision)
+    image, sumwt = invert_to_host(imager, vis, dopsf, normalize)
+    return Image(image, im.wcs.deepcopy(), im.polarisation_frame), sumwt
 
 
 def predict_wstack(vis, model, vis_slices, gcfcf=None, precision=None, **kwargs):
     """W-stack predict over all slices at once: equals ``predict_list_serial_workflow``
     with context 'wstack' (each slice's rows get predict_wstack_single's values)."""
-    precision = dv.resolve_precision(precision)
-    device = dv.require_cuda()
-    s = _wstack_setup(vis, model, vis_slices, gcfcf, precision, device, kwargs)
-    gd, cd = s['gd'], s['cd']
-    nchan, npol, ny, nx = model.shape
-    d = model.data
-    m_t = d.to(device=device, dtype=torch.float64).contiguous() if isinstance(d, torch.Tensor) else \
-        dv.to_device(numpy.asarray(d, numpy.float64), torch.float64, device)
-    grid_t = torch.empty((nchan, npol, vis_slices, ny, nx), dtype=dv.CDTYPE[precision], device=device)
-    gcf_d = _gcf_t(s['gcf'], device)
-    nat.call('arlgpu_wstack_image_to_grid', nat.ptr(m_t), nat.ptr(gcf_d), nat.ptr(s['wmean']),
-             s['cellsize'], ctypes.byref(gd), nat.PRECISIONS[precision], nat.ptr(grid_t), nat.stream_ptr())
-    out = torch.empty((s['uvw'].shape[0], npol), dtype=dv.CDTYPE[precision], device=device)
-    nat.call('arlgpu_degrid_planned', s['uvw'].shape[0], nat.PRECISIONS[precision], nat.ptr(s['cf_t']),
-             ctypes.byref(cd), nat.ptr(grid_t), ctypes.byref(gd), nat.ptr(out), nat.ptr(s['ws']), s['ws'].numel(),
-             nat.stream_ptr())
+    imager = WStackImager(vis, model, vis_slices, gcfcf=gcfcf, precision=precision)
+    out = imager.predict(model.data)
     if isinstance(vis, DeviceVisibility):
-        return DeviceVisibility(vis.uvw, vis.frequency, out, vis.imaging_weight, vis.polarisation_frame,
+        return DeviceVisibility(vis.uvw, vis.frequency, out.clone(), vis.imaging_weight, vis.polarisation_frame,
                                 vis.phasecentre)
     newvis = copy_visibility(vis, zero=True)
     newvis.data['vis'][...] = out.cpu().numpy()
     return newvis
+
+
+def _wstack_fftbuf(gd, grid_t, precision, device):
+    """FP64 transform scratch of the w-stack invert: the grid itself on the FP64
+    path, else a buffer of the size the library asks for (one group of planes)."""
+    if precision == 'fp64':
+        return grid_t
+    nbytes = ctypes.c_size_t(0)
+    nat.call('arlgpu_wstack_fftbuf_bytes', ctypes.byref(gd), ctypes.byref(nbytes))
+    return torch.empty(nbytes.value // 16, dtype=torch.complex128, device=device)
 
 
 def invert_wstack_single(vis, im, dopsf, normalize=True, remove=True, gcfcf=None, precision=None, **kwargs):
@@ -310,7 +244,7 @@ def _single_slice_invert(vis, im, dopsf, normalize, gcfcf, precision):
              nat.ptr(s['ws']), s['ws'].numel(), nat.stream_ptr())
     image = torch.empty((nchan, npol, ny, nx), dtype=torch.float64, device=device)
     norm = sumwt if normalize else torch.ones_like(sumwt)
-    fftbuf = grid_t if precision == 'fp64' else torch.empty(grid_t.shape, dtype=torch.complex128, device=device)
+    fftbuf = _wstack_fftbuf(gd, grid_t, precision, device)
     gcf_d = _gcf_t(s['gcf'], device)
     nat.call('arlgpu_wstack_grid_to_image', nat.ptr(grid_t), ctypes.byref(gd), nat.PRECISIONS[precision],
              nat.ptr(gcf_d), nat.ptr(s['wmean']), s['cellsize'], nat.ptr(norm), nat.ptr(image),

@@ -97,17 +97,82 @@ def predict_point_sources(uvw, l, m, flux, npol=1, device=None, dtype=torch.comp
 
 
 WORKLOADS = {
+    # Plain 2-D imaging, PSWF kernel, no w-correction (w used as is, one plane).
     'C1': dict(nants=64, radius=1000.0, ntimes=60, freqs=[1e8], npol=1, npixel=512, cellsize=1e-3,
                kernel='pswf', support=8, oversampling=8, nsources=10, seed=1001),
+    # W-projection, 64 w-kernel planes whose support grows 8 -> 32 with |w|.
     'C2': dict(nants=256, radius=5000.0, ntimes=120, freqs=list(numpy.linspace(100e6, 120e6, 4)), npol=1,
                npixel=1024, cellsize=5e-4, kernel='wproj', nwplanes=64, support=32, support_min=8,
                oversampling=8, nsources=50, seed=1002),
+    # Batched w-stacking, 4 polarisations, 64 channels with seeded per-channel
+    # flagging of U(0, 0.6) of the rows (flagged rows dropped), channels summed
+    # into one image (multi-frequency synthesis).
+    'C3': dict(nants=512, radius=10000.0, ntimes=12, freqs=list(numpy.linspace(100e6, 130e6, 64)), npol=4,
+               npixel=4096, cellsize=5e-5, kernel='pswf', support=8, oversampling=16, nsources=20,
+               source_radius=0.08, vis_slices=20, flag_max=0.6, mfs=True, seed=1003),
+    # Differentiable predict + gain solve: the model is an image of Gaussian-
+    # smoothed point sources; observed visibilities come from the gridded
+    # predict of that model with per-antenna gains and Gaussian noise.
+    'C4': dict(nants=128, radius=2000.0, ntimes=240, freqs=list(numpy.linspace(100e6, 120e6, 8)), npol=1,
+               npixel=2048, cellsize=3e-4, kernel='pswf', support=8, oversampling=8, nsources=200,
+               source_radius=0.25, smooth_px=2.0, gain_amp_sigma=0.1, noise=0.01, mfs=True, model='image',
+               seed=1004),
+    # Large single-GPU stress: ~1e8 rows, 8192^2 grid, 32 w-stack planes.
+    'C5': dict(nants=512, radius=40000.0, ntimes=3, freqs=list(numpy.linspace(100e6, 150e6, 256)), npol=1,
+               npixel=8192, cellsize=1.2e-5, kernel='pswf', support=8, oversampling=16, nsources=20,
+               source_radius=0.04, vis_slices=32, mfs=True, seed=1005),
 }
 
 
+def flag_rows(freq, freqs, flag_max, rng):
+    """Keep-mask of per-channel flagging: channel c drops each of its rows with
+    probability f_c ~ U(0, flag_max) (ARL's Visibility has no flag column, so
+    flagged rows are removed)."""
+    frac = rng.uniform(0.0, flag_max, len(freqs))
+    ch = numpy.searchsorted(numpy.asarray(freqs), freq)
+    return rng.uniform(size=freq.shape[0]) >= frac[ch]
+
+
+def smoothed_point_image(npixel, cellsize, nsources, radius, sigma_px, rng, fmin=0.1, fmax=10.0):
+    """[1, 1, npixel, npixel] image of nsources point sources (random pixels
+    within +/-radius rad of the centre, flux log-uniform in [fmin, fmax]) each
+    smoothed by a unit-sum Gaussian of sigma_px pixels."""
+    half = int(radius / cellsize)
+    c = npixel // 2
+    img = numpy.zeros((npixel, npixel))
+    ys = rng.integers(c - half, c + half, nsources)
+    xs = rng.integers(c - half, c + half, nsources)
+    flux = numpy.exp(rng.uniform(numpy.log(fmin), numpy.log(fmax), nsources))
+    numpy.add.at(img, (ys, xs), flux)
+    r = int(numpy.ceil(4 * sigma_px))
+    k = numpy.exp(-0.5 * (numpy.arange(-r, r + 1) / sigma_px) ** 2)
+    k /= k.sum()
+    img = numpy.apply_along_axis(lambda a: numpy.convolve(a, k, mode='same'), 0, img)
+    img = numpy.apply_along_axis(lambda a: numpy.convolve(a, k, mode='same'), 1, img)
+    return img[None, None]
+
+
+def antenna_gains(nants, amp_sigma, rng):
+    """Complex per-antenna gains: amplitude N(1, amp_sigma), phase U(-pi, pi)."""
+    return rng.normal(1.0, amp_sigma, nants) * numpy.exp(1j * rng.uniform(-numpy.pi, numpy.pi, nants))
+
+
+def observe(model_vis, gains, a1, a2, noise, seed):
+    """V_obs = g[a2] conj(g[a1]) M + n, n complex Gaussian of std `noise` per
+    component (torch, on model_vis's device; gains, a1, a2 tensors there)."""
+    gen = torch.Generator(device=model_vis.device).manual_seed(seed)
+    rdt = torch.float64 if model_vis.dtype == torch.complex128 else torch.float32
+    nr = torch.randn(model_vis.shape, dtype=rdt, device=model_vis.device, generator=gen)
+    ni = torch.randn(model_vis.shape, dtype=rdt, device=model_vis.device, generator=gen)
+    gg = (gains[a2] * torch.conj(gains[a1])).to(model_vis.dtype)[:, None]
+    return gg * model_vis + noise * torch.complex(nr, ni)
+
+
 def make_workload(name, max_rows=None, device=None, rng_seed=None):
-    """Rows, vis and image geometry of a named workload (after the uv-cut).
-    ``max_rows`` keeps a seeded random subset of rows (for the CPU oracle)."""
+    """Rows, vis and image geometry of a named workload (after the uv-cut and
+    any flagging).  ``max_rows`` keeps a seeded random subset of rows (for the
+    CPU oracle).  Workloads with ``model='image'`` carry a model image and
+    antenna gains instead of point-source visibilities (``vis`` is None)."""
     cfg = dict(WORKLOADS[name])
     rng = numpy.random.default_rng(cfg['seed'] if rng_seed is None else rng_seed)
     xyz = antennas_in_disk(cfg['nants'], cfg['radius'], rng)
@@ -115,17 +180,38 @@ def make_workload(name, max_rows=None, device=None, rng_seed=None):
     uvw, freq, a1, a2, tix = rows(xyz, ha, cfg['freqs'])
     keep = uv_cut(uvw, cfg['npixel'], cfg['cellsize'], cfg['support'])
     nrows_generated = uvw.shape[0]
+    if cfg.get('flag_max'):
+        keep &= flag_rows(freq, cfg['freqs'], cfg['flag_max'], numpy.random.default_rng(cfg['seed'] + 3))
     uvw, freq, a1, a2, tix = uvw[keep], freq[keep], a1[keep], a2[keep], tix[keep]
+    del keep
     if max_rows is not None and uvw.shape[0] > max_rows:
         sel = numpy.sort(numpy.random.default_rng(cfg['seed'] + 7).choice(uvw.shape[0], max_rows, replace=False))
         uvw, freq, a1, a2, tix = uvw[sel], freq[sel], a1[sel], a2[sel], tix[sel]
-    l, m, flux = point_sources(cfg['nsources'], rng)
-    vis = predict_point_sources(uvw, l, m, flux, cfg['npol'], device=device)
-    out = dict(cfg, uvw=numpy.ascontiguousarray(uvw), frequency=freq, antenna1=a1, antenna2=a2, time_index=tix,
-               vis=vis, weight=numpy.ones((uvw.shape[0], cfg['npol'])), nrows_generated=nrows_generated,
-               sources=(l, m, flux))
+    uvw = numpy.ascontiguousarray(uvw)
+    out = dict(cfg, uvw=uvw, frequency=freq, antenna1=a1, antenna2=a2, time_index=tix,
+               nrows_generated=nrows_generated)
     freqs = numpy.asarray(cfg['freqs'])
     out['channel_bandwidth'] = float(freqs[1] - freqs[0]) if len(freqs) > 1 else 1e6
+    if cfg.get('mfs'):
+        # One image channel whose FREQ pixel is wide enough that every row's
+        # channel rounds to it: the channels are summed on the grid.
+        out['image_frequency'] = [float(freqs.mean())]
+        out['image_bandwidth'] = float(2.0 * (freqs.max() - freqs.min()) + out['channel_bandwidth'])
+    else:
+        out['image_frequency'] = list(cfg['freqs'])
+        out['image_bandwidth'] = out['channel_bandwidth']
+    # Natural weighting: unit weights (a read-only broadcast view; index or
+    # copy it before writing).
+    out['weight'] = numpy.broadcast_to(numpy.ones(1), (uvw.shape[0], cfg['npol']))
+    if cfg.get('model') == 'image':
+        out['vis'] = None
+        out['model_image'] = smoothed_point_image(cfg['npixel'], cfg['cellsize'], cfg['nsources'],
+                                                  cfg['source_radius'], cfg['smooth_px'], rng)
+        out['gains'] = antenna_gains(cfg['nants'], cfg['gain_amp_sigma'], rng)
+    else:
+        l, m, flux = point_sources(cfg['nsources'], rng, radius=cfg.get('source_radius', 0.1))
+        out['vis'] = predict_point_sources(uvw, l, m, flux, cfg['npol'], device=device)
+        out['sources'] = (l, m, flux)
     if cfg['kernel'] == 'wproj':
         wmax = numpy.max(numpy.abs(uvw[:, 2]))
         nwp = cfg['nwplanes']
@@ -136,3 +222,14 @@ def make_workload(name, max_rows=None, device=None, rng_seed=None):
         s = from_min + (to_max - from_min) * w / w.max()
         out['plane_support'] = (2 * numpy.ceil(s / 2)).astype(numpy.int32).clip(from_min, to_max)
     return out
+
+
+def workload_image(arl, w):
+    """Template image of a workload (phase centre at dec -45 deg, the
+    observation's pointing), with the workload's polarisation count."""
+    frame = {1: 'stokesI', 2: 'linearnp', 4: 'linear'}[w['npol']]
+    return arl.create_image(npixel=w['npixel'], cellsize=w['cellsize'],
+                            frequency=numpy.asarray(w['image_frequency']),
+                            channel_bandwidth=numpy.array([w['image_bandwidth']]),
+                            polarisation_frame=arl.PolarisationFrame(frame),
+                            phasecentre=arl.PhaseCentre(0.0, -45.0))

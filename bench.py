@@ -51,6 +51,8 @@ def parse():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline')
     ap.add_argument('--cpu-seconds', type=float, default=12.0, help='CPU-baseline time budget')
     ap.add_argument('--no-tune', action='store_true', help='keep the library\'s default kernel variants')
+    ap.add_argument('--no-stages', action='store_true',
+                    help='skip the invert_2d / predict_2d / gradient-step rates')
     ap.add_argument('--profile-rows', type=int, default=0,
                     help='profiling case for ncu: the workload subsampled to this many rows, --warmup + --steps '
                          'untimed steps with the library defaults, no other arms')
@@ -191,7 +193,7 @@ def build_context(arl, torch, w, precision, device):
     ctx['uvw'] = torch.as_tensor(w['uvw'], device=device)
     ctx['freq'] = torch.as_tensor(w['frequency'], device=device)
     ctx['vis'] = w['vis'].to(device=device, dtype=dv.CDTYPE[precision]).contiguous()
-    ctx['wt'] = torch.as_tensor(w['weight'], device=device).to(dv.RDTYPE[precision]).contiguous()
+    ctx['wt'] = torch.ones((w['uvw'].shape[0], w['npol']), dtype=dv.RDTYPE[precision], device=device)
     ctx['grid'] = torch.empty((gd.nchan, gd.npol, gd.nw, gd.ny, gd.nx), dtype=dv.CDTYPE[precision], device=device)
     ctx['sumwt'] = torch.empty((gd.nchan, gd.npol), dtype=torch.float64, device=device)
     ctx['out'] = torch.empty((n, npol), dtype=dv.CDTYPE[precision], device=device)
@@ -279,6 +281,99 @@ def e2e_steps(arl, torch, ctx, steps, warmup):
     torch.cuda.synchronize()
     del dev
     return e0.elapsed_time(e1) / steps, h2d, d2h
+
+
+def _events(torch, n):
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
+def stage_rates(arl, torch, ctx, steps, warmup, flush):
+    """vis/s of invert_2d (plan + grid + FP64 inverse FFT with grid correction
+    and sumwt normalisation) and predict_2d (gcf multiply + forward FFT +
+    degrid) on the bench's device-resident rows; L2 flushed between steps."""
+    nat = arl._native
+    P = nat.PRECISIONS[ctx['precision']]
+    gd, cd, ws = ctx['gd'], ctx['cd'], ctx['ws']
+    dev = ctx['uvw'].device
+    gcf = arl.gridding._gcf_t(ctx['gcf'], dev)
+    nb = gd.nchan * gd.npol
+    image = torch.empty((gd.nchan, gd.npol, gd.ny, gd.nx), dtype=torch.float64, device=dev)
+    fftbuf = torch.empty(nb * gd.ny * gd.nx, dtype=torch.complex128, device=dev)
+    model = torch.zeros_like(image)
+    model[..., gd.ny // 2 - 40:gd.ny // 2 + 40:7, gd.nx // 2 - 40:gd.nx // 2 + 40:5] = 1.0
+    stream = torch.cuda.current_stream()
+    sp = nat.stream_ptr()
+
+    def invert():
+        nat.call('arlgpu_plan_build', nat.ptr(ctx['uvw']), nat.ptr(ctx['freq']), ctx['n'], ctypes.byref(gd),
+                 ctypes.byref(cd), nat.ptr(ws), ws.numel(), nat.ptr(ctx['nbad']), sp)
+        nat.call('arlgpu_grid_planned', nat.ptr(ctx['vis']), nat.ptr(ctx['wt']), ctx['n'], P, nat.ptr(ctx['cf_t']),
+                 ctypes.byref(cd), nat.ptr(ctx['grid']), ctypes.byref(gd), nat.ptr(ctx['sumwt']), nat.ptr(ws),
+                 ws.numel(), sp)
+        nat.call('arlgpu_fft_grid_to_image', nat.ptr(ctx['grid']), ctypes.byref(gd), P, nat.ptr(gcf),
+                 nat.ptr(ctx['sumwt']), nat.ptr(image), None, nat.ptr(fftbuf), sp)
+
+    def predict():
+        nat.call('arlgpu_plan_build', nat.ptr(ctx['uvw']), nat.ptr(ctx['freq']), ctx['n'], ctypes.byref(gd),
+                 ctypes.byref(cd), nat.ptr(ws), ws.numel(), nat.ptr(ctx['nbad']), sp)
+        nat.call('arlgpu_fft_image_to_grid', nat.ptr(model), nat.ptr(gcf), ctypes.byref(gd), P, nat.ptr(ctx['grid']),
+                 sp)
+        nat.call('arlgpu_degrid_planned', ctx['n'], P, nat.ptr(ctx['cf_t']), ctypes.byref(cd), nat.ptr(ctx['grid']),
+                 ctypes.byref(gd), nat.ptr(ctx['out']), nat.ptr(ws), ws.numel(), sp)
+
+    out = {}
+    for name, fn in (('invert_2d', invert), ('predict_2d', predict)):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ev = [_events(torch, 2) for _ in range(steps)]
+        for k in range(steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            fn()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+        out[name] = {'value': ctx['n'] / (ms / 1e3), 'unit': 'vis/s', 'ms': ms}
+    return out
+
+
+def gradient_step_rate(arl, torch, device, steps, warmup, flush):
+    """vis/s of one chi^2 gradient step of the gain-solve workload (C4: 128
+    antennas, 8 channels summed onto a 2048^2 image, 240 times, PSWF 8 x 8):
+    predict (FFT + degrid), the gain chi^2 with its Wirtinger gradients, and
+    the adjoint (grid + FFT) for the image gradient, FP32C."""
+    sim = arl.simulation
+    w = sim.make_workload('C4')
+    im = sim.workload_image(arl, w)
+    gcfcf = arl.create_pswf_convolutionfunction(im, oversampling=w['oversampling'], support=w['support'])
+    n = w['uvw'].shape[0]
+    dvis = arl.DeviceVisibility(torch.as_tensor(w['uvw'], device=device),
+                                torch.as_tensor(w['frequency'], device=device),
+                                torch.zeros((n, 1), dtype=torch.complex64, device=device),
+                                torch.ones((n, 1), dtype=torch.float32, device=device))
+    op = arl.autograd.GriddingOperator(dvis, im, gcfcf, precision='fp32c')
+    model = torch.as_tensor(w['model_image'], device=device)
+    gains = torch.as_tensor(w['gains'], device=device)
+    a1 = torch.as_tensor(w['antenna1'].astype(numpy.int32), device=device)
+    a2 = torch.as_tensor(w['antenna2'].astype(numpy.int32), device=device)
+    vobs = sim.observe(op.predict(model), gains, a1, a2, w['noise'], seed=1004)
+    x = 0.7 * model
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        arl.autograd.gain_chi2_step(x, gains, vobs, op, a1, a2)
+    torch.cuda.synchronize()
+    ev = [_events(torch, 2) for _ in range(steps)]
+    for k in range(steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        arl.autograd.gain_chi2_step(x, gains, vobs, op, a1, a2)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    return {'value': n / (ms / 1e3), 'unit': 'vis/s', 'ms': ms,
+            'workload': 'C4 gain solve: 128 antennas / 2 km disk, 8 chan 100-120 MHz summed, 240 times, 2048^2, '
+                        'PSWF S=8 O=8, %d rows; chi^2 + image and gain gradients, FP32C' % n}
 
 
 # ---------------------------------------------------------------------------
@@ -463,6 +558,12 @@ def arm_gb300(args, torch, world, rank, local):
         torch.cuda.empty_cache()
 
     e2e_ms, h2d, d2h = e2e_steps(arl, torch, ctx, max(3, args.steps // 2), 2)
+    stages = None
+    if not args.no_stages:
+        stages = {'grid': {'value': n / (r['grid_ms'] / 1e3), 'unit': 'vis/s', 'ms': r['grid_ms']},
+                  'degrid': {'value': n / (r['degrid_ms'] / 1e3), 'unit': 'vis/s', 'ms': r['degrid_ms']}}
+        stages.update(stage_rates(arl, torch, ctx, max(3, args.steps // 2), 2, flush))
+        stages['gradient_step'] = gradient_step_rate(arl, torch, device, 3, 2, flush)
     e2e_ms = max_over_ranks(torch, world, e2e_ms)
 
     # Roofline of the dominant kernel (grid or degrid launch), HBM-bound.
@@ -497,6 +598,7 @@ def arm_gb300(args, torch, world, rank, local):
         'e2e': {'value': world * n / (e2e_ms / 1e3), 'unit': 'vis/s', 'h2d_bytes_per_step': h2d,
                 'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_ms, 'path': 'C ABI, pinned host buffers'},
         'gpu_launches': r['launches'],
+        'stages': stages,
         'clocks': clk,
         'autotune': tuned,
     }

@@ -184,10 +184,15 @@ int arlgpu_fft_image_to_grid(const double *image, const double *gcf, const arlgp
  * cellsize the image cell (radians).
  * arlgpu_wstack_grid_to_image: image = gcf * sum_s Re(wbeam(wmean[s]) * ifft_s) * nx*ny / sumwt,
  *   i.e. the sumwt-weighted sum of the slices' invert_wstack_single images divided by
- *   the total sumwt [nchan][npol].  fftbuf: nchan*npol*nw*ny*nx complex128 scratch (the
- *   transforms run in FP64); with precision FP64 it may be the grid itself.
+ *   the total sumwt [nchan][npol].  fftbuf: complex128 scratch of
+ *   arlgpu_wstack_fftbuf_bytes() bytes (the transforms run in FP64, on groups of
+ *   planes of at most 2 GiB of complex128 each); with precision FP64 the grid itself
+ *   may be passed instead (it is then destroyed).
  * arlgpu_wstack_image_to_grid: plane s = fft(conj(wbeam(wmean[s])) * image * gcf), so one
- *   degrid over all rows is predict_wstack_single summed over the slices. */
+ *   degrid over all rows is predict_wstack_single summed over the slices.
+ * arlgpu_wstack_fftbuf_bytes: bytes of fftbuf for a grid of shape gd (no reference
+ *   counterpart: the reference transforms one slice at a time in NumPy). */
+int arlgpu_wstack_fftbuf_bytes(const arlgpu_grid_desc *gd, size_t *bytes);
 int arlgpu_wstack_grid_to_image(const void *grid, const arlgpu_grid_desc *gd, int precision, const double *gcf,
                                 const double *wmean, double cellsize, const double *sumwt, double *image,
                                 void *fftbuf, void *stream);

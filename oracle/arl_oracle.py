@@ -203,6 +203,44 @@ def degrid_vec(grid, maps, cf, chunk=1 << 15):
     return out
 
 
+def window_index(maps, gshape, S):
+    """Flat indices [nvis, npol, S, S] of each row's S x S window in a grid of
+    shape gshape: the slice ``grid[c, p, zg, pv-S/2:pv+S/2, pu-S/2:pu+S/2]`` of
+    ``gridding.py:128`` and ``:261``."""
+    pu, pu_off, pv, pv_off, pwg, pwc, pfreq = maps
+    nchan, npol, nw, ny, nx = gshape
+    jj = np.arange(S) - S // 2
+    base = ((pfreq[:, None] * npol + np.arange(npol)[None, :]) * nw + pwg[:, None]) * ny
+    rows = (base[:, :, None] + pv[:, None, None] + jj[None, None, :]) * nx
+    return rows[:, :, :, None] + (pu[:, None, None, None] + jj[None, None, None, :])
+
+
+def grid_sparse(vis, wt, maps, cf, gshape):
+    """``grid_vec`` restricted to the cells the rows touch, for grids too large
+    to hold densely: (sorted flat cell indices, complex128 cell values, sumwt)."""
+    pu, pu_off, pv, pv_off, pwg, pwc, pfreq = maps
+    nchan, npol = gshape[:2]
+    S = cf.shape[-1]
+    idx = window_index(maps, gshape, S).reshape(-1)
+    taps = np.conjugate(cf[pfreq, :, pwc, pv_off, pu_off])          # [n, npol, S, S]
+    val = (taps * (vis * wt)[:, :, None, None]).reshape(-1)
+    cells, inv = np.unique(idx, return_inverse=True)
+    out = np.bincount(inv, weights=val.real, minlength=cells.size) + \
+        1j * np.bincount(inv, weights=val.imag, minlength=cells.size)
+    sumwt = np.zeros((nchan, npol))
+    np.add.at(sumwt, pfreq, wt)
+    return cells, out, sumwt
+
+
+def degrid_windows(windows, maps, cf):
+    """``degrid_vec`` from each row's window of grid values, windows[nvis, npol,
+    S, S] gathered at ``window_index``: vis[r, p] = sum(window * cf taps)
+    (``gridding.py:256-265``)."""
+    pu, pu_off, pv, pv_off, pwg, pwc, pfreq = maps
+    taps = cf[pfreq, :, pwc, pv_off, pu_off]
+    return np.einsum('rpij,rpij->rp', windows, taps)
+
+
 def grid_weight(wt, maps, gshape):
     """``grid_weight_to_griddata`` (``gridding.py:161-183``): nearest-cell weight sum."""
     pu, pu_off, pv, pv_off, pwg, pwc, pfreq = maps

@@ -102,3 +102,51 @@ def test_phasecentre_lmn(arl):
     l, m, n1 = b.lmn(a)
     assert l > 0 and m > 0 and n1 < 0
     assert abs(l * l + m * m + (n1 + 1) ** 2 - 1.0) < 1e-14
+
+
+def test_sparse_oracle_matches_dense(oracle):
+    """grid_sparse / degrid_windows (used where the grid is too large to hold
+    densely on the host) agree with grid_vec / degrid_vec."""
+    rng = numpy.random.default_rng(11)
+    img = oracle.image_geometry(64, 4e-3, nchan=1, npol=2)
+    gax = oracle.grid_axes(img, nw=3, wstep=10.0)
+    cax = oracle.cf_axes(img, 8, 8)
+    _, cf = oracle.create_pswf_cf(1, 2, 64, 64, 8, 8)
+    lim = (32 - 4 - 2) / (64 * 4e-3)
+    n = 500
+    uvw = numpy.stack([rng.uniform(-lim, lim, n), rng.uniform(-lim, lim, n), rng.uniform(-14, 14, n)], axis=1)
+    maps = oracle.convolution_mapping(uvw, numpy.full(n, 1e8), gax, cax)
+    vis = rng.normal(size=(n, 2)) + 1j * rng.normal(size=(n, 2))
+    wt = rng.uniform(0.5, 1.5, (n, 2))
+    g, sw = oracle.grid_vec(vis, wt, maps, cf, gax['shape'])
+    cells, vals, sw2 = oracle.grid_sparse(vis, wt, maps, cf, gax['shape'])
+    dense = numpy.zeros(g.size, complex)
+    dense[cells] = vals
+    assert numpy.max(numpy.abs(dense - g.reshape(-1))) < 1e-12 * numpy.abs(g).max()
+    assert numpy.allclose(sw, sw2, rtol=1e-15)
+    win = g.reshape(-1)[oracle.window_index(maps, gax['shape'], 8)]
+    d1 = oracle.degrid_windows(win, maps, cf)
+    d2 = oracle.degrid_vec(g, maps, cf)
+    assert numpy.max(numpy.abs(d1 - d2)) < 1e-12 * numpy.abs(d2).max()
+
+
+def test_workload_shapes(arl):
+    """C1-C5 rows: uv-cut keeps every window inside the grid; C3 drops flagged
+    rows per channel; multi-frequency synthesis puts every channel on the one
+    image channel."""
+    sim = arl.simulation
+    c3 = sim.make_workload('C3', max_rows=200000)
+    for name in ('C1', 'C3', 'C4', 'C5'):
+        w = c3 if name == 'C3' else sim.make_workload(name, max_rows=20000)
+        lim = (w['npixel'] // 2 - w['support'] // 2 - 2) / (w['npixel'] * w['cellsize'])
+        assert numpy.abs(w['uvw'][:, :2]).max() < lim
+        if w.get('mfs'):
+            p = numpy.round((w['frequency'] - w['image_frequency'][0]) / w['image_bandwidth'])
+            assert numpy.all(p == 0)
+    frac = 1.0 - c3['nrows_generated'] / (512 * 511 // 2 * 12 * 64)
+    assert frac == 0.0
+    counts = numpy.bincount(numpy.searchsorted(numpy.asarray(c3['freqs']), c3['frequency']), minlength=64)
+    assert counts.min() < 0.7 * counts.max()  # uneven per-channel counts after flagging
+    c4 = sim.make_workload('C4', max_rows=1000)
+    assert c4['vis'] is None and c4['model_image'].shape == (1, 1, 2048, 2048)
+    assert abs(numpy.abs(c4['gains']).mean() - 1.0) < 0.05
