@@ -30,7 +30,7 @@ class GridDesc(ctypes.Structure):
 class CfDesc(ctypes.Structure):
     _fields_ = [('nchan', _i32), ('npol', _i32), ('nz', _i32), ('oversampling', _i32), ('support', _i32),
                 ('chan_stride', _i64), ('pol_stride', _i64), ('du', Axis), ('dv', Axis), ('z', Axis),
-                ('plane_support', _vp)]
+                ('plane_support', _vp), ('tap_absmax', _f64)]
 
 
 _P = ctypes.POINTER

@@ -45,6 +45,7 @@ struct Geom {
   arlgpu_axis gu, gv, gw, gf, cdu, cdv, cz;
   double rcp_gu, rcp_gv, rcp_gw, rcp_gf, rcp_cdu, rcp_cdv, rcp_cz;
   const int32_t *plane_support;        // device, may be null
+  float tap_absmax;                    // bound of |Re|, |Im| over the cf taps (0: unknown)
   int32_t fast_uv;                     // 1: u/v mapping may use the one-FMA fast path
   // binning
   int32_t T;       // tile edge (grid pixels)

@@ -46,7 +46,8 @@ const char *last_error() { return g_last_error.c_str(); }
 static std::atomic<unsigned long long> g_launches{0};
 
 // Kernel-variant choices (set by the autotuner through arlgpu_set_tuning).
-static std::atomic<int> g_tune_grid_kernel{2};    // 0: atomics + TwoSum, 1: band owner, 2: lean, 3: uncompensated
+static std::atomic<int> g_tune_grid_kernel{2};    // 0: atomics + TwoSum, 1: band owner, 2: lean, 3: uncompensated,
+                                                  // 4: fixed point + residual, 5: fixed point
 static std::atomic<int> g_tune_degrid_kernel{2};  // 0: warp per row, 1: batched rows, 2: lean
 static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automatic)
 static std::atomic<int> g_tune_chunk{512};        // sorted rows per gridder / degridder CTA
@@ -1083,6 +1084,180 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   }
 }
 
+// K3 (fixed-point variant, FP32C only; grid_kernel 4 and 5).
+//
+// Each staged segment (the rows of one bin inside one chunk) is accumulated in
+// 32-bit integers.  A pre-pass over the segment's rows finds the largest
+// |Re| / |Im| of vis * weight, vmax; with tap_absmax bounding every tap
+// component, each contribution conj(tap) * vis * weight has components of at
+// most B = 2 * tap_absmax * vmax.  Contributions are scaled by L / B, with
+// L = min(2^21, 2^30 / rows), rounded to integers by one FMA with the
+// 1.5 * 2^23 shift (exact round-to-nearest for magnitudes below 2^22), and
+// added with integer shared-memory atomics whose result is unused: the tile
+// sums are exact and independent of the order of the atomics, and no warp
+// waits on an atomic's returned value.  A cell sums at most `rows`
+// contributions, so it stays below 2^30.
+//
+// RESID (grid_kernel 4, the FP32C gridder when tap_absmax is given): the
+// rounding residual of each scaled contribution, x * L / B - round(x * L / B),
+// is exact in one FMA and is added to a float plane.  A flushed cell is then
+// (integer sum + residual sum) * B / L, i.e. the exact sum of the FP32
+// contributions up to the rounding of the residual sum (|residual| <= 1/2).
+// Without RESID (grid_kernel 5, measurement only) each contribution carries a
+// quantisation error of at most B / L / 2.
+template <bool RESID>
+__device__ __forceinline__ void fx_add(int *q, float *r, float x, float scale) {
+  const float t = fmaf(x, scale, 12582912.0f);
+  atomicAdd(q, __float_as_int(t) - 0x4B400000);
+  if (RESID) atomicAdd(r, fmaf(x, scale, 12582912.0f - t));
+}
+
+template <int NPOL, int NW, bool RESID>
+__global__ void __launch_bounds__(NW * 32)
+k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
+          const uint32_t *__restrict__ off, uint32_t chunk, const float2 *__restrict__ vis,
+          const float *__restrict__ wt, const float2 *__restrict__ cf, float2 *__restrict__ grid,
+          double *__restrict__ sumwt) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ float s_vmax[NW];
+  const int SG = g.SG, SG2 = SG * SG;
+  // Planar subgrid: integer plane (p, c) at subq + (2 p + c) SG2 (c = 0 real,
+  // 1 imaginary); RESID float planes after all integer planes.
+  int *subq = reinterpret_cast<int *>(smraw);
+  float *subr = reinterpret_cast<float *>(subq + (size_t)2 * NPOL * SG2);
+  constexpr int kPlanes = RESID ? 4 * NPOL : 2 * NPOL;
+  const uint32_t nvalid = off[g.nbins];
+  const uint32_t c0 = blockIdx.x * chunk;
+  if (c0 >= nvalid) return;
+  const uint32_t c1 = min(c0 + chunk, nvalid);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int S = g.S, O = g.O;
+  const int ps = (int)g.cf_pol_stride;
+  const int64_t plane_elems = (int64_t)g.ny * g.nx;
+
+  uint32_t pos = c0;
+  while (pos < c1) {
+    const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    float scale = 0.f;
+    double inv = 0.0;
+    if (!sg.direct) {
+      for (int k = threadIdx.x; k < kPlanes * SG2; k += blockDim.x) subq[k] = 0;
+      float vm = 0.f;
+      for (uint32_t r = pos + threadIdx.x; r < sg.end; r += blockDim.x) {
+        const uint32_t idx = sidx[r];
+#pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          const float2 v = vis[(size_t)idx * NPOL + p];
+          const float w = wt[(size_t)idx * NPOL + p];
+          vm = fmaxf(vm, fmaxf(fabsf(v.x * w), fabsf(v.y * w)));
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+      if (lane == 0) s_vmax[warp] = vm;
+      __syncthreads();
+      vm = s_vmax[0];
+#pragma unroll
+      for (int k = 1; k < NW; ++k) vm = fmaxf(vm, s_vmax[k]);
+      const uint32_t rows = sg.end - pos;
+      const double lim = rows <= 512u ? 2097152.0 : 1073741824.0 / (double)rows;
+      const double bound = 2.0 * (double)g.tap_absmax * (double)vm;
+      if (bound > 0.0) {
+        scale = (float)(lim / bound);
+        inv = 1.0 / (double)scale;
+      }
+    }
+    double wsum[NPOL];
+#pragma unroll
+    for (int p = 0; p < NPOL; ++p) wsum[p] = 0.0;
+    uint32_t r = pos + warp;
+    RowMap mnext;
+    uint32_t inext = 0;
+    if (r < sg.end) {
+      mnext = smap[r];
+      inext = sidx[r];
+    }
+    for (; r < sg.end; r += NW) {
+      const RowMap m = mnext;
+      const uint32_t idx = inext;
+      if (r + NW < sg.end) {
+        mnext = smap[r + NW];
+        inext = sidx[r + NW];
+      }
+      const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+      const int sz = plane_sz(g, zc);
+      const int toff = (S - sz) >> 1;
+      const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
+      float2 vw[NPOL];
+#pragma unroll
+      for (int p = 0; p < NPOL; ++p) {
+        const float2 v = vis[(size_t)idx * NPOL + p];
+        const float w = wt[(size_t)idx * NPOL + p];
+        vw[p].x = v.x * w;
+        vw[p].y = v.y * w;
+        if (lane == 0) wsum[p] += (double)w;
+      }
+      const float2 *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                         ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+      if (sg.direct) {
+        RowWalk wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
+        float2 *gb = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
+                     (int64_t)wv * g.nx + wu;
+        for (int t = lane; t < wk.n; t += 32) {
+#pragma unroll
+          for (int p = 0; p < NPOL; ++p) {
+            const float2 tp = kb[p * ps + wk.ko];
+            float2 c;
+            c.x = tp.x * vw[p].x + tp.y * vw[p].y;
+            c.y = tp.x * vw[p].y - tp.y * vw[p].x;
+            red_global<float2>(gb + (int64_t)p * g.nw * plane_elems + wk.so, c);
+          }
+          row_step(wk);
+        }
+        continue;
+      }
+      RowWalk wk = row_walk(sz, S, SG, wv - sg.v0, wu - sg.u0, lane);
+      for (int t = lane; t < wk.n; t += 32) {
+#pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          const float2 tp = kb[p * ps + wk.ko];
+          const float cx = tp.x * vw[p].x + tp.y * vw[p].y;  // conj(tap) * vw
+          const float cy = tp.x * vw[p].y - tp.y * vw[p].x;
+          fx_add<RESID>(subq + 2 * p * SG2 + wk.so, subr + 2 * p * SG2 + wk.so, cx, scale);
+          fx_add<RESID>(subq + (2 * p + 1) * SG2 + wk.so, subr + (2 * p + 1) * SG2 + wk.so, cy, scale);
+        }
+        row_step(wk);
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NPOL; ++p) {
+      double s = wsum[p];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0 && s != 0.0) atomicAdd(&sumwt[sg.ch * NPOL + p], s);
+    }
+    if (!sg.direct) {
+      __syncthreads();
+      for (int k = threadIdx.x; k < NPOL * SG2; k += blockDim.x) {
+        const int p = k / SG2, cell = k - p * SG2;
+        const int qx = subq[2 * p * SG2 + cell], qy = subq[(2 * p + 1) * SG2 + cell];
+        const float rx = RESID ? subr[2 * p * SG2 + cell] : 0.f;
+        const float ry = RESID ? subr[(2 * p + 1) * SG2 + cell] : 0.f;
+        if (qx == 0 && qy == 0 && rx == 0.f && ry == 0.f) continue;
+        const int y = cell / SG, x = cell - y * SG;
+        const int gy = sg.v0 + y, gx = sg.u0 + x;
+        if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
+        float2 val;
+        val.x = (float)(((double)qx + (double)rx) * inv);
+        val.y = (float)(((double)qy + (double)ry) * inv);
+        red_global<float2>(grid + ((int64_t)(sg.ch * NPOL + p) * g.nw + sg.zg) * plane_elems +
+                               (int64_t)gy * g.nx + gx,
+                           val);
+      }
+      __syncthreads();
+    }
+    pos = sg.end;
+  }
+}
+
 // K4 (lean variant): warp per row, specialised on the polarisation count,
 // 32-bit incremental offsets, two taps per iteration with independent sums.
 template <typename R, int NPOL, int NW>
@@ -1264,6 +1439,7 @@ int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precisio
   g->rcp_cdv = rcp(cd->dv.cdelt);
   g->rcp_cz = rcp(cd->z.cdelt);
   g->plane_support = cd->plane_support;
+  g->tap_absmax = cd->tap_absmax > 0.0 && cd->tap_absmax < 1e30 ? (float)cd->tap_absmax : 0.f;
   {
     // The fast u/v mapping needs zero crvals, integer crpixes and the cf's
     // sub-pixel cdelt equal to the grid cdelt / O (ARL builds both from one
@@ -1363,6 +1539,30 @@ int plan_build(const double *uvw, const double *freq, int64_t nvis, const Geom &
 static constexpr int kWarps = 8;
 static inline uint32_t chunk_rows() { return (uint32_t)g_tune_chunk.load(); }
 
+static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const void *vis, const void *wt,
+                          const void *cf, void *grid, double *sumwt, bool resid, cudaStream_t st) {
+  const size_t smem = (size_t)(resid ? 4 : 2) * g.npol * g.SG * g.SG * 4;
+  if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
+  void (*kern)(Geom, const RowMap *, const uint32_t *, const uint32_t *, uint32_t, const float2 *, const float *,
+               const float2 *, float2 *, double *);
+  if (resid)
+    kern = g.npol == 1 ? k_grid_fx<1, kWarps, true> : g.npol == 2 ? k_grid_fx<2, kWarps, true>
+                                                                   : k_grid_fx<4, kWarps, true>;
+  else
+    kern = g.npol == 1 ? k_grid_fx<1, kWarps, false> : g.npol == 2 ? k_grid_fx<2, kWarps, false>
+                                                                    : k_grid_fx<4, kWarps, false>;
+  ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const uint32_t chunk = chunk_rows();
+  unsigned blocks = (unsigned)((nvis + chunk - 1) / chunk);
+  if (blocks == 0) return ARLGPU_OK;
+  kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk, static_cast<const float2 *>(vis),
+                                          static_cast<const float *>(wt), static_cast<const float2 *>(cf),
+                                          static_cast<float2 *>(grid), sumwt);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
+}
+
 template <typename R>
 static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const void *vis, const void *wt,
                        const void *cf, void *grid, double *sumwt, cudaStream_t st) {
@@ -1380,6 +1580,13 @@ static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const voi
                        : g.npol == 2 ? k_grid_lean<R, 2, kWarps, PlainAcc<R>> : k_grid_lean<R, 4, kWarps, PlainAcc<R>>;
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean gridder handles 1, 2 or 4 polarisations");
     smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T);
+  } else if (g_tune_grid_kernel.load() >= 4) {
+    if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean gridder handles 1, 2 or 4 polarisations");
+    if (sizeof(R) == 4 && g.tap_absmax > 0.f)
+      return launch_grid_fx(g, b, nvis, vis, wt, cf, grid, sumwt, g_tune_grid_kernel.load() == 4, st);
+    // FP64, or no tap bound: the compensated float variant
+    kern = g.npol == 1 ? k_grid_lean<R, 1, kWarps> : g.npol == 2 ? k_grid_lean<R, 2, kWarps>
+                                                                  : k_grid_lean<R, 4, kWarps>;
   }
   // The lean variants' planar subgrid has the same size as the interleaved one.
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
@@ -1547,7 +1754,7 @@ extern "C" int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const a
 extern "C" int arlgpu_set_tuning(const char *key, int value) {
   if (!key) return fail(ARLGPU_ERR_INVALID, "null key");
   const std::string k(key);
-  if (k == "grid_kernel" && value >= 0 && value <= 3) g_tune_grid_kernel = value;
+  if (k == "grid_kernel" && value >= 0 && value <= 5) g_tune_grid_kernel = value;
   else if (k == "degrid_kernel" && value >= 0 && value <= 2) g_tune_degrid_kernel = value;
   else if (k == "subgrid" && (value == 0 || (value >= 16 && value <= 128))) g_tune_subgrid = value;
   else if (k == "chunk" && value >= 32 && value <= (1 << 20)) g_tune_chunk = value;

@@ -62,15 +62,32 @@ def grid_desc(grid_wcs, shape):
     return d
 
 
-def cf_desc(cf_wcs, shape, chan_stride, pol_stride, plane_support=None):
+def cf_desc(cf_wcs, shape, chan_stride, pol_stride, plane_support=None, table=None):
     """CfDesc from a ConvolutionFunction WCS (UU, VV, DUU, DVV, WW, ...) and shape
-    [nchan, npol, nz, O, O, S, S]; strides in elements."""
+    [nchan, npol, nz, O, O, S, S]; strides in elements.  With the device
+    ``table`` (from device_cf) the descriptor carries the table's largest tap
+    component, which lets the FP32C gridder sum tiles in fixed point."""
     d = nat.CfDesc()
     d.nchan, d.npol, d.nz, d.oversampling, _, d.support, _ = (int(s) for s in shape)
     d.chan_stride, d.pol_stride = int(chan_stride), int(pol_stride)
     d.du, d.dv, d.z = _axis(cf_wcs, 2), _axis(cf_wcs, 3), _axis(cf_wcs, 4)
     d.plane_support = None if plane_support is None else plane_support.data_ptr()
+    d.tap_absmax = 0.0 if table is None else tap_absmax(table)
     return d
+
+
+_ABSMAX = {}
+
+
+def tap_absmax(table):
+    """max(|Re|, |Im|) over a device cf table, remembered per (tensor, version)."""
+    key = (table.data_ptr(), table.numel(), table._version)
+    hit = _ABSMAX.get(id(table))
+    if hit is not None and hit[0] == key:
+        return hit[1]
+    v = float(torch.view_as_real(table).abs().max().item()) if table.numel() else 0.0
+    _ABSMAX[id(table)] = (key, v)
+    return v
 
 
 # ---------------------------------------------------------------------------

@@ -103,7 +103,7 @@ def invert_2d(vis, im, dopsf=False, normalize=True, gcfcf=None, precision=None, 
     nchan, npol, ny, nx = im.shape
     gd = dv.grid_desc(_grid_wcs(im, 1, 1e15), (nchan, npol, 1, ny, nx))
     cf_t, cs, ps, psup = dv.device_cf(cf, precision, device)
-    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup)
+    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
     grid_t, sumwt, n_bad = dv.grid(uvw, f, v, w, cf_t, cd, gd, precision)
     _assert_in_grid(n_bad)
     imaginary = get_parameter(kwargs, 'imaginary', False)
@@ -136,7 +136,7 @@ def predict_2d(vis, model, gcfcf=None, precision=None, **kwargs):
         dv.to_device(numpy.asarray(d, numpy.float64), torch.float64, device)
     grid_t = dv.fft_image_to_grid(m_t, _gcf_t(gcf, device), gd, precision)
     cf_t, cs, ps, psup = dv.device_cf(cf, precision, device)
-    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup)
+    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
     uvw, f, _, _ = _rows(vis, precision, device, need_vis=False)
     out, n_bad = dv.degrid(uvw, f, grid_t, cf_t, cd, gd, precision)
     _assert_in_grid(n_bad)
@@ -216,7 +216,7 @@ def _single_slice(vis, im, gcfcf, precision, device):
     nchan, npol, ny, nx = im.shape
     gd = dv.grid_desc(_grid_wcs(im, 1, 1e15), (nchan, npol, 1, ny, nx))
     cf_t, cs, ps, psup = dv.device_cf(cf, precision, device)
-    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup)
+    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
     ws = dv.WORKSPACE.get(dv.plan_bytes(uvw.shape[0], gd, cd), device)
     n_bad = torch.zeros(1, dtype=torch.int64, device=device)
     nat.call('arlgpu_plan_build', nat.ptr(uvw), nat.ptr(f), uvw.shape[0], ctypes.byref(gd), ctypes.byref(cd),

@@ -14,7 +14,7 @@ import torch
 from . import _native as nat
 from . import device as dv
 
-GRID_KERNELS = (0, 1, 2)     # shared atomics + TwoSum, band owner + Kahan, lean atomics
+GRID_KERNELS = (0, 1, 2, 4)  # shared atomics + TwoSum, band owner + Kahan, lean atomics, fixed point
 DEGRID_KERNELS = (0, 1, 2)   # warp per row, 32-row batches, lean warp per row
 SUBGRIDS = (32, 48, 64)
 CHUNKS = (512, 2048)

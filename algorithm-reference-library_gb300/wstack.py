@@ -77,7 +77,7 @@ class WStackImager:
         self.gwcs.wcs.crval[2], self.gwcs.wcs.crpix[2], self.gwcs.wcs.cdelt[2] = self.w_axis
         self.gd = dv.grid_desc(self.gwcs, (nchan, npol, vis_slices, ny, nx))
         self.cf_t, cs, ps, self._psup = dv.device_cf(cf, self.precision, self.device)
-        self.cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, self._psup)
+        self.cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, self._psup, table=self.cf_t)
         self.ws = torch.empty(dv.plan_bytes(self.n, self.gd, self.cd), dtype=torch.uint8, device=self.device)
         self.n_bad = torch.zeros(1, dtype=torch.int64, device=self.device)
         self.wmean = torch.empty(vis_slices, dtype=torch.float64, device=self.device)

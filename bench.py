@@ -186,7 +186,7 @@ def build_context(arl, torch, w, precision, device):
         gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=w['oversampling'], support=w['support'])
     gd = dv.grid_desc(arl.kernels._grid_wcs(im, 1, 1e15), (im.nchan, im.npol, 1, w['npixel'], w['npixel']))
     cf_t, cs, ps, psup = dv.device_cf(cf, precision, device)
-    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup)
+    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
     n = w['uvw'].shape[0]
     npol = w['npol']
     ctx = dict(precision=precision, n=n, gd=gd, cd=cd, cf_t=cf_t, psup=psup, im=im, cf=cf, gcf=gcf)

@@ -63,12 +63,17 @@ typedef struct {
  * [nchan][npol][nz][O][O][S][S]; chan_stride / pol_stride are element strides
  * between channel / polarisation blocks (0 = the same kernel for all).
  * plane_support, if not NULL, is a device array of nz even supports <= S: plane
- * z then uses only the central plane_support[z] x plane_support[z] taps. */
+ * z then uses only the central plane_support[z] x plane_support[z] taps.
+ * tap_absmax is an upper bound of |Re| and |Im| over every tap of the table, or
+ * 0 when the caller does not know one.  With a bound the FP32C gridder can sum
+ * each tile exactly in fixed point (grid_kernel 4); without one it uses the
+ * compensated float variant.  A bound that is too small gives wrong grids. */
 typedef struct {
   int32_t nchan, npol, nz, oversampling, support;
   int64_t chan_stride, pol_stride;
   arlgpu_axis du, dv, z;        /* cf grid_wcs axes DUU, DVV and WW */
   const int32_t *plane_support;
+  double tap_absmax;
 } arlgpu_cf_desc;
 
 /* Library version string and the message of the last failure on this thread. */
@@ -85,9 +90,13 @@ unsigned long long arlgpu_kernel_launches(void);
  *                       read-modify-write with a per-cell Kahan term,
  *                   2 = as 0, specialised on npol with 32-bit incremental offsets (default),
  *                   3 = as 2 without the compensation (measurement only: FP32C
- *                       promises compensated sums, so the autotuner never picks it)
+ *                       promises compensated sums, so the autotuner never picks it),
+ *                   4 = FP32C tiles summed exactly in 32-bit fixed point, plus a float
+ *                       plane of the rounding residuals (needs cf tap_absmax; FP64 and
+ *                       an unknown bound use 2),
+ *                   5 = as 4 without the residual plane (measurement only)
  *   "degrid_kernel" 0 = one warp per row, 1 = 32-row batches per warp,
- *                   2 = one warp per row, specialised on npol, two taps per step (default)
+ *                   2 = one warp per row, specialised on npol, four taps per step (default)
  *   "subgrid"       subgrid edge in cells (16..128), 0 = automatic (48, or 32 when 4 pols)
  *   "chunk"         sorted rows per gridder / degridder CTA (32..2^20, default 512)
  * No reference counterpart (ARL has one Python loop per function). */

@@ -59,9 +59,10 @@ def test_struct_layout_matches_c(arl):
 #include <stddef.h>
 #include "arlgpu.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(arlgpu_axis), sizeof(arlgpu_grid_desc),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(arlgpu_axis), sizeof(arlgpu_grid_desc),
          offsetof(arlgpu_grid_desc, u), offsetof(arlgpu_grid_desc, f), sizeof(arlgpu_cf_desc),
-         offsetof(arlgpu_cf_desc, chan_stride), offsetof(arlgpu_cf_desc, plane_support));
+         offsetof(arlgpu_cf_desc, chan_stride), offsetof(arlgpu_cf_desc, plane_support),
+         offsetof(arlgpu_cf_desc, tap_absmax));
   return 0;
 }
 '''
@@ -73,7 +74,8 @@ int main(void) {
         got = [int(x) for x in subprocess.check_output([exe]).split()]
     n = arl._native
     want = [ctypes.sizeof(n.Axis), ctypes.sizeof(n.GridDesc), n.GridDesc.u.offset, n.GridDesc.f.offset,
-            ctypes.sizeof(n.CfDesc), n.CfDesc.chan_stride.offset, n.CfDesc.plane_support.offset]
+            ctypes.sizeof(n.CfDesc), n.CfDesc.chan_stride.offset, n.CfDesc.plane_support.offset,
+            n.CfDesc.tap_absmax.offset]
     assert got == want
 
 

@@ -352,11 +352,13 @@ def test_c2_full_size_properties(arl):
 
 
 @pytest.mark.parametrize('grid_kernel,degrid_kernel,subgrid,chunk', [
-    (0, 0, 48, 512), (1, 1, 0, 512), (2, 2, 32, 2048), (2, 2, 0, 512), (3, 0, 0, 512)])
+    (0, 0, 48, 512), (1, 1, 0, 512), (2, 2, 32, 2048), (2, 2, 0, 512), (3, 0, 0, 512), (4, 2, 0, 512),
+    (4, 2, 32, 2048), (5, 2, 0, 512)])
 @pytest.mark.parametrize('npol', [1, 2, 4])
 def test_kernel_variants_vs_oracle(arl, oracle, grid_kernel, degrid_kernel, subgrid, chunk, npol):
-    """Every gridder / degridder variant, against the oracle (grid_kernel 3 is
-    the uncompensated measurement variant: FP32 sums, same 1e-5 bound here)."""
+    """Every gridder / degridder variant, against the oracle (grid_kernels 3 and
+    5 are the uncompensated measurement variants, held to the same 1e-5 bound
+    here; 4 and 5 are the fixed-point gridders, FP32C only: FP64 runs 2)."""
     before = arl.tune.get_tuning()
     try:
         arl.tune.set_tuning(grid_kernel=grid_kernel, degrid_kernel=degrid_kernel, subgrid=subgrid, chunk=chunk)

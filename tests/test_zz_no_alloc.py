@@ -36,7 +36,7 @@ def case(arl):
              wt=torch.as_tensor(rng.uniform(0.5, 2, (n, 1)), device=dev).to(torch.float32))
     gd = arl.device.grid_desc(arl.kernels._grid_wcs(im, 1, 1e15), (2, 1, 1, N, N))
     cf_t, cs, ps, psup = arl.device.device_cf(cf, 'fp32c', dev)
-    cd = arl.device.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup)
+    cd = arl.device.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
     return arl, t, gd, cd, cf_t, n
 
 
