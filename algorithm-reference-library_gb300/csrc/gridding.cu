@@ -1099,17 +1099,26 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
 // contributions, so it stays below 2^30.
 //
 // RESID (grid_kernel 4, the FP32C gridder when tap_absmax is given): the
-// rounding residual of each scaled contribution, x * L / B - round(x * L / B),
-// is exact in one FMA and is added to a float plane.  A flushed cell is then
-// (integer sum + residual sum) * B / L, i.e. the exact sum of the FP32
-// contributions up to the rounding of the residual sum (|residual| <= 1/2).
-// Without RESID (grid_kernel 5, measurement only) each contribution carries a
-// quantisation error of at most B / L / 2.
+// rounding residual of each scaled contribution, x * L / B - round(x * L / B)
+// (one FMA, |residual| <= 1/2), is rounded to units of 1 / R, R = min(2^20,
+// 2^30 / rows), and summed in a second integer plane.  A flushed cell is
+// (sum + residual sum / R) * B / L: the sum of the FP32 contributions to
+// within B / (2 L R) per contribution, about 2^-42 of the segment's largest
+// one for segments of up to 512 rows.  Without RESID (grid_kernel 5,
+// measurement only) each contribution carries a quantisation error of at most
+// B / L / 2.
 template <bool RESID>
-__device__ __forceinline__ void fx_add(int *q, float *r, float x, float scale) {
+__device__ __forceinline__ void fx_add(int *q, int *r, float x, float scale, float rscale) {
   const float t = fmaf(x, scale, 12582912.0f);
   atomicAdd(q, __float_as_int(t) - 0x4B400000);
-  if (RESID) atomicAdd(r, fmaf(x, scale, 12582912.0f - t));
+  if (RESID) {
+    // residual x * scale - round(x * scale), |.| <= 1/2, as a second limb in
+    // units of 1 / rscale: |limb| <= rscale / 2 <= 2^19, and a cell's sum of
+    // limbs stays below 2^29 (rscale <= 2^30 / rows)
+    const float rs = fmaf(x, scale, 12582912.0f - t);
+    const float t2 = fmaf(rs, rscale, 12582912.0f);
+    atomicAdd(r, __float_as_int(t2) - 0x4B400000);
+  }
 }
 
 template <int NPOL, int NW, bool RESID>
@@ -1122,9 +1131,9 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   __shared__ float s_vmax[NW];
   const int SG = g.SG, SG2 = SG * SG;
   // Planar subgrid: integer plane (p, c) at subq + (2 p + c) SG2 (c = 0 real,
-  // 1 imaginary); RESID float planes after all integer planes.
+  // 1 imaginary); with RESID the residual-limb planes follow all of them.
   int *subq = reinterpret_cast<int *>(smraw);
-  float *subr = reinterpret_cast<float *>(subq + (size_t)2 * NPOL * SG2);
+  int *subr = subq + (size_t)2 * NPOL * SG2;
   constexpr int kPlanes = RESID ? 4 * NPOL : 2 * NPOL;
   const uint32_t nvalid = off[g.nbins];
   const uint32_t c0 = blockIdx.x * chunk;
@@ -1138,8 +1147,8 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   uint32_t pos = c0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
-    float scale = 0.f;
-    double inv = 0.0;
+    float scale = 0.f, rscale = 0.f;
+    double inv = 0.0, rinv = 0.0;
     if (!sg.direct) {
       for (int k = threadIdx.x; k < kPlanes * SG2; k += blockDim.x) subq[k] = 0;
       float vm = 0.f;
@@ -1162,9 +1171,11 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       const double lim = rows <= 512u ? 2097152.0 : 1073741824.0 / (double)rows;
       const double bound = 2.0 * (double)g.tap_absmax * (double)vm;
       if (bound > 0.0) {
-        scale = (float)(lim / bound);
+        scale = (float)fmin(lim / bound, 1e30);  // tiny segments: coarser units, never inf
         inv = 1.0 / (double)scale;
       }
+      rscale = rows <= 1024u ? 1048576.0f : (float)(1073741824.0 / (double)rows);
+      rinv = 1.0 / (double)rscale;
     }
     double wsum[NPOL];
 #pragma unroll
@@ -1216,16 +1227,31 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         continue;
       }
       RowWalk wk = row_walk(sz, S, SG, wv - sg.v0, wu - sg.u0, lane);
-      for (int t = lane; t < wk.n; t += 32) {
+      // Four taps per lane per iteration: the tap loads of all four are in
+      // flight before the first atomic.
+      for (int t = lane; t < wk.n; t += 128) {
+        int so[4];
+        float2 tp[NPOL][4];
+        bool on[4];
 #pragma unroll
-        for (int p = 0; p < NPOL; ++p) {
-          const float2 tp = kb[p * ps + wk.ko];
-          const float cx = tp.x * vw[p].x + tp.y * vw[p].y;  // conj(tap) * vw
-          const float cy = tp.x * vw[p].y - tp.y * vw[p].x;
-          fx_add<RESID>(subq + 2 * p * SG2 + wk.so, subr + 2 * p * SG2 + wk.so, cx, scale);
-          fx_add<RESID>(subq + (2 * p + 1) * SG2 + wk.so, subr + (2 * p + 1) * SG2 + wk.so, cy, scale);
+        for (int u = 0; u < 4; ++u) {
+          on[u] = t + 32 * u < wk.n;
+          so[u] = wk.so;
+#pragma unroll
+          for (int p = 0; p < NPOL; ++p) tp[p][u] = on[u] ? kb[p * ps + wk.ko] : make_float2(0.f, 0.f);
+          row_step(wk);
         }
-        row_step(wk);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (!on[u]) break;
+#pragma unroll
+          for (int p = 0; p < NPOL; ++p) {
+            const float cx = tp[p][u].x * vw[p].x + tp[p][u].y * vw[p].y;  // conj(tap) * vw
+            const float cy = tp[p][u].x * vw[p].y - tp[p][u].y * vw[p].x;
+            fx_add<RESID>(subq + 2 * p * SG2 + so[u], subr + 2 * p * SG2 + so[u], cx, scale, rscale);
+            fx_add<RESID>(subq + (2 * p + 1) * SG2 + so[u], subr + (2 * p + 1) * SG2 + so[u], cy, scale, rscale);
+          }
+        }
       }
     }
 #pragma unroll
@@ -1239,15 +1265,15 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       for (int k = threadIdx.x; k < NPOL * SG2; k += blockDim.x) {
         const int p = k / SG2, cell = k - p * SG2;
         const int qx = subq[2 * p * SG2 + cell], qy = subq[(2 * p + 1) * SG2 + cell];
-        const float rx = RESID ? subr[2 * p * SG2 + cell] : 0.f;
-        const float ry = RESID ? subr[(2 * p + 1) * SG2 + cell] : 0.f;
-        if (qx == 0 && qy == 0 && rx == 0.f && ry == 0.f) continue;
+        const int rx = RESID ? subr[2 * p * SG2 + cell] : 0;
+        const int ry = RESID ? subr[(2 * p + 1) * SG2 + cell] : 0;
+        if (qx == 0 && qy == 0 && rx == 0 && ry == 0) continue;
         const int y = cell / SG, x = cell - y * SG;
         const int gy = sg.v0 + y, gx = sg.u0 + x;
         if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
         float2 val;
-        val.x = (float)(((double)qx + (double)rx) * inv);
-        val.y = (float)(((double)qy + (double)ry) * inv);
+        val.x = (float)(((double)qx + (double)rx * rinv) * inv);
+        val.y = (float)(((double)qy + (double)ry * rinv) * inv);
         red_global<float2>(grid + ((int64_t)(sg.ch * NPOL + p) * g.nw + sg.zg) * plane_elems +
                                (int64_t)gy * g.nx + gx,
                            val);

@@ -73,7 +73,7 @@ def _rows(vis, precision, device, need_vis=True):
 def _descs(griddata, cf, precision, device):
     gd = dv.grid_desc(griddata.grid_wcs, griddata.data.shape)
     t, cs, ps, psup = dv.device_cf(cf, precision, device)
-    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
+    cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=t)
     return gd, cd, t
 
 
