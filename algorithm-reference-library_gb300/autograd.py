@@ -44,7 +44,7 @@ class GriddingOperator:
         self.gd = dv.grid_desc(_grid_wcs(im, 1, 1e15), (nchan, npol, 1, ny, nx))
         self.cf_t, cs, ps, psup = dv.device_cf(cf, self.precision, device)
         self._psup = psup
-        self.cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
+        self.cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=self.cf_t)
         self.gcf = _gcf_t(gcf, device)
         self.n = self.uvw.shape[0]
         self.ws = torch.empty(dv.plan_bytes(self.n, self.gd, self.cd), dtype=torch.uint8, device=device)

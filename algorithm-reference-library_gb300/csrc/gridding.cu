@@ -46,7 +46,7 @@ const char *last_error() { return g_last_error.c_str(); }
 static std::atomic<unsigned long long> g_launches{0};
 
 // Kernel-variant choices (set by the autotuner through arlgpu_set_tuning).
-static std::atomic<int> g_tune_grid_kernel{2};    // 0: atomics + TwoSum, 1: band owner, 2: lean, 3: uncompensated,
+static std::atomic<int> g_tune_grid_kernel{4};    // 0: atomics + TwoSum, 1: band owner, 2: lean, 3: uncompensated,
                                                   // 4: fixed point + residual, 5: fixed point
 static std::atomic<int> g_tune_degrid_kernel{2};  // 0: warp per row, 1: batched rows, 2: lean
 static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automatic)
@@ -400,6 +400,85 @@ __device__ __forceinline__ SegInfo seg_at(uint32_t pos, uint32_t c1, const RowMa
   // Few rows for a whole subgrid: go straight to global memory.
   s.direct = (uint64_t)(s.end - pos) * g.S * g.S * 2ull < (uint64_t)g.SG * g.SG;
   return s;
+}
+
+// Footprint of one segment in subgrid coordinates: the bounding box
+// [x0, x1) x [y0, y1) of its rows' windows, the window edge (all rows of a
+// segment share a w-plane, hence a support) and, for the gridder, the largest
+// |Re| / |Im| of vis * weight.  One block-wide pass over the segment's rows;
+// contains a __syncthreads.  s_red holds NW * 6 words; callers alternate two
+// such buffers between consecutive segments, so a segment's writes never meet
+// the previous segment's reads when no other barrier lies between them.
+struct SegBox {
+  int x0, x1, y0, y1, sz;
+  float vmax;
+};
+
+template <int NW, int NPOL, bool VMAX>
+__device__ __forceinline__ SegBox seg_box(const SegInfo &sg, uint32_t pos, const RowMap *__restrict__ smap,
+                                          const uint32_t *__restrict__ sidx, const float2 *__restrict__ vis,
+                                          const float *__restrict__ wt, const Geom &g, int *s_red) {
+  int x0 = 0x7fffffff, y0 = 0x7fffffff, x1 = -0x7fffffff, y1 = -0x7fffffff, sz = 0;
+  float vm = 0.f;
+  for (uint32_t r = pos + threadIdx.x; r < sg.end; r += blockDim.x) {
+    const RowMap m = smap[r];
+    sz = plane_sz(g, m.sub >> 16);
+    const int lx = m.pu - (sz >> 1) - sg.u0, ly = m.pv - (sz >> 1) - sg.v0;
+    x0 = min(x0, lx);
+    x1 = max(x1, lx + sz);
+    y0 = min(y0, ly);
+    y1 = max(y1, ly + sz);
+    if (VMAX) {
+      const uint32_t idx = sidx[r];
+#pragma unroll
+      for (int p = 0; p < NPOL; ++p) {
+        const float2 v = vis[(size_t)idx * NPOL + p];
+        const float w = wt[(size_t)idx * NPOL + p];
+        vm = fmaxf(vm, fmaxf(fabsf(v.x * w), fabsf(v.y * w)));
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    x0 = min(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+    y0 = min(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+    x1 = max(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+    y1 = max(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    sz = max(sz, __shfl_xor_sync(0xffffffffu, sz, o));
+    if (VMAX) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+  }
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    s_red[warp * 6 + 0] = x0;
+    s_red[warp * 6 + 1] = x1;
+    s_red[warp * 6 + 2] = y0;
+    s_red[warp * 6 + 3] = y1;
+    s_red[warp * 6 + 4] = sz;
+    s_red[warp * 6 + 5] = __float_as_int(vm);
+  }
+  __syncthreads();
+  SegBox b;
+  b.x0 = s_red[0];
+  b.x1 = s_red[1];
+  b.y0 = s_red[2];
+  b.y1 = s_red[3];
+  b.sz = s_red[4];
+  b.vmax = __int_as_float(s_red[5]);
+#pragma unroll
+  for (int k = 1; k < NW; ++k) {
+    b.x0 = min(b.x0, s_red[k * 6 + 0]);
+    b.x1 = max(b.x1, s_red[k * 6 + 1]);
+    b.y0 = min(b.y0, s_red[k * 6 + 2]);
+    b.y1 = max(b.y1, s_red[k * 6 + 3]);
+    b.sz = max(b.sz, s_red[k * 6 + 4]);
+    if (VMAX) b.vmax = fmaxf(b.vmax, __int_as_float(s_red[k * 6 + 5]));
+  }
+  return b;
+}
+
+// A segment goes straight to global memory when its rows' windows do not
+// overlap enough to repay staging: rows * sz^2 taps against the footprint.
+__device__ __forceinline__ bool seg_direct(const SegBox &b, uint32_t rows) {
+  return (uint64_t)rows * (uint64_t)(b.sz * b.sz) <= (uint64_t)(b.x1 - b.x0) * (uint64_t)(b.y1 - b.y0);
 }
 
 template <typename R, int NW>
@@ -984,13 +1063,16 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   const int ps = (int)g.cf_pol_stride;
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
 
+  // The planes are zero between segments: the flush clears what it reads.
+  for (int k = threadIdx.x; k < 2 * NPOL * SG2 * ACC::kWords; k += blockDim.x) sub[k] = (R)0;
+  __shared__ int s_red[2][NW * 6];
   uint32_t pos = c0;
+  int parity = 0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
-    if (!sg.direct) {
-      for (int k = threadIdx.x; k < 2 * NPOL * SG2 * ACC::kWords; k += blockDim.x) sub[k] = (R)0;
-      __syncthreads();
-    }
+    const SegBox box = seg_box<NW, 1, false>(sg, pos, smap, sidx, nullptr, nullptr, g, s_red[parity]);
+    parity ^= 1;
+    const bool direct = seg_direct(box, sg.end - pos);
     double wsum[NPOL];
 #pragma unroll
     for (int p = 0; p < NPOL; ++p) wsum[p] = 0.0;
@@ -1009,7 +1091,7 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
         inext = sidx[r + NW];
       }
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = plane_sz(g, zc);
+      const int sz = box.sz;
       const int toff = (S - sz) >> 1;
       const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
       CT vw[NPOL];
@@ -1023,7 +1105,7 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
       }
       const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
                      ((int64_t)(vf * O + uf) * S + toff) * S + toff;
-      if (sg.direct) {
+      if (direct) {
         RowWalk wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
         CT *gb = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
                  (int64_t)wv * g.nx + wu;
@@ -1060,25 +1142,34 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (lane == 0 && s != 0.0) atomicAdd(&sumwt[sg.ch * NPOL + p], s);
     }
-    if (!sg.direct) {
+    if (!direct) {
       __syncthreads();
-      for (int k = threadIdx.x; k < NPOL * SG2; k += blockDim.x) {
-        const int pp = k / SG2, cell = k - pp * SG2;
-        CT val;
-        val.x = sub[2 * pp * SG2 + cell];
-        val.y = sub[(2 * pp + 1) * SG2 + cell];
-        if (ACC::kWords == 2) {
-          val.x += comp[2 * pp * SG2 + cell];
-          val.y += comp[(2 * pp + 1) * SG2 + cell];
+      // Flush the footprint and clear it: warps over its rows, lanes over its columns.
+      for (int y = box.y0 + warp; y < box.y1; y += NW) {
+        const int gy = sg.v0 + y;
+        for (int x = box.x0 + lane; x < box.x1; x += 32) {
+          const int gx = sg.u0 + x, cell = y * SG + x;
+#pragma unroll
+          for (int p = 0; p < NPOL; ++p) {
+            CT val;
+            val.x = sub[2 * p * SG2 + cell];
+            val.y = sub[(2 * p + 1) * SG2 + cell];
+            sub[2 * p * SG2 + cell] = (R)0;
+            sub[(2 * p + 1) * SG2 + cell] = (R)0;
+            if (ACC::kWords == 2) {
+              val.x += comp[2 * p * SG2 + cell];
+              val.y += comp[(2 * p + 1) * SG2 + cell];
+              comp[2 * p * SG2 + cell] = (R)0;
+              comp[(2 * p + 1) * SG2 + cell] = (R)0;
+            }
+            if (val.x == (R)0 && val.y == (R)0) continue;
+            if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
+            red_global<CT>(grid + ((int64_t)(sg.ch * NPOL + p) * g.nw + sg.zg) * plane_elems +
+                               (int64_t)gy * g.nx + gx,
+                           val);
+          }
         }
-        if (val.x == (R)0 && val.y == (R)0) continue;
-        const int p = k / SG2, rem = k - p * SG2, y = rem / SG, x = rem - y * SG;
-        const int gy = sg.v0 + y, gx = sg.u0 + x;
-        if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
-        red_global<CT>(grid + ((int64_t)(sg.ch * NPOL + p) * g.nw + sg.zg) * plane_elems + (int64_t)gy * g.nx + gx,
-                       val);
       }
-      __syncthreads();
     }
     pos = sg.end;
   }
@@ -1128,10 +1219,11 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
           const float *__restrict__ wt, const float2 *__restrict__ cf, float2 *__restrict__ grid,
           double *__restrict__ sumwt) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ float s_vmax[NW];
+  __shared__ int s_red[2][NW * 6];
   const int SG = g.SG, SG2 = SG * SG;
   // Planar subgrid: integer plane (p, c) at subq + (2 p + c) SG2 (c = 0 real,
   // 1 imaginary); with RESID the residual-limb planes follow all of them.
+  // The planes are zero between segments: the flush clears what it reads.
   int *subq = reinterpret_cast<int *>(smraw);
   int *subr = subq + (size_t)2 * NPOL * SG2;
   constexpr int kPlanes = RESID ? 4 * NPOL : 2 * NPOL;
@@ -1143,33 +1235,21 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   const int S = g.S, O = g.O;
   const int ps = (int)g.cf_pol_stride;
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
+  for (int k = threadIdx.x; k < kPlanes * SG2; k += blockDim.x) subq[k] = 0;
 
   uint32_t pos = c0;
+  int parity = 0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    const SegBox box = seg_box<NW, NPOL, true>(sg, pos, smap, sidx, vis, wt, g, s_red[parity]);
+    parity ^= 1;
+    const uint32_t rows = sg.end - pos;
+    const bool direct = seg_direct(box, rows);
     float scale = 0.f, rscale = 0.f;
     double inv = 0.0, rinv = 0.0;
-    if (!sg.direct) {
-      for (int k = threadIdx.x; k < kPlanes * SG2; k += blockDim.x) subq[k] = 0;
-      float vm = 0.f;
-      for (uint32_t r = pos + threadIdx.x; r < sg.end; r += blockDim.x) {
-        const uint32_t idx = sidx[r];
-#pragma unroll
-        for (int p = 0; p < NPOL; ++p) {
-          const float2 v = vis[(size_t)idx * NPOL + p];
-          const float w = wt[(size_t)idx * NPOL + p];
-          vm = fmaxf(vm, fmaxf(fabsf(v.x * w), fabsf(v.y * w)));
-        }
-      }
-      for (int o = 16; o > 0; o >>= 1) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
-      if (lane == 0) s_vmax[warp] = vm;
-      __syncthreads();
-      vm = s_vmax[0];
-#pragma unroll
-      for (int k = 1; k < NW; ++k) vm = fmaxf(vm, s_vmax[k]);
-      const uint32_t rows = sg.end - pos;
+    if (!direct) {
       const double lim = rows <= 512u ? 2097152.0 : 1073741824.0 / (double)rows;
-      const double bound = 2.0 * (double)g.tap_absmax * (double)vm;
+      const double bound = 2.0 * (double)g.tap_absmax * (double)box.vmax;
       if (bound > 0.0) {
         scale = (float)fmin(lim / bound, 1e30);  // tiny segments: coarser units, never inf
         inv = 1.0 / (double)scale;
@@ -1195,7 +1275,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         inext = sidx[r + NW];
       }
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = plane_sz(g, zc);
+      const int sz = box.sz;
       const int toff = (S - sz) >> 1;
       const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
       float2 vw[NPOL];
@@ -1209,7 +1289,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       }
       const float2 *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
                          ((int64_t)(vf * O + uf) * S + toff) * S + toff;
-      if (sg.direct) {
+      if (direct) {
         RowWalk wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
         float2 *gb = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
                      (int64_t)wv * g.nx + wu;
@@ -1260,25 +1340,36 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (lane == 0 && s != 0.0) atomicAdd(&sumwt[sg.ch * NPOL + p], s);
     }
-    if (!sg.direct) {
+    if (!direct) {
       __syncthreads();
-      for (int k = threadIdx.x; k < NPOL * SG2; k += blockDim.x) {
-        const int p = k / SG2, cell = k - p * SG2;
-        const int qx = subq[2 * p * SG2 + cell], qy = subq[(2 * p + 1) * SG2 + cell];
-        const int rx = RESID ? subr[2 * p * SG2 + cell] : 0;
-        const int ry = RESID ? subr[(2 * p + 1) * SG2 + cell] : 0;
-        if (qx == 0 && qy == 0 && rx == 0 && ry == 0) continue;
-        const int y = cell / SG, x = cell - y * SG;
-        const int gy = sg.v0 + y, gx = sg.u0 + x;
-        if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
-        float2 val;
-        val.x = (float)(((double)qx + (double)rx * rinv) * inv);
-        val.y = (float)(((double)qy + (double)ry * rinv) * inv);
-        red_global<float2>(grid + ((int64_t)(sg.ch * NPOL + p) * g.nw + sg.zg) * plane_elems +
-                               (int64_t)gy * g.nx + gx,
-                           val);
+      // Flush the footprint (and clear it for the next segment): warps over
+      // its rows, lanes over its columns.
+      for (int y = box.y0 + warp; y < box.y1; y += NW) {
+        const int gy = sg.v0 + y;
+        for (int x = box.x0 + lane; x < box.x1; x += 32) {
+          const int gx = sg.u0 + x, cell = y * SG + x;
+#pragma unroll
+          for (int p = 0; p < NPOL; ++p) {
+            const int qx = subq[2 * p * SG2 + cell], qy = subq[(2 * p + 1) * SG2 + cell];
+            const int rx = RESID ? subr[2 * p * SG2 + cell] : 0;
+            const int ry = RESID ? subr[(2 * p + 1) * SG2 + cell] : 0;
+            if (qx == 0 && qy == 0 && rx == 0 && ry == 0) continue;
+            subq[2 * p * SG2 + cell] = 0;
+            subq[(2 * p + 1) * SG2 + cell] = 0;
+            if (RESID) {
+              subr[2 * p * SG2 + cell] = 0;
+              subr[(2 * p + 1) * SG2 + cell] = 0;
+            }
+            if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
+            float2 val;
+            val.x = (float)(((double)qx + (double)rx * rinv) * inv);
+            val.y = (float)(((double)qy + (double)ry * rinv) * inv);
+            red_global<float2>(grid + ((int64_t)(sg.ch * NPOL + p) * g.nw + sg.zg) * plane_elems +
+                                   (int64_t)gy * g.nx + gx,
+                               val);
+          }
+        }
       }
-      __syncthreads();
     }
     pos = sg.end;
   }
@@ -1311,18 +1402,29 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   const int ps = (int)g.cf_pol_stride;
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
 
+  __shared__ int s_red[2][NW * 6];
   uint32_t pos = c0;
+  int parity = 0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    // The footprint pass ends in a barrier, which also orders the previous
+    // segment's reads of the subgrid before this segment's staging.
+    const SegBox box = seg_box<NW, 1, false>(sg, pos, smap, sidx, nullptr, nullptr, g, s_red[parity]);
+    parity ^= 1;
+    const bool direct = seg_direct(box, sg.end - pos);
     const CT *gplane = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems;
-    if (!sg.direct) {
-      for (int k = threadIdx.x; k < NPOL * SG2; k += blockDim.x) {
-        const int p = k / SG2, rem = k - p * SG2, y = rem / SG, x = rem - y * SG;
-        const int gy = sg.v0 + y, gx = sg.u0 + x;
-        CT val = czero<CT>();
-        if (gy >= 0 && gy < g.ny && gx >= 0 && gx < g.nx)
-          val = gplane[(int64_t)p * g.nw * plane_elems + (int64_t)gy * g.nx + gx];
-        sub[k] = val;
+    if (!direct) {
+      // Stage the footprint only: warps over its rows, lanes over its columns.
+      for (int y = box.y0 + warp; y < box.y1; y += NW) {
+        const int gy = sg.v0 + y;
+        for (int x = box.x0 + lane; x < box.x1; x += 32) {
+          const int gx = sg.u0 + x;
+          const bool in = gy >= 0 && gy < g.ny && gx >= 0 && gx < g.nx;
+#pragma unroll
+          for (int p = 0; p < NPOL; ++p)
+            sub[p * SG2 + y * SG + x] =
+                in ? gplane[(int64_t)p * g.nw * plane_elems + (int64_t)gy * g.nx + gx] : czero<CT>();
+        }
       }
       __syncthreads();
     }
@@ -1343,7 +1445,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
         inext = sidx[r + NW];
       }
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = plane_sz(g, zc);
+      const int sz = box.sz;
       const int toff = (S - sz) >> 1;
       const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
       const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
@@ -1351,7 +1453,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       const CT *src;
       int64_t pstride;
       RowWalk wk;
-      if (sg.direct) {
+      if (direct) {
         src = gplane + (int64_t)wv * g.nx + wu;
         pstride = (int64_t)g.nw * plane_elems;
         wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
@@ -1411,7 +1513,6 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
         }
       }
     }
-    if (!sg.direct) __syncthreads();
     pos = sg.end;
   }
 }

@@ -88,12 +88,12 @@ unsigned long long arlgpu_kernel_launches(void);
  *   "grid_kernel"   0 = shared-memory atomics with TwoSum compensation,
  *                   1 = band owner: each warp owns a band of the subgrid, plain
  *                       read-modify-write with a per-cell Kahan term,
- *                   2 = as 0, specialised on npol with 32-bit incremental offsets (default),
+ *                   2 = as 0, specialised on npol with 32-bit incremental offsets,
  *                   3 = as 2 without the compensation (measurement only: FP32C
  *                       promises compensated sums, so the autotuner never picks it),
- *                   4 = FP32C tiles summed exactly in 32-bit fixed point, plus a float
- *                       plane of the rounding residuals (needs cf tap_absmax; FP64 and
- *                       an unknown bound use 2),
+ *                   4 = FP32C tiles summed in two-limb 32-bit fixed point: the rounded
+ *                       contributions and their rounding residuals (default; needs cf
+ *                       tap_absmax; FP64 and an unknown bound use 2),
  *                   5 = as 4 without the residual plane (measurement only)
  *   "degrid_kernel" 0 = one warp per row, 1 = 32-row batches per warp,
  *                   2 = one warp per row, specialised on npol, four taps per step (default)
