@@ -403,9 +403,10 @@ __device__ __forceinline__ SegInfo seg_at(uint32_t pos, uint32_t c1, const RowMa
 }
 
 // Footprint of one segment in subgrid coordinates: the bounding box
-// [x0, x1) x [y0, y1) of its rows' windows, the window edge (all rows of a
-// segment share a w-plane, hence a support) and, for the gridder, the largest
-// |Re| / |Im| of vis * weight.  One block-wide pass over the segment's rows;
+// [x0, x1) x [y0, y1) of its rows' windows, the largest window edge (rows of
+// one segment share a grid plane, but under w-projection their cf planes, and
+// so their supports, differ) and, for the gridder, the largest |Re| / |Im| of
+// vis * weight.  One block-wide pass over the segment's rows;
 // contains a __syncthreads.  s_red holds NW * 6 words; callers alternate two
 // such buffers between consecutive segments, so a segment's writes never meet
 // the previous segment's reads when no other barrier lies between them.
@@ -476,7 +477,8 @@ __device__ __forceinline__ SegBox seg_box(const SegInfo &sg, uint32_t pos, const
 }
 
 // A segment goes straight to global memory when its rows' windows do not
-// overlap enough to repay staging: rows * sz^2 taps against the footprint.
+// overlap enough to repay staging: rows * sz^2 taps (sz the largest support)
+// against the footprint.
 __device__ __forceinline__ bool seg_direct(const SegBox &b, uint32_t rows) {
   return (uint64_t)rows * (uint64_t)(b.sz * b.sz) <= (uint64_t)(b.x1 - b.x0) * (uint64_t)(b.y1 - b.y0);
 }
@@ -1091,7 +1093,7 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
         inext = sidx[r + NW];
       }
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = box.sz;
+      const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
       const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
       CT vw[NPOL];
@@ -1275,7 +1277,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         inext = sidx[r + NW];
       }
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = box.sz;
+      const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
       const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
       float2 vw[NPOL];
@@ -1445,7 +1447,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
         inext = sidx[r + NW];
       }
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = box.sz;
+      const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
       const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
       const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
