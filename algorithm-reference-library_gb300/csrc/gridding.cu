@@ -1039,6 +1039,25 @@ __device__ __forceinline__ void row_step(RowWalk &w) {
   }
 }
 
+// Tap walk through a per-CTA byte table.  For an even support sz the taps of
+// a window are numbered t = 0 .. sz^2 - 1 in row-major order and lane l of a
+// warp takes taps l, l + 32, l + 64, ...; tab[tap_base(sz) + t] = t / sz is the
+// window row of tap t.  Tap t then sits at  t + j (S - sz)  in the cf
+// sub-kernel (row stride S) and at  t + j (W - sz)  in a target of row stride
+// W (the shared subgrid, or the grid itself), so a tap costs one byte load
+// and two integer multiply-adds, with no per-tap division or wrap test.
+__host__ __device__ constexpr int tap_base(int sz) {
+  return 4 * (sz / 2 - 1) * (sz / 2) * (sz - 1) / 6;  // sum of s^2 over even s < sz
+}
+__host__ __device__ constexpr int tap_table_bytes(int S) { return (tap_base(S + 2) + 15) & ~15; }
+
+__device__ __forceinline__ void build_tap_table(unsigned char *tab, int S) {
+  for (int sz = 2; sz <= S; sz += 2) {
+    const int b = tap_base(sz), n = sz * sz;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) tab[b + t] = (unsigned char)(t / sz);
+  }
+}
+
 // K3 (lean variant): warp per row, compensated shared-memory atomics as in
 // k_grid, specialised on the polarisation count, with 32-bit incremental
 // offsets into the tap table and the subgrid.
@@ -1056,6 +1075,7 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   // FP32 keeps the compensation planes after all value planes.
   R *sub = reinterpret_cast<R *>(smraw);
   R *comp = sub + (size_t)2 * NPOL * SG2;
+  unsigned char *tab = smraw + (size_t)2 * NPOL * SG2 * ACC::kWords * sizeof(R);
   const uint32_t nvalid = off[g.nbins];
   const uint32_t c0 = blockIdx.x * chunk;
   if (c0 >= nvalid) return;
@@ -1067,6 +1087,7 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
 
   // The planes are zero between segments: the flush clears what it reads.
   for (int k = threadIdx.x; k < 2 * NPOL * SG2 * ACC::kWords; k += blockDim.x) sub[k] = (R)0;
+  build_tap_table(tab, S);
   __shared__ int s_red[2][NW * 6];
   uint32_t pos = c0;
   int parity = 0;
@@ -1107,35 +1128,39 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
       }
       const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
                      ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+      const int n = sz * sz, dk = S - sz;
+      const unsigned char *tj = tab + tap_base(sz) + lane;
+      const CT *kl = kb + lane;
       if (direct) {
-        RowWalk wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
-        CT *gb = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
-                 (int64_t)wv * g.nx + wu;
-        for (int t = lane; t < wk.n; t += 32) {
+        CT *gl = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
+                 (int64_t)wv * g.nx + wu + lane;
+        const int dg = (int)g.nx - sz;
+        for (int t = 0; t + lane < n; t += 32) {
+          const int j = tj[t];
 #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
-            const CT tp = kb[p * ps + wk.ko];
+            const CT tp = kl[p * ps + t + j * dk];
             CT c;
             c.x = tp.x * vw[p].x + tp.y * vw[p].y;
             c.y = tp.x * vw[p].y - tp.y * vw[p].x;
-            red_global<CT>(gb + (int64_t)p * g.nw * plane_elems + wk.so, c);
+            red_global<CT>(gl + (int64_t)p * g.nw * plane_elems + t + j * dg, c);
           }
-          row_step(wk);
         }
         continue;
       }
-      RowWalk wk = row_walk(sz, S, SG, wv - sg.v0, wu - sg.u0, lane);
-      for (int t = lane; t < wk.n; t += 32) {
+      const int wofs = (wv - sg.v0) * SG + (wu - sg.u0) + lane, dg = SG - sz;
+      for (int t = 0; t + lane < n; t += 32) {
+        const int j = tj[t];
+        const int so = wofs + t + j * dg;
 #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
-          const CT tp = kb[p * ps + wk.ko];
+          const CT tp = kl[p * ps + t + j * dk];
           CT c;  // conj(tap) * vw
           c.x = tp.x * vw[p].x + tp.y * vw[p].y;
           c.y = tp.x * vw[p].y - tp.y * vw[p].x;
-          ACC::add1(sub + 2 * p * SG2 + wk.so, comp + 2 * p * SG2 + wk.so, c.x);
-          ACC::add1(sub + (2 * p + 1) * SG2 + wk.so, comp + (2 * p + 1) * SG2 + wk.so, c.y);
+          ACC::add1(sub + 2 * p * SG2 + so, comp + 2 * p * SG2 + so, c.x);
+          ACC::add1(sub + (2 * p + 1) * SG2 + so, comp + (2 * p + 1) * SG2 + so, c.y);
         }
-        row_step(wk);
       }
     }
 #pragma unroll
@@ -1180,26 +1205,26 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
 // K3 (fixed-point variant, FP32C only; grid_kernel 4 and 5).
 //
 // Each staged segment (the rows of one bin inside one chunk) is accumulated in
-// 32-bit integers.  A pre-pass over the segment's rows finds the largest
-// |Re| / |Im| of vis * weight, vmax; with tap_absmax bounding every tap
+// 32-bit integers.  The footprint pass over the segment's rows also finds the
+// largest |Re| / |Im| of vis * weight, vmax; with tap_absmax bounding every tap
 // component, each contribution conj(tap) * vis * weight has components of at
-// most B = 2 * tap_absmax * vmax.  Contributions are scaled by L / B, with
-// L = min(2^21, 2^30 / rows), rounded to integers by one FMA with the
-// 1.5 * 2^23 shift (exact round-to-nearest for magnitudes below 2^22), and
-// added with integer shared-memory atomics whose result is unused: the tile
-// sums are exact and independent of the order of the atomics, and no warp
-// waits on an atomic's returned value.  A cell sums at most `rows`
-// contributions, so it stays below 2^30.
+// most B = 2 * tap_absmax * vmax.  Contributions are scaled by 2^e, the
+// largest power of two <= L / B with L = min(2^21, 2^30 / rows), rounded to
+// integers by one FMA with the 1.5 * 2^23 shift (exact round-to-nearest for
+// magnitudes below 2^22), and added with integer shared-memory atomics whose
+// result is unused: the tile sums are exact and independent of the order of
+// the atomics, and no warp waits on an atomic's returned value.  A cell sums
+// at most `rows` contributions, so it stays below 2^30.
 //
 // RESID (grid_kernel 4, the FP32C gridder when tap_absmax is given): the
-// rounding residual of each scaled contribution, x * L / B - round(x * L / B)
-// (one FMA, |residual| <= 1/2), is rounded to units of 1 / R, R = min(2^20,
-// 2^30 / rows), and summed in a second integer plane.  A flushed cell is
-// (sum + residual sum / R) * B / L: the sum of the FP32 contributions to
-// within B / (2 L R) per contribution, about 2^-42 of the segment's largest
-// one for segments of up to 512 rows.  Without RESID (grid_kernel 5,
-// measurement only) each contribution carries a quantisation error of at most
-// B / L / 2.
+// rounding residual of each scaled contribution (one FMA, |residual| <= 1/2)
+// is rounded to units of 2^-f, f = min(20, 30 - ceil(log2 rows)), and summed
+// in a second integer plane.  A flushed cell is (sum + residual sum 2^-f) 2^-e,
+// formed with one FMA: the sum of the FP32 contributions to within 2^-f-1 of a
+// unit per contribution (about 2^-42 of the segment's largest contribution for
+// segments of up to 512 rows) plus the final FP32 rounding.  Without RESID
+// (grid_kernel 5, measurement only) each contribution carries a quantisation
+// error of up to half a unit, 2^-e-1.
 template <bool RESID>
 __device__ __forceinline__ void fx_add(int *q, int *r, float x, float scale, float rscale) {
   const float t = fmaf(x, scale, 12582912.0f);
@@ -1229,6 +1254,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   int *subq = reinterpret_cast<int *>(smraw);
   int *subr = subq + (size_t)2 * NPOL * SG2;
   constexpr int kPlanes = RESID ? 4 * NPOL : 2 * NPOL;
+  unsigned char *tab = smraw + (size_t)kPlanes * SG2 * 4;
   const uint32_t nvalid = off[g.nbins];
   const uint32_t c0 = blockIdx.x * chunk;
   if (c0 >= nvalid) return;
@@ -1238,6 +1264,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   const int ps = (int)g.cf_pol_stride;
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
   for (int k = threadIdx.x; k < kPlanes * SG2; k += blockDim.x) subq[k] = 0;
+  build_tap_table(tab, S);
 
   uint32_t pos = c0;
   int parity = 0;
@@ -1247,17 +1274,23 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
     parity ^= 1;
     const uint32_t rows = sg.end - pos;
     const bool direct = seg_direct(box, rows);
-    float scale = 0.f, rscale = 0.f;
-    double inv = 0.0, rinv = 0.0;
+    // Power-of-two units, so that unscaling at the flush is exact:
+    // scale = 2^e <= L / B, rscale = 2^f <= min(2^20, 2^30 / rows).
+    float scale = 0.f, inv = 0.f, rscale = 0.f, rinv = 0.f;
     if (!direct) {
-      const double lim = rows <= 512u ? 2097152.0 : 1073741824.0 / (double)rows;
-      const double bound = 2.0 * (double)g.tap_absmax * (double)box.vmax;
-      if (bound > 0.0) {
-        scale = (float)fmin(lim / bound, 1e30);  // tiny segments: coarser units, never inf
-        inv = 1.0 / (double)scale;
+      const float lim = rows <= 512u ? 2097152.f : 1073741824.f / (float)rows;
+      const float bound = 2.f * g.tap_absmax * box.vmax;
+      if (bound > 0.f) {
+        const float q = fminf(lim / bound, 1e30f);  // tiny segments: coarser units, never inf
+        int e;
+        frexpf(q, &e);  // q = m 2^e, m in [1/2, 1)
+        scale = ldexpf(1.f, e - 1);
+        inv = ldexpf(1.f, 1 - e);
       }
-      rscale = rows <= 1024u ? 1048576.0f : (float)(1073741824.0 / (double)rows);
-      rinv = 1.0 / (double)rscale;
+      const int lr = 32 - __clz((int)rows - 1);  // ceil(log2(rows))
+      const int f = min(20, 30 - lr);
+      rscale = ldexpf(1.f, f);
+      rinv = ldexpf(1.f, -f);
     }
     double wsum[NPOL];
 #pragma unroll
@@ -1291,48 +1324,62 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       }
       const float2 *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
                          ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+      const int n = sz * sz, dk = S - sz;
+      const unsigned char *tj = tab + tap_base(sz) + lane;
+      const float2 *kl = kb + lane;
       if (direct) {
-        RowWalk wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
-        float2 *gb = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
-                     (int64_t)wv * g.nx + wu;
-        for (int t = lane; t < wk.n; t += 32) {
+        float2 *gl = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
+                     (int64_t)wv * g.nx + wu + lane;
+        const int dg = (int)g.nx - sz;
+        for (int t = 0; t + lane < n; t += 32) {
+          const int j = tj[t];
 #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
-            const float2 tp = kb[p * ps + wk.ko];
+            const float2 tp = kl[p * ps + t + j * dk];
             float2 c;
             c.x = tp.x * vw[p].x + tp.y * vw[p].y;
             c.y = tp.x * vw[p].y - tp.y * vw[p].x;
-            red_global<float2>(gb + (int64_t)p * g.nw * plane_elems + wk.so, c);
+            red_global<float2>(gl + (int64_t)p * g.nw * plane_elems + t + j * dg, c);
           }
-          row_step(wk);
         }
         continue;
       }
-      RowWalk wk = row_walk(sz, S, SG, wv - sg.v0, wu - sg.u0, lane);
-      // Four taps per lane per iteration: the tap loads of all four are in
-      // flight before the first atomic.
-      for (int t = lane; t < wk.n; t += 128) {
-        int so[4];
+      const int wofs = (wv - sg.v0) * SG + (wu - sg.u0) + lane, dg = SG - sz;
+      // Full warp steps four at a time (all tap loads in flight before the
+      // first atomic), then single steps, then the partial last step.
+      const int nfull = n >> 5;
+      int t = 0;
+      for (; t + 128 <= (nfull << 5); t += 128) {
+        int j[4];
         float2 tp[NPOL][4];
-        bool on[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          on[u] = t + 32 * u < wk.n;
-          so[u] = wk.so;
+          j[u] = tj[t + 32 * u];
 #pragma unroll
-          for (int p = 0; p < NPOL; ++p) tp[p][u] = on[u] ? kb[p * ps + wk.ko] : make_float2(0.f, 0.f);
-          row_step(wk);
+          for (int p = 0; p < NPOL; ++p) tp[p][u] = kl[p * ps + t + 32 * u + j[u] * dk];
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          if (!on[u]) break;
+          const int so = wofs + t + 32 * u + j[u] * dg;
 #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
             const float cx = tp[p][u].x * vw[p].x + tp[p][u].y * vw[p].y;  // conj(tap) * vw
             const float cy = tp[p][u].x * vw[p].y - tp[p][u].y * vw[p].x;
-            fx_add<RESID>(subq + 2 * p * SG2 + so[u], subr + 2 * p * SG2 + so[u], cx, scale, rscale);
-            fx_add<RESID>(subq + (2 * p + 1) * SG2 + so[u], subr + (2 * p + 1) * SG2 + so[u], cy, scale, rscale);
+            fx_add<RESID>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
+            fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
           }
+        }
+      }
+      for (; t + lane < n; t += 32) {
+        const int j = tj[t];
+        const int so = wofs + t + j * dg;
+#pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          const float2 tp = kl[p * ps + t + j * dk];
+          const float cx = tp.x * vw[p].x + tp.y * vw[p].y;
+          const float cy = tp.x * vw[p].y - tp.y * vw[p].x;
+          fx_add<RESID>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
+          fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
         }
       }
     }
@@ -1363,9 +1410,11 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
               subr[(2 * p + 1) * SG2 + cell] = 0;
             }
             if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
+            // inv and rinv * inv are powers of two: one rounding in the FMA
+            // (and in the int -> float conversions of sums beyond 2^24)
             float2 val;
-            val.x = (float)(((double)qx + (double)rx * rinv) * inv);
-            val.y = (float)(((double)qy + (double)ry * rinv) * inv);
+            val.x = fmaf((float)rx, rinv * inv, (float)qx * inv);
+            val.y = fmaf((float)ry, rinv * inv, (float)qy * inv);
             red_global<float2>(grid + ((int64_t)(sg.ch * NPOL + p) * g.nw + sg.zg) * plane_elems +
                                    (int64_t)gy * g.nx + gx,
                                val);
@@ -1389,6 +1438,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   extern __shared__ __align__(16) unsigned char smraw[];
   const int SG = g.SG, SG2 = SG * SG;
   CT *sub = reinterpret_cast<CT *>(smraw);
+  unsigned char *tab = smraw + (size_t)NPOL * SG2 * sizeof(CT);
   const uint32_t nvalid = off[g.nbins];
   const uint32_t c0 = blockIdx.x * chunk;
   if (c0 >= (uint32_t)nvis) return;
@@ -1405,6 +1455,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
 
   __shared__ int s_red[2][NW * 6];
+  build_tap_table(tab, S);  // ordered before first use by the barrier in seg_box
   uint32_t pos = c0;
   int parity = 0;
   while (pos < c1) {
@@ -1452,52 +1503,55 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
       const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
                      ((int64_t)(vf * O + uf) * S + toff) * S + toff;
-      const CT *src;
+      const CT *gl;
       int64_t pstride;
-      RowWalk wk;
+      int dg;
       if (direct) {
-        src = gplane + (int64_t)wv * g.nx + wu;
+        gl = gplane + (int64_t)wv * g.nx + wu + lane;
         pstride = (int64_t)g.nw * plane_elems;
-        wk = row_walk(sz, S, (int)g.nx, 0, 0, lane);
+        dg = (int)g.nx - sz;
       } else {
-        src = sub;
+        gl = sub + (wv - sg.v0) * SG + (wu - sg.u0) + lane;
         pstride = SG2;
-        wk = row_walk(sz, S, SG, wv - sg.v0, wu - sg.u0, lane);
+        dg = SG - sz;
       }
+      const int n = sz * sz, dk = S - sz;
+      const unsigned char *tj = tab + tap_base(sz) + lane;
+      const CT *kl = kb + lane;
       R ax[NPOL], ay[NPOL];
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = 0;
-      // Four taps per lane per iteration: all eight loads are issued before
-      // the multiply-adds that use them.
-      for (int t = lane; t < wk.n; t += 128) {
-        int ko[4], so[4];
-        bool on[4];
+      // Full warp steps four at a time (all loads in flight before the
+      // multiply-adds that use them), then single steps, then the partial
+      // last step.
+      const int nfull = n >> 5;
+      int t = 0;
+      for (; t + 128 <= (nfull << 5); t += 128) {
+        int j[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          on[u] = t + 32 * u < wk.n;
-          ko[u] = wk.ko;
-          so[u] = wk.so;
-          row_step(wk);
-        }
+        for (int u = 0; u < 4; ++u) j[u] = tj[t + 32 * u];
 #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
-          const CT *sp = src + p * pstride;
           CT tp[4], gv[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            if (on[u]) {
-              tp[u] = kb[p * ps + ko[u]];
-              gv[u] = sp[so[u]];
-            } else {
-              tp[u] = czero<CT>();
-              gv[u] = czero<CT>();
-            }
+            tp[u] = kl[p * ps + t + 32 * u + j[u] * dk];
+            gv[u] = gl[p * pstride + t + 32 * u + j[u] * dg];
           }
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             ax[p] += gv[u].x * tp[u].x - gv[u].y * tp[u].y;
             ay[p] += gv[u].x * tp[u].y + gv[u].y * tp[u].x;
           }
+        }
+      }
+      for (; t + lane < n; t += 32) {
+        const int j = tj[t];
+#pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          const CT tp = kl[p * ps + t + j * dk], gv = gl[p * pstride + t + j * dg];
+          ax[p] += gv.x * tp.x - gv.y * tp.y;
+          ay[p] += gv.x * tp.y + gv.y * tp.x;
         }
       }
 #pragma unroll
@@ -1670,7 +1724,7 @@ static inline uint32_t chunk_rows() { return (uint32_t)g_tune_chunk.load(); }
 
 static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const void *vis, const void *wt,
                           const void *cf, void *grid, double *sumwt, bool resid, cudaStream_t st) {
-  const size_t smem = (size_t)(resid ? 4 : 2) * g.npol * g.SG * g.SG * 4;
+  const size_t smem = (size_t)(resid ? 4 : 2) * g.npol * g.SG * g.SG * 4 + tap_table_bytes(g.S);
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
   void (*kern)(Geom, const RowMap *, const uint32_t *, const uint32_t *, uint32_t, const float2 *, const float *,
                const float2 *, float2 *, double *);
@@ -1704,11 +1758,12 @@ static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const voi
     kern = g.npol == 1 ? k_grid_lean<R, 1, kWarps> : g.npol == 2 ? k_grid_lean<R, 2, kWarps>
                                                                   : k_grid_lean<R, 4, kWarps>;
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean gridder handles 1, 2 or 4 polarisations");
+    smem += tap_table_bytes(g.S);
   } else if (g_tune_grid_kernel.load() == 3) {
     kern = g.npol == 1 ? k_grid_lean<R, 1, kWarps, PlainAcc<R>>
                        : g.npol == 2 ? k_grid_lean<R, 2, kWarps, PlainAcc<R>> : k_grid_lean<R, 4, kWarps, PlainAcc<R>>;
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean gridder handles 1, 2 or 4 polarisations");
-    smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T);
+    smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T) + tap_table_bytes(g.S);
   } else if (g_tune_grid_kernel.load() >= 4) {
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean gridder handles 1, 2 or 4 polarisations");
     if (sizeof(R) == 4 && g.tap_absmax > 0.f)
@@ -1716,6 +1771,7 @@ static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const voi
     // FP64, or no tap bound: the compensated float variant
     kern = g.npol == 1 ? k_grid_lean<R, 1, kWarps> : g.npol == 2 ? k_grid_lean<R, 2, kWarps>
                                                                   : k_grid_lean<R, 4, kWarps>;
+    smem += tap_table_bytes(g.S);
   }
   // The lean variants' planar subgrid has the same size as the interleaved one.
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
@@ -1744,7 +1800,9 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
     kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps> : g.npol == 2 ? k_degrid_lean<R, 2, kWarps>
                                                                     : k_degrid_lean<R, 4, kWarps>;
+    smem += tap_table_bytes(g.S);
   }
+  if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "degridder needs %zu bytes of shared memory", smem);
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t chunk = chunk_rows();
   unsigned blocks = (unsigned)((nvis + chunk - 1) / chunk);
