@@ -1089,16 +1089,23 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   for (int k = threadIdx.x; k < 2 * NPOL * SG2 * ACC::kWords; k += blockDim.x) sub[k] = (R)0;
   build_tap_table(tab, S);
   __shared__ int s_red[2][NW * 6];
+  __shared__ uint32_t s_next[2];
   uint32_t pos = c0;
   int parity = 0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    if (threadIdx.x == 0) s_next[parity] = pos + NW;  // published by the barrier in seg_box
+    uint32_t *next_row = &s_next[parity];
     const SegBox box = seg_box<NW, 1, false>(sg, pos, smap, sidx, nullptr, nullptr, g, s_red[parity]);
     parity ^= 1;
     const bool direct = seg_direct(box, sg.end - pos);
     double wsum[NPOL];
 #pragma unroll
     for (int p = 0; p < NPOL; ++p) wsum[p] = 0.0;
+    // Rows after each warp's first come from a shared counter, one at a
+    // time, which balances rows of different support across the warps; each
+    // warp holds the next row's index and metadata while it computes the
+    // current one.
     uint32_t r = pos + warp;
     RowMap mnext;
     uint32_t inext = 0;
@@ -1106,13 +1113,17 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
       mnext = smap[r];
       inext = sidx[r];
     }
-    for (; r < sg.end; r += NW) {
+    while (r < sg.end) {
       const RowMap m = mnext;
       const uint32_t idx = inext;
-      if (r + NW < sg.end) {  // next row's metadata in flight during this row
-        mnext = smap[r + NW];
-        inext = sidx[r + NW];
+      uint32_t rn = 0;
+      if (lane == 0) rn = atomicAdd(next_row, 1u);
+      rn = __shfl_sync(0xffffffffu, rn, 0);
+      if (rn < sg.end) {
+        mnext = smap[rn];
+        inext = sidx[rn];
       }
+      r = rn;
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
       const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
@@ -1266,10 +1277,13 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   for (int k = threadIdx.x; k < kPlanes * SG2; k += blockDim.x) subq[k] = 0;
   build_tap_table(tab, S);
 
+  __shared__ uint32_t s_next[2];
   uint32_t pos = c0;
   int parity = 0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    if (threadIdx.x == 0) s_next[parity] = pos + NW;  // published by the barrier in seg_box
+    uint32_t *next_row = &s_next[parity];
     const SegBox box = seg_box<NW, NPOL, true>(sg, pos, smap, sidx, vis, wt, g, s_red[parity]);
     parity ^= 1;
     const uint32_t rows = sg.end - pos;
@@ -1295,6 +1309,10 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
     double wsum[NPOL];
 #pragma unroll
     for (int p = 0; p < NPOL; ++p) wsum[p] = 0.0;
+    // Rows after each warp's first come from a shared counter, one at a
+    // time, which balances rows of different support across the warps; each
+    // warp holds the next row's index and metadata while it computes the
+    // current one.
     uint32_t r = pos + warp;
     RowMap mnext;
     uint32_t inext = 0;
@@ -1302,13 +1320,17 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       mnext = smap[r];
       inext = sidx[r];
     }
-    for (; r < sg.end; r += NW) {
+    while (r < sg.end) {
       const RowMap m = mnext;
       const uint32_t idx = inext;
-      if (r + NW < sg.end) {
-        mnext = smap[r + NW];
-        inext = sidx[r + NW];
+      uint32_t rn = 0;
+      if (lane == 0) rn = atomicAdd(next_row, 1u);
+      rn = __shfl_sync(0xffffffffu, rn, 0);
+      if (rn < sg.end) {
+        mnext = smap[rn];
+        inext = sidx[rn];
       }
+      r = rn;
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
       const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
@@ -1345,21 +1367,23 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         continue;
       }
       const int wofs = (wv - sg.v0) * SG + (wu - sg.u0) + lane, dg = SG - sz;
-      // Full warp steps four at a time (all tap loads in flight before the
-      // first atomic), then single steps, then the partial last step.
-      const int nfull = n >> 5;
-      int t = 0;
-      for (; t + 128 <= (nfull << 5); t += 128) {
+      // Four warp steps at a time, the last group masked per lane: all tap
+      // loads of a group are in flight before its first atomic.
+      for (int t = 0; t < n; t += 128) {
         int j[4];
+        bool on[4];
         float2 tp[NPOL][4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          j[u] = tj[t + 32 * u];
+          on[u] = t + 32 * u + lane < n;
+          j[u] = on[u] ? tj[t + 32 * u] : 0;
 #pragma unroll
-          for (int p = 0; p < NPOL; ++p) tp[p][u] = kl[p * ps + t + 32 * u + j[u] * dk];
+          for (int p = 0; p < NPOL; ++p)
+            tp[p][u] = on[u] ? kl[p * ps + t + 32 * u + j[u] * dk] : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
+          if (!on[u]) break;
           const int so = wofs + t + 32 * u + j[u] * dg;
 #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
@@ -1368,18 +1392,6 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
             fx_add<RESID>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
             fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
           }
-        }
-      }
-      for (; t + lane < n; t += 32) {
-        const int j = tj[t];
-        const int so = wofs + t + j * dg;
-#pragma unroll
-        for (int p = 0; p < NPOL; ++p) {
-          const float2 tp = kl[p * ps + t + j * dk];
-          const float cx = tp.x * vw[p].x + tp.y * vw[p].y;
-          const float cy = tp.x * vw[p].y - tp.y * vw[p].x;
-          fx_add<RESID>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
-          fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
         }
       }
     }
@@ -1455,11 +1467,14 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
 
   __shared__ int s_red[2][NW * 6];
+  __shared__ uint32_t s_next[2];
   build_tap_table(tab, S);  // ordered before first use by the barrier in seg_box
   uint32_t pos = c0;
   int parity = 0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    if (threadIdx.x == 0) s_next[parity] = pos + NW;  // published by the barrier in seg_box
+    uint32_t *next_row = &s_next[parity];
     // The footprint pass ends in a barrier, which also orders the previous
     // segment's reads of the subgrid before this segment's staging.
     const SegBox box = seg_box<NW, 1, false>(sg, pos, smap, sidx, nullptr, nullptr, g, s_red[parity]);
@@ -1483,6 +1498,10 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
     }
     // Rows of this warp: r = pos + warp, pos + warp + NW, ...; the metadata of
     // the next row is loaded while the current one is computed.
+    // Rows after each warp's first come from a shared counter, one at a
+    // time, which balances rows of different support across the warps; each
+    // warp holds the next row's index and metadata while it computes the
+    // current one.
     uint32_t r = pos + warp;
     RowMap mnext;
     uint32_t inext = 0;
@@ -1490,13 +1509,17 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       mnext = smap[r];
       inext = sidx[r];
     }
-    for (; r < sg.end; r += NW) {
+    while (r < sg.end) {
       const RowMap m = mnext;
       const uint32_t idx = inext;
-      if (r + NW < sg.end) {
-        mnext = smap[r + NW];
-        inext = sidx[r + NW];
+      uint32_t rn = 0;
+      if (lane == 0) rn = atomicAdd(next_row, 1u);
+      rn = __shfl_sync(0xffffffffu, rn, 0);
+      if (rn < sg.end) {
+        mnext = smap[rn];
+        inext = sidx[rn];
       }
+      r = rn;
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
       const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
@@ -1521,37 +1544,29 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       R ax[NPOL], ay[NPOL];
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = 0;
-      // Full warp steps four at a time (all loads in flight before the
-      // multiply-adds that use them), then single steps, then the partial
-      // last step.
-      const int nfull = n >> 5;
-      int t = 0;
-      for (; t + 128 <= (nfull << 5); t += 128) {
+      // Four warp steps at a time, the last group masked per lane: all loads
+      // of a group are in flight before the multiply-adds that use them.
+      for (int t = 0; t < n; t += 128) {
         int j[4];
+        bool on[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) j[u] = tj[t + 32 * u];
+        for (int u = 0; u < 4; ++u) {
+          on[u] = t + 32 * u + lane < n;
+          j[u] = on[u] ? tj[t + 32 * u] : 0;
+        }
 #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
           CT tp[4], gv[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            tp[u] = kl[p * ps + t + 32 * u + j[u] * dk];
-            gv[u] = gl[p * pstride + t + 32 * u + j[u] * dg];
+            tp[u] = on[u] ? kl[p * ps + t + 32 * u + j[u] * dk] : czero<CT>();
+            gv[u] = on[u] ? gl[p * pstride + t + 32 * u + j[u] * dg] : czero<CT>();
           }
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             ax[p] += gv[u].x * tp[u].x - gv[u].y * tp[u].y;
             ay[p] += gv[u].x * tp[u].y + gv[u].y * tp[u].x;
           }
-        }
-      }
-      for (; t + lane < n; t += 32) {
-        const int j = tj[t];
-#pragma unroll
-        for (int p = 0; p < NPOL; ++p) {
-          const CT tp = kl[p * ps + t + j * dk], gv = gl[p * pstride + t + j * dg];
-          ax[p] += gv.x * tp.x - gv.y * tp.y;
-          ay[p] += gv.x * tp.y + gv.y * tp.x;
         }
       }
 #pragma unroll
