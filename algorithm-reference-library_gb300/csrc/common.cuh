@@ -47,6 +47,13 @@ struct Geom {
   const int32_t *plane_support;        // device, may be null
   float tap_absmax;                    // bound of |Re|, |Im| over the cf taps (0: unknown)
   int32_t fast_uv;                     // 1: u/v mapping may use the one-FMA fast path
+  // Sub-pixel fast path (fast_uv with a power-of-two O): X = P * O by one FMA,
+  // pixel and sub-pixel index from floor(X) by integer shifts.
+  int32_t pow2O, log2O;
+  double rOu, cOu, rOv, cOv;           // X = fma(u, rOu, cOu)
+  double Xlim_u, Xlim_v, tolX_u, tolX_v;
+  // Nearest-plane axes (WW grid, WW cf, FREQ): |P| < Plim uses the fixed tolerance
+  double Plim_w, tol_w, Plim_z, tol_z, Plim_f, tol_f;
   // binning
   int32_t T;       // tile edge (grid pixels)
   int32_t SG;      // staged subgrid edge = T + S

@@ -127,10 +127,41 @@ struct RawMap {
   double pu, pv, uf, vf, zg, zc, ch;
 };
 
+// Nearest-plane index with a tolerance fixed per axis on the host (valid for
+// |P| < Plim, which covers every in-range index): the exact sequence when the
+// fast value is within tol of a half-integer or beyond Plim.
+__device__ __forceinline__ double round_w2p_tol(double x, const arlgpu_axis &a, double rcp, double Plim,
+                                                double tol) {
+  const double p = fma(__dsub_rn(x, a.crval), rcp, a.crpix - 1.0);
+  const double r = rint(p);
+  if (fabs(p) < Plim && fabs(p - r) < 0.5 - tol) return r;
+  return rint(w2p_exact(x, a));
+}
+
+// Pixel and sub-pixel index of one axis from X = P * O (power-of-two O): away
+// from integers of X, rint(P) = floor((floor(X) + O/2) / O) and the sub-pixel
+// index is the remainder.  Returns false when X is within tol of an integer or
+// beyond Xlim (the caller then takes the exact sequence).
+__device__ __forceinline__ bool map_axis_x(double x, double rO, double cO, double Xlim, double tol, int O,
+                                           int log2O, double *pix, double *sub) {
+  const double X = fma(x, rO, cO);
+  if (!(fabs(X) < Xlim)) return false;
+  const double n = floor(X), fr = X - n;
+  if (fr < tol || fr > 1.0 - tol) return false;
+  const int a = (int)n + (O >> 1);
+  const int pu = a >> log2O;  // arithmetic shift: floor division by O
+  *pix = (double)pu;
+  *sub = (double)(a - (pu << log2O));
+  return true;
+}
+
 __device__ __forceinline__ RawMap map_raw(double u, double v, double w, double f, const Geom &g) {
   RawMap r;
   bool exact = !g.fast_uv;
-  if (!exact) {
+  if (!exact && g.pow2O) {
+    exact = !(map_axis_x(u, g.rOu, g.cOu, g.Xlim_u, g.tolX_u, g.O, g.log2O, &r.pu, &r.uf) &&
+              map_axis_x(v, g.rOv, g.cOv, g.Xlim_v, g.tolX_v, g.O, g.log2O, &r.pv, &r.vf));
+  } else if (!exact) {
     // One-FMA fast path (valid when crval == 0 on UU, VV, DUU, DVV and the cf's
     // DUU / DVV cdelt is the grid cdelt / O; the host checks this).  With
     // P = u / cdelt + crpix - 1, the nearest pixel is rint(P) and the sub-pixel
@@ -153,9 +184,9 @@ __device__ __forceinline__ RawMap map_raw(double u, double v, double w, double f
     map_axis_exact(u, g.gu, g.rcp_gu, g.cdu, g.rcp_cdu, &r.pu, &r.uf);
     map_axis_exact(v, g.gv, g.rcp_gv, g.cdv, g.rcp_cdv, &r.pv, &r.vf);
   }
-  r.zg = round_w2p_fma(w, g.gw, g.rcp_gw);
-  r.zc = round_w2p_fma(w, g.cz, g.rcp_cz);
-  r.ch = round_w2p_fma(f, g.gf, g.rcp_gf);
+  r.zg = round_w2p_tol(w, g.gw, g.rcp_gw, g.Plim_w, g.tol_w);
+  r.zc = round_w2p_tol(w, g.cz, g.rcp_cz, g.Plim_z, g.tol_z);
+  r.ch = round_w2p_tol(f, g.gf, g.rcp_gf, g.Plim_f, g.tol_f);
   return r;
 }
 
@@ -1648,7 +1679,33 @@ int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precisio
                  integral(cd->dv.crpix) && cd->du.cdelt == gd->u.cdelt / cd->oversampling &&
                  cd->dv.cdelt == gd->v.cdelt / cd->oversampling && fabs(gd->u.crpix) < 1e9 &&
                  fabs(gd->v.crpix) < 1e9;
+    const int O = cd->oversampling;
+    g->pow2O = g->fast_uv && O >= 2 && (O & (O - 1)) == 0 && O <= 256 && cd->du.crpix - 1.0 == (double)(O / 2) &&
+               cd->dv.crpix - 1.0 == (double)(O / 2);
+    g->log2O = 0;
+    while ((1 << g->log2O) < O) ++g->log2O;
+    // X = fma(u, rcp * O, (crpix - 1) O) is within ~2.2e-16 (|X| + |cO|) of the
+    // exact value and NumPy's sequence within a few ulps of it: tol has a
+    // 10x margin over both for every |X| < Xlim.
+    g->rOu = g->rcp_gu * O;
+    g->rOv = g->rcp_gv * O;
+    g->cOu = (gd->u.crpix - 1.0) * O;
+    g->cOv = (gd->v.crpix - 1.0) * O;
+    g->Xlim_u = ((double)gd->nx + 2.0 * cd->support + 4.0) * O + fabs(g->cOu);
+    g->Xlim_v = ((double)gd->ny + 2.0 * cd->support + 4.0) * O + fabs(g->cOv);
+    g->tolX_u = 1e-14 * (g->Xlim_u + fabs(g->cOu) + 2.0 * O);
+    g->tolX_v = 1e-14 * (g->Xlim_v + fabs(g->cOv) + 2.0 * O);
+    if (g->Xlim_u > 1e9 || g->Xlim_v > 1e9) g->pow2O = 0;  // keep floor(X) within int range
   }
+  // Fixed tolerances of the nearest-plane axes, valid for |P| < Plim (the
+  // per-row tolerance 1e-14 (|P| + |crpix| + 2) of the exact-fallback test,
+  // bounded over that range).
+  g->Plim_w = (double)gd->nw + 2.0;
+  g->tol_w = 1e-14 * (g->Plim_w + fabs(gd->w.crpix) + 2.0);
+  g->Plim_z = (double)cd->nz + 2.0;
+  g->tol_z = 1e-14 * (g->Plim_z + fabs(cd->z.crpix) + 2.0);
+  g->Plim_f = (double)gd->nchan + 2.0;
+  g->tol_f = 1e-14 * (g->Plim_f + fabs(gd->f.crpix) + 2.0);
   // Subgrid edge: 64 cells when npol planes of it (with the FP32 compensation
   // words) fit in 64 KiB of shared memory, else 32.
   const size_t cell = precision == ARLGPU_FP64 ? 16 : 16;  // c128, or c64 sum + c64 comp

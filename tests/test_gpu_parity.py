@@ -63,18 +63,20 @@ def test_mapping_matches_golden(arl, golden):
         assert numpy.array_equal(got, want)
 
 
-def test_mapping_bit_exact_at_rounding_boundaries(arl, oracle):
+@pytest.mark.parametrize('N,cell,O', [(512, 1e-3, 8), (1024, 3e-4, 16), (256, 2e-3, 6)])
+def test_mapping_bit_exact_at_rounding_boundaries(arl, oracle, N, cell, O):
     """Rows placed exactly on (and one ulp either side of) the half-pixel and
-    sub-pixel boundaries where round-half-even / floor decide the index."""
-    N, cell, O, S = 512, 1e-3, 8, 8
+    sub-pixel boundaries where round-half-even / floor decide the index (power
+    of two oversampling takes the X = P * O path, 6 the one-FMA path)."""
+    S = 8
     im = make_image(arl, N, cell, [1e8], 1e6)
     gd = arl.create_griddata_from_image(im)
     cf = arl.create_convolutionfunction_from_image(im, oversampling=O, support=S)
     du = gd.grid_wcs.wcs.cdelt[0]
     rng = numpy.random.default_rng(5)
-    k = rng.integers(-200, 200, 4000).astype(float)
+    k = rng.integers(-N // 3, N // 3, 4000).astype(float)
     base = numpy.concatenate([(k + 0.5) * du, (k + 0.5 + rng.integers(0, O, 4000) / O) * du,
-                              rng.uniform(-200, 200, 4000) * du])
+                              rng.uniform(-N // 3, N // 3, 4000) * du])
     u = numpy.concatenate([base, numpy.nextafter(base, numpy.inf), numpy.nextafter(base, -numpy.inf)])
     n = u.size
     uvw = numpy.stack([u, u[::-1], rng.uniform(-100, 100, n)], axis=1)
