@@ -27,5 +27,10 @@ from .kernels import (apply_bounding_box_convolutionfunction, calculate_bounding
                       set_plane_support, support_schedule)
 from .wcs import WCS  # noqa: F401
 from .wstack import WStackImager  # noqa: F401
+from .weighting import (grid_weight_to_griddata, griddata_merge_weights, griddata_reweight,  # noqa: F401
+                        weight_visibility)
+from .coalesce import (convert_blockvisibility_to_visibility, convert_visibility_to_blockvisibility,  # noqa: F401
+                       decoalesce_visibility)
+from .data_models import copy_blockvisibility  # noqa: F401
 
 __version__ = '0.1.0'

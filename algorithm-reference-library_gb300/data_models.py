@@ -180,33 +180,90 @@ class Visibility:
 
 
 class BlockVisibility:
-    """Baseline-block visibility table (``memory_data_models.py:940-1093``): uvw
-    in metres, vis [ntimes, nants, nants, nchan, npol]; baseline (a1 < a2) is
-    stored at [a2, a1]."""
+    """Baseline-block visibility table (``memory_data_models.py:940-1093``).
 
-    def __init__(self, frequency, channel_bandwidth, uvw, time, vis, weight=None, phasecentre=None,
-                 polarisation_frame=PolarisationFrame('stokesI'), configuration=None):
+    ``data`` is ARL's structured array with one record per time: index, uvw
+    [nants, nants, 3] in metres, time, integration_time, vis / weight /
+    imaging_weight [nants, nants, nchan, npol].  Baseline (a1 < a2) is stored
+    at [a2, a1]."""
+
+    def __init__(self, data=None, frequency=None, channel_bandwidth=None, phasecentre=None, configuration=None,
+                 uvw=None, time=None, vis=None, weight=None, integration_time=None,
+                 polarisation_frame=PolarisationFrame('stokesI'), imaging_weight=None, source='anonymous',
+                 meta=None):
+        if data is None and vis is not None:
+            ntimes, nants, _, nchan, npol = vis.shape
+            if weight is None:
+                weight = numpy.ones(vis.shape)
+            if imaging_weight is None:
+                imaging_weight = weight
+            assert numpy.shape(weight) == vis.shape
+            assert len(frequency) == nchan and len(channel_bandwidth) == nchan
+            desc = [('index', 'i8'), ('uvw', 'f8', (nants, nants, 3)), ('time', 'f8'),
+                    ('integration_time', 'f8'), ('vis', 'c16', (nants, nants, nchan, npol)),
+                    ('weight', 'f8', (nants, nants, nchan, npol)),
+                    ('imaging_weight', 'f8', (nants, nants, nchan, npol))]
+            data = numpy.zeros(shape=[ntimes], dtype=desc)
+            data['index'] = numpy.arange(ntimes)
+            data['uvw'] = uvw
+            data['time'] = time if time is not None else 0.0
+            data['integration_time'] = integration_time if integration_time is not None else 0.0
+            data['vis'] = vis
+            data['weight'] = weight
+            data['imaging_weight'] = imaging_weight
+        self.data = data
         self.frequency = numpy.asarray(frequency, dtype=numpy.float64)
         self.channel_bandwidth = numpy.asarray(channel_bandwidth, dtype=numpy.float64)
-        self.uvw = uvw
-        self.time = time
-        self.vis = vis
-        self.weight = numpy.ones(vis.shape) if weight is None else weight
         self.phasecentre = phasecentre
-        self.polarisation_frame = polarisation_frame
         self.configuration = configuration
+        self.polarisation_frame = polarisation_frame
+        self.source = source
+        self.meta = meta
 
     @property
     def nants(self):
-        return self.vis.shape[1]
+        return self.data['vis'].shape[1]
 
     @property
     def nchan(self):
-        return self.vis.shape[3]
+        return self.data['vis'].shape[3]
 
     @property
     def npol(self):
-        return self.vis.shape[4]
+        return self.data['vis'].shape[4]
+
+    @property
+    def uvw(self):
+        return self.data['uvw']
+
+    @property
+    def time(self):
+        return self.data['time']
+
+    @property
+    def integration_time(self):
+        return self.data['integration_time']
+
+    @property
+    def vis(self):
+        return self.data['vis']
+
+    @property
+    def weight(self):
+        return self.data['weight']
+
+    @property
+    def imaging_weight(self):
+        return self.data['imaging_weight']
+
+
+def copy_blockvisibility(bvis, zero=False):
+    """``copy_visibility`` for a BlockVisibility (``visibility/base.py``)."""
+    out = copy.copy(bvis)
+    out.data = bvis.data.copy()
+    if zero:
+        out.data['vis'][...] = 0.0
+    return out
 
 
 class Image:

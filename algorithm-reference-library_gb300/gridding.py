@@ -45,6 +45,13 @@ class DeviceVisibility:
         return 'fp64' if self.vis.dtype == torch.complex128 else 'fp32c'
 
     @classmethod
+    def from_blockvisibility(cls, bvis, precision=None):
+        """Rows formed on the device from an uploaded BlockVisibility
+        (``convert_blocks``, ``visibility/coalesce.py:331-443``)."""
+        from .coalesce import device_rows_from_blocks
+        return device_rows_from_blocks(bvis, precision)
+
+    @classmethod
     def from_visibility(cls, vis, precision=None, device=None):
         precision = dv.resolve_precision(precision)
         device = device or dv.require_cuda()

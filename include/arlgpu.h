@@ -208,6 +208,44 @@ int arlgpu_wstack_grid_to_image(const void *grid, const arlgpu_grid_desc *gd, in
 int arlgpu_wstack_image_to_grid(const double *image, const double *gcf, const double *wmean, double cellsize,
                                 const arlgpu_grid_desc *gd, int precision, void *grid, void *stream);
 
+/* ---- (f1) uniform weighting: grid_weight_to_griddata (gridding.py:161-183),
+ * griddata_reweight (gridding.py:213-230), as weight_visibility (imaging/weighting.py:19-40)
+ * calls them ----
+ * arlgpu_grid_weights: wgrid [nchan][npol][nw][ny][nx] float64 and sumwt [nchan][npol]
+ *   are zeroed, then each row's weight [nvis][npol] (float32 for FP32C, float64 for FP64)
+ *   is added to its nearest cell and to sumwt.  Rows whose cell, w-plane, cf plane or
+ *   channel is out of range are counted in *n_bad_dev (ARL asserts) and skipped.
+ * arlgpu_reweight: each row's weights are divided by its cells when every
+ *   polarisation's cell is non-zero (the reference's `real(cell).all() > 0`). */
+int arlgpu_grid_weights(const double *uvw, const double *frequency, const void *weight, int64_t nvis,
+                        int precision, const arlgpu_cf_desc *cd, double *wgrid, const arlgpu_grid_desc *gd,
+                        double *sumwt, int64_t *n_bad_dev, void *stream);
+int arlgpu_reweight(const double *uvw, const double *frequency, void *weight, int64_t nvis, int precision,
+                    const arlgpu_cf_desc *cd, const double *wgrid, const arlgpu_grid_desc *gd, void *stream);
+
+/* ---- (f2) BlockVisibility -> Visibility: convert_blocks (visibility/coalesce.py:331-443)
+ * and the copy-back of decoalesce_visibility (coalesce.py:112-143) ----
+ * arlgpu_convert_blocks: block arrays [ntimes][nant][nant][nchan][npol] (vis complex,
+ *   weights real, both of the precision; block_uvw [ntimes][nant][nant][3] float64 in
+ *   metres; frequency [nchan]) -> rows ordered (time, a2, a1, channel) over a2 > a1:
+ *   vis, uvw [nrows][3] in wavelengths (uvw * (f / c)), weight, imaging_weight,
+ *   row_frequency, antenna1, antenna2, time_index; nrows = ntimes nant (nant-1)/2 nchan.
+ *   cindex [ntimes][nant][nant][nchan] int64 (may be NULL): the row of each block cell,
+ *   0 for cells with i <= j.
+ * arlgpu_decoalesce: one column (elem_bytes 4, 8 or 16 per element) of rows
+ *   [nrows][npol] back into block [ntimes][nant][nant][nchan][npol] with the reference
+ *   loop's result (flat[i:i+npol] = row[cindex[i]] for every cell i, overlapping when
+ *   npol > 1; positions past ncell + npol - 2 keep their values).  Indices outside
+ *   [0, nrows) are counted in *n_bad_dev and skipped. */
+int arlgpu_convert_blocks(const void *block_vis, const double *block_uvw, const void *block_weight,
+                          const void *block_imaging_weight, const double *frequency, int32_t ntimes,
+                          int32_t nant, int32_t nchan, int32_t npol, int precision, void *vis, double *uvw,
+                          void *weight, void *imaging_weight, double *row_frequency, int32_t *antenna1,
+                          int32_t *antenna2, int32_t *time_index, int64_t *cindex, void *stream);
+int arlgpu_decoalesce(const void *rows, int64_t nrows, const int64_t *cindex, int32_t ntimes, int32_t nant,
+                      int32_t nchan, int32_t npol, int elem_bytes, void *block, int64_t *n_bad_dev,
+                      void *stream);
+
 /* ---- a7/a8: create_pswf_convolutionfunction (griddata/kernels.py:52-97), FP64 ----
  * cf_out: [O][O][S][S] complex128 (one plane; ARL broadcasts it over chan/pol);
  * gcf_out: [ny][nx] float64. */

@@ -253,6 +253,72 @@ def grid_weight(wt, maps, gshape):
     return grid, sumwt
 
 
+def reweight(wt, maps, wgrid):
+    """``griddata_reweight`` (``gridding.py:213-230``): each row's imaging weight
+    divided by the real part of its nearest cell of the weight grid, when every
+    polarisation's cell is non-zero (the reference tests ``real(cell).all() > 0``,
+    i.e. all non-zero).  Returns a new array."""
+    pu, pu_off, pv, pv_off, pwg, pwc, pfreq = maps
+    out = np.array(wt, dtype=np.float64, copy=True)
+    for r in range(out.shape[0]):
+        cell = np.real(wgrid[pfreq[r], :, pwg[r], pv[r], pu[r]])
+        if cell.all() > 0.0:
+            out[r] /= cell
+    return out
+
+
+def weight_uniform(wt, maps, gshape):
+    """``weight_visibility`` (``imaging/weighting.py:19-40``): grid the weights,
+    then reweight the rows."""
+    wgrid, _ = grid_weight(wt, maps, gshape)
+    return reweight(wt, maps, wgrid)
+
+
+# ---------------------------------------------------------------------------
+# a15: BlockVisibility <-> Visibility (visibility/coalesce.py:85-143,331-443)
+# ---------------------------------------------------------------------------
+def convert_blocks(vis, uvw, wts, imaging_wts, times, integration_time, frequency, channel_bandwidth):
+    """``convert_blocks`` (``coalesce.py:331-443``): rows ordered (time, a2, a1,
+    channel) over the baselines a2 > a1 of the [ntimes, nant, nant, nchan, npol]
+    block; uvw converted from metres to wavelengths as uvw * (f / c).  Returns
+    (vis, uvw, wts, imaging_wts, time, frequency, channel_bandwidth, a1, a2,
+    integration_time, cindex)."""
+    ntimes, nant, _, nchan, npol = vis.shape
+    a2, a1 = np.tril_indices(nant, -1)
+    order = np.lexsort((a1, a2))          # a2 ascending, then a1
+    a2, a1 = a2[order], a1[order]
+    nbl = a1.size
+    t = np.repeat(np.arange(ntimes), nbl * nchan)
+    b = np.tile(np.repeat(np.arange(nbl), nchan), ntimes)
+    c = np.tile(np.arange(nchan), ntimes * nbl)
+    ca1, ca2 = a1[b], a2[b]
+    cfreq = np.asarray(frequency)[c]
+    cuvw = uvw[t, ca2, ca1, :] * (cfreq / C_M_S)[:, None]
+    cvis = vis[t, ca2, ca1, c, :]
+    cwts = wts[t, ca2, ca1, c, :]
+    cimw = imaging_wts[t, ca2, ca1, c, :]
+    cindex = np.zeros(ntimes * nant * nant * nchan, dtype=np.int64)
+    cindex[((t * nant + ca2) * nant + ca1) * nchan + c] = np.arange(t.size)
+    return (cvis, cuvw, cwts, cimw, np.asarray(times)[t], cfreq, np.asarray(channel_bandwidth)[c], ca1, ca2,
+            np.asarray(integration_time)[t], cindex)
+
+
+def decoalesce(block, rows, cindex):
+    """The overwrite loop of ``decoalesce_visibility`` (``coalesce.py:128-137``)
+    for one column: for i over the block's cells, flat[i:i + npol] =
+    rows[cindex[i]].  The slices overlap when npol > 1, so the reference's
+    result is reproduced as written: position k holds element k - i of row
+    cindex[i] for the last i that wrote it, and positions past N + npol - 2
+    keep the block's values."""
+    out = np.array(block, copy=True)
+    flat = out.reshape(-1)
+    npol = block.shape[-1]
+    n = flat.size // npol
+    for i in range(n):
+        flat[i:i + npol] = rows[cindex[i]]
+    return out
+
+
 # ---------------------------------------------------------------------------
 # a6: centred FFTs (processing_library/fourier_transforms/fft_support.py:21-89)
 # ---------------------------------------------------------------------------

@@ -124,10 +124,15 @@ class _Mod(types.ModuleType):
     def __getattr__(self, name):
         if name.startswith('__'):
             raise AttributeError(name)
+        full = self.__name__ + '.' + name
+        if full in _SPECIAL:  # e.g. ``from astropy import constants``
+            return importlib.import_module(full)
         return _Inert
 
 
 _SPECIAL = {
+    # speed of light as astropy.constants.c.value (SI, exact)
+    'astropy.constants': {'c': types.SimpleNamespace(value=299792458.0)},
     'astropy.wcs': {'WCS': WCS, 'FITSFixedWarning': UserWarning},
     'astropy.wcs.utils': {'pixel_to_skycoord': pixel_to_skycoord},
     'astropy.coordinates': {'SkyCoord': SkyCoord},

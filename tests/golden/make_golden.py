@@ -186,11 +186,81 @@ def case_kernels(out):
                            wker=cfw.data[0, 0], bbox=numpy.array([[b[0], *b[1], *b[2]] for b in bb]))
 
 
+def case_weighting(out):
+    """grid_weight_to_griddata and weight_visibility (uniform weighting,
+    ``processing_components/griddata/gridding.py:161-230``,
+    ``processing_components/imaging/weighting.py:19-40``), 2 channels x 2 pols,
+    with half of the rows sharing a cell with another row."""
+    from processing_components.imaging.weighting import weight_visibility
+    rng = numpy.random.default_rng(4545)
+    N, cell, O, S = 64, 8e-3, 8, 8
+    freqs = numpy.array([1.0e8, 1.1e8])
+    im = make_image(N, cell, freqs, 1e7, 'stokesIQ')
+    du = abs(1.0 / (N * cell))
+    vis = make_vis(rng, 2000, 2, (N // 2 - 2) * du, 30.0, freqs, 'stokesIQ')
+    vis.data['uvw'][1000:] = vis.data['uvw'][:1000] + rng.uniform(-0.01, 0.01, (1000, 3)) * du
+    vis.data['frequency'][1000:] = vis.data['frequency'][:1000]
+    gcf, cf = kernels.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    wt_before = vis.imaging_weight.copy()
+    gd, sumwt = gridding.grid_weight_to_griddata(vis, create_griddata_from_image(im), cf)
+    wgrid = gd.data.copy()
+    vis2 = weight_visibility(vis, im, gcfcf=(gcf, cf))
+    numpy.savez_compressed(out, N=N, cell=cell, O=O, S=S, freqs=freqs, dfreq=1e7, uvw=vis.uvw,
+                           frequency=vis.frequency, wt_before=wt_before, wgrid=wgrid, sumwt=sumwt,
+                           wt_after=vis2.imaging_weight.copy())
+
+
+def case_blocks(out):
+    """convert_blockvisibility_to_visibility and its inverse
+    (``processing_components/visibility/coalesce.py:85-109,331-443,446-474``) on
+    seeded blocks, one and two polarisations."""
+    from data_models.memory_data_models import BlockVisibility
+    from processing_components.visibility.coalesce import convert_blockvisibility_to_visibility, \
+        convert_visibility_to_blockvisibility
+    rng = numpy.random.default_rng(4646)
+    res = {}
+    for npol, frame in ((1, 'stokesI'), (2, 'linearnp')):
+        ntimes, nant, nchan = 3, 5, 4
+        freqs = numpy.linspace(1.0e8, 1.3e8, nchan)
+        shape = (ntimes, nant, nant, nchan, npol)
+        uvw = rng.uniform(-500.0, 500.0, (ntimes, nant, nant, 3))
+        bvis = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        wt = rng.uniform(0.5, 2.0, shape)
+        iwt = rng.uniform(0.5, 2.0, shape)
+        times = numpy.arange(ntimes) * 30.0 + 4.5e9
+        bv = BlockVisibility(frequency=freqs, channel_bandwidth=numpy.full(nchan, 1e7),
+                             phasecentre=SkyCoord(0.0, -45.0), configuration=None, uvw=uvw, time=times,
+                             vis=bvis, weight=wt, integration_time=numpy.full(ntimes, 30.0),
+                             polarisation_frame=PolarisationFrame(frame), imaging_weight=iwt)
+        v = convert_blockvisibility_to_visibility(bv)
+        rows = dict(uvw=v.uvw.copy(), vis=v.vis.copy(), weight=v.weight.copy(),
+                    imaging_weight=v.imaging_weight.copy(), time=v.time.copy(), frequency=v.frequency.copy(),
+                    antenna1=numpy.asarray(v.antenna1).copy(), antenna2=numpy.asarray(v.antenna2).copy(),
+                    cindex=numpy.asarray(v.cindex).copy())
+        v.data['vis'] *= (2.0 + 1.0j)
+        v.data['weight'] *= 3.0
+        back = convert_visibility_to_blockvisibility(v)
+        for k, a in rows.items():
+            res['p%d_%s' % (npol, k)] = a
+        res['p%d_block_uvw' % npol] = uvw
+        res['p%d_block_vis' % npol] = bvis
+        res['p%d_block_weight' % npol] = wt
+        res['p%d_block_imaging_weight' % npol] = iwt
+        res['p%d_freqs' % npol] = freqs
+        res['p%d_times' % npol] = times
+        res['p%d_back_vis' % npol] = back.data['vis'].copy()
+        res['p%d_back_weight' % npol] = back.data['weight'].copy()
+        res['p%d_back_imaging_weight' % npol] = back.data['imaging_weight'].copy()
+    numpy.savez_compressed(out, **res)
+
+
 if __name__ == '__main__':
     case_2d_pswf(os.path.join(HERE, 'ref_2d_pswf.npz'))
     case_wproj_2chan_2pol(os.path.join(HERE, 'ref_wproj_2chan_2pol.npz'))
     case_wstack(os.path.join(HERE, 'ref_wstack.npz'))
     case_kernels(os.path.join(HERE, 'ref_kernels.npz'))
+    case_weighting(os.path.join(HERE, 'ref_weighting.npz'))
+    case_blocks(os.path.join(HERE, 'ref_blocks.npz'))
     for f in sorted(os.listdir(HERE)):
         if f.endswith('.npz'):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -1,6 +1,7 @@
 """The oracle against outputs of the reference's own code (tests/golden/*.npz,
 made by tests/golden/make_golden.py from the ARL sources)."""
 import numpy
+import pytest
 
 
 def _rel(a, b):
@@ -78,3 +79,34 @@ def test_kernels(oracle, golden):
     assert numpy.array_equal(cfw[0, 0], d['wker']) and numpy.array_equal(gcf[0, 0], d['gcf'])
     bb = oracle.bounding_box(cfw, 1e-3)
     assert numpy.array_equal(numpy.array([[b[0], *b[1], *b[2]] for b in bb]), d['bbox'])
+
+
+def test_uniform_weighting_matches_reference(oracle, golden):
+    """grid_weight_to_griddata and weight_visibility, run by the reference."""
+    d = golden('ref_weighting.npz')
+    img = oracle.image_geometry(int(d['N']), float(d['cell']), 2, 2, float(d['freqs'][0]), float(d['dfreq']))
+    gax = oracle.grid_axes(img)
+    cax = oracle.cf_axes(img, int(d['O']), int(d['S']))
+    maps = oracle.convolution_mapping(d['uvw'], d['frequency'], gax, cax)
+    wgrid, sumwt = oracle.grid_weight(d['wt_before'], maps, gax['shape'])
+    assert numpy.array_equal(wgrid, d['wgrid'])
+    assert numpy.array_equal(sumwt, d['sumwt'])
+    assert numpy.array_equal(oracle.weight_uniform(d['wt_before'], maps, gax['shape']), d['wt_after'])
+
+
+@pytest.mark.parametrize('npol', [1, 2])
+def test_block_conversion_matches_reference(oracle, golden, npol):
+    """convert_blockvisibility_to_visibility and convert_visibility_to_blockvisibility."""
+    d = golden('ref_blocks.npz')
+    g = {k[3:]: d[k] for k in d.files if k.startswith('p%d_' % npol)}
+    nt = g['times'].size
+    out = oracle.convert_blocks(g['block_vis'], g['block_uvw'], g['block_weight'], g['block_imaging_weight'],
+                                g['times'], numpy.full(nt, 30.0), g['freqs'], numpy.full(g['freqs'].size, 1e7))
+    names = ('vis', 'uvw', 'weight', 'imaging_weight', 'time', 'frequency', None, 'antenna1', 'antenna2', None,
+             'cindex')
+    for name, arr in zip(names, out):
+        if name is not None:
+            assert numpy.array_equal(arr, g[name]), name
+    for col, scale in (('vis', 2.0 + 1.0j), ('weight', 3.0), ('imaging_weight', 1.0)):
+        back = oracle.decoalesce(g['block_' + col], g[col] * scale, g['cindex'])
+        assert numpy.array_equal(back, g['back_' + col]), col
