@@ -41,7 +41,7 @@ def test_grid_weights_and_uniform_weighting_match_reference(arl, golden):
     im, gcfcf, vis = _weight_case(arl, d)
     gd, sumwt = arl.grid_weight_to_griddata(vis, arl.create_griddata_from_image(im), gcfcf[1])
     assert rel(gd.data, d['wgrid']) < 1e-15
-    assert rel(sumwt, d['sumwt']) < 1e-15
+    assert rel(sumwt, d['sumwt']) < 1e-12  # ~1000 FP64 terms summed in a different order
     out = arl.weight_visibility(vis, im, gcfcf=gcfcf)
     assert out is vis
     assert rel(vis.imaging_weight, d['wt_after']) < 1e-15
