@@ -70,7 +70,7 @@ def test_merge_weights(arl, golden):
     b = arl.grid_weight_to_griddata(vis, arl.create_griddata_from_image(im), gcfcf[1])
     m, sw = arl.griddata_merge_weights([a, b])
     assert numpy.allclose(m.data, 2 * d['wgrid'], rtol=1e-15, atol=0)
-    assert numpy.allclose(sw, 2 * d['sumwt'], rtol=1e-15, atol=0)
+    assert numpy.allclose(sw, 2 * d['sumwt'], rtol=1e-12, atol=0)
 
 
 def _block(arl, g, npol):
