@@ -31,6 +31,7 @@ from .weighting import (grid_weight_to_griddata, griddata_merge_weights, griddat
                         weight_visibility)
 from .coalesce import (convert_blockvisibility_to_visibility, convert_visibility_to_blockvisibility,  # noqa: F401
                        decoalesce_visibility)
-from .data_models import copy_blockvisibility  # noqa: F401
+from .data_models import Skycomponent, copy_blockvisibility  # noqa: F401
+from .skycomponents import predict_skycomponent_visibility  # noqa: F401
 
 __version__ = '0.1.0'

@@ -266,6 +266,29 @@ def copy_blockvisibility(bvis, zero=False):
     return out
 
 
+class Skycomponent:
+    """A point component (``memory_data_models.py`` Skycomponent): direction,
+    frequency [nchan], flux [nchan, npol], shape 'Point'."""
+
+    def __init__(self, direction=None, frequency=None, name=None, flux=None, shape='Point',
+                 polarisation_frame=PolarisationFrame('stokesI'), params=None):
+        self.direction = direction
+        self.frequency = numpy.asarray(frequency, dtype=numpy.float64)
+        self.name = name
+        self.flux = numpy.asarray(flux, dtype=numpy.float64)
+        self.shape = shape
+        self.polarisation_frame = polarisation_frame
+        self.params = params if params is not None else {}
+
+    @property
+    def nchan(self):
+        return self.flux.shape[0]
+
+    @property
+    def npol(self):
+        return self.flux.shape[1]
+
+
 class Image:
     """Image [nchan, npol, ny, nx] with its WCS (``memory_data_models.py:349-434``)."""
 

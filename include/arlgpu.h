@@ -246,6 +246,20 @@ int arlgpu_decoalesce(const void *rows, int64_t nrows, const int64_t *cindex, in
                       int32_t nchan, int32_t npol, int elem_bytes, void *block, int64_t *n_bad_dev,
                       void *stream);
 
+/* ---- (f3) DFT predict: predict_skycomponent_visibility (imaging/base.py:192-244) with
+ * simulate_point (util/coordinate_support.py:192-212) ----
+ * arlgpu_dft_predict: vis[r][p] += sum_k flux[k][row_chan[r]][p] exp(-2 pi i (u l + v m + w n))
+ *   for uvw [nvis][3] (wavelengths), lmn [ncomp][3] = (l, m, sqrt(1-l^2-m^2) - 1), flux
+ *   [ncomp][nchan][npol] float64, vis [nvis][npol] complex of the precision (updated in
+ *   place).  row_chan [nvis] int32 may be NULL when nchan == 1.  Phases in FP64.
+ * arlgpu_dft_adjoint: image[k][p] += Re sum_r conj(exp(-2 pi i uvw_r . lmn_k)) x[r][p], the
+ *   adjoint for one channel (no reference counterpart; the dense gradient reference). */
+int arlgpu_dft_predict(const double *uvw, const int32_t *row_chan, int64_t nvis, const double *lmn,
+                       const double *flux, int32_t ncomp, int32_t nchan, int32_t npol, int precision, void *vis,
+                       void *stream);
+int arlgpu_dft_adjoint(const double *uvw, int64_t nvis, const double *lmn, int32_t ncomp, int32_t npol,
+                       int precision, const void *x, double *image, void *stream);
+
 /* ---- a7/a8: create_pswf_convolutionfunction (griddata/kernels.py:52-97), FP64 ----
  * cf_out: [O][O][S][S] complex128 (one plane; ARL broadcasts it over chan/pol);
  * gcf_out: [ny][nx] float64. */
