@@ -1,0 +1,200 @@
+// Hogbom CLEAN on the GPU.
+//
+// Reference behaviour:
+//   hogbom, overlapIndices    processing_library/arrays/cleaners.py:12-69, :134-154
+//   deconvolve_cube('hogbom') processing_components/image/deconvolution.py:43-300
+//
+// Each minor-cycle iteration is two launches on one stream, with no host
+// round trip:
+//   k_hog_find  argmax of |res * window| (or |res|) over the image, first
+//               index on ties as numpy.argmax; the last block to finish
+//               (counted with an atomic, no waiting) reduces the per-block
+//               maxima, forms mval = res[peak] * gain / pmax and adds it to the
+//               component image;
+//   k_hog_sub   res[overlap] -= psf[overlap] * mval, and the stopping test
+//               |res[peak]| < 0.9 * threshold on the updated peak.
+// A set stop flag turns the remaining launches into no-ops; the host reads
+// the flag every kCheck iterations to stop launching.  All arithmetic is FP64
+// with each operation rounded on its own (no FMA contraction), in the
+// reference's order, so the result equals NumPy's bit for bit.
+#include "common.cuh"
+
+namespace arlgpu {
+
+void count_launch(unsigned n);
+
+struct HogState {
+  double mval;
+  long long peak;  // flat index of the peak, row-major [nx][ny]
+  int stop;
+  int iters;
+  unsigned int counter;
+};
+
+struct Best {
+  double v;
+  long long i;
+};
+
+__device__ __forceinline__ Best better(Best a, Best b) {
+  // larger value wins; on equal values the smaller index (numpy.argmax)
+  if (b.v > a.v || (b.v == a.v && b.i < a.i)) return b;
+  return a;
+}
+
+constexpr int kFindThreads = 256;
+
+__global__ void __launch_bounds__(kFindThreads)
+k_hog_find(const double *__restrict__ res, const double *__restrict__ window, long long n, double gain, double pmax,
+           double *__restrict__ comps, Best *__restrict__ partial, HogState *__restrict__ st) {
+  if (st->stop) return;
+  __shared__ Best s_best[kFindThreads / 32];
+  __shared__ bool s_last;
+  Best b{-1.0, 0x7fffffffffffffffll};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double a = window ? fabs(__dmul_rn(res[i], window[i])) : fabs(res[i]);
+    b = better(b, Best{a, i});
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    Best c;
+    c.v = __shfl_xor_sync(0xffffffffu, b.v, o);
+    c.i = __shfl_xor_sync(0xffffffffu, b.i, o);
+    b = better(b, c);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) s_best[warp] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Best t = s_best[0];
+    for (int k = 1; k < kFindThreads / 32; ++k) t = better(t, s_best[k]);
+    partial[blockIdx.x] = t;
+    __threadfence();
+    s_last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  // Last block: reduce the per-block maxima.
+  __threadfence();
+  Best t{-1.0, 0x7fffffffffffffffll};
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    Best q;  // other blocks' results: read past L1
+    q.v = __ldcg(&partial[k].v);
+    q.i = __ldcg(&partial[k].i);
+    t = better(t, q);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    Best c;
+    c.v = __shfl_xor_sync(0xffffffffu, t.v, o);
+    c.i = __shfl_xor_sync(0xffffffffu, t.i, o);
+    t = better(t, c);
+  }
+  if (lane == 0) s_best[warp] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Best f = s_best[0];
+    for (int k = 1; k < kFindThreads / 32; ++k) f = better(f, s_best[k]);
+    const double mval = __ddiv_rn(__dmul_rn(res[f.i], gain), pmax);
+    comps[f.i] = __dadd_rn(comps[f.i], mval);
+    st->mval = mval;
+    st->peak = f.i;
+    st->counter = 0;
+  }
+}
+
+// res[overlap] -= psf[overlap] * mval (overlapIndices of the reference), then
+// the stopping test on the updated peak.
+__global__ void k_hog_sub(double *__restrict__ res, int nx, int ny, const double *__restrict__ psf, int pnx, int pny,
+                          double stop_level, HogState *__restrict__ st) {
+  if (st->stop) return;
+  const long long peak = st->peak;
+  const int mx = (int)(peak / ny), my = (int)(peak - (long long)mx * ny);
+  const double mval = st->mval;
+  const int wx = pnx / 2, wy = pny / 2;
+  const int r0 = max(0, mx - wx), r1 = min(nx, mx + wx);
+  const int c0 = max(0, my - wy), c1 = min(my + wy, ny);
+  const int p0 = max(0, wx + (r0 - mx)), q0 = max(0, wy + (c0 - my));
+  const int p1 = min(pnx, wx + (r1 - mx)), q1 = min(wy + (c1 - my), pny);
+  // numpy slices of unequal length would raise; the extents agree for every
+  // peak inside the image, so the patch is (r1 - r0) x (c1 - c0)
+  const int h = min(r1 - r0, p1 - p0), w = min(c1 - c0, q1 - q0);
+  const long long total = (long long)h * w;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+       k += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(k / w), j = (int)(k - (long long)i * w);
+    const long long ri = (long long)(r0 + i) * ny + (c0 + j);
+    const double nv = __dsub_rn(res[ri], __dmul_rn(psf[(long long)(p0 + i) * pny + (q0 + j)], mval));
+    res[ri] = nv;
+    if (ri == peak) {
+      st->iters += 1;
+      if (fabs(nv) < stop_level) st->stop = 1;
+    }
+  }
+}
+
+static int nblk(long long n, int cap) {
+  long long b = (n + 255) / 256;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+}  // namespace arlgpu
+
+using namespace arlgpu;
+
+extern "C" int arlgpu_hogbom(const double *dirty, const double *psf, const double *window, int32_t nx, int32_t ny,
+                             int32_t psf_nx, int32_t psf_ny, double gain, double thresh, int32_t niter,
+                             double fracthresh, double dirty_absmax, double psf_max, double *comps, double *res,
+                             int32_t *iterations, void *stream) {
+  if (!dirty || !psf || !comps || !res || !iterations) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  if (nx < 1 || ny < 1 || psf_nx < 2 || psf_ny < 2) return fail(ARLGPU_ERR_INVALID, "bad image or psf shape");
+  if (!(gain > 0.0 && gain < 2.0)) return fail(ARLGPU_ERR_INVALID, "gain must be in (0, 2)");
+  if (niter < 1) return fail(ARLGPU_ERR_INVALID, "niter must be > 0");
+  if (!(psf_max > 0.0)) return fail(ARLGPU_ERR_INVALID, "psf maximum must be > 0");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long long n = (long long)nx * ny;
+  const int fblocks = nblk(n, 152 * 4);
+  const int sblocks = nblk((long long)psf_nx * psf_ny, 152 * 8);
+  HogState *state = nullptr;
+  Best *partial = nullptr;
+  ARL_CUDA(cudaMallocAsync(&state, sizeof(HogState), st));
+  int rc = ARLGPU_OK;
+  if (cudaMallocAsync(&partial, sizeof(Best) * fblocks, st) != cudaSuccess) {
+    cudaFreeAsync(state, st);
+    return fail(ARLGPU_ERR_CUDA, "cudaMallocAsync failed");
+  }
+  const double absthresh = fmax(thresh, fracthresh * dirty_absmax);
+  const double stop_level = 0.9 * absthresh;
+  constexpr int kCheck = 64;
+  int it = 0;
+  HogState hs{};
+  do {
+    if (cudaMemsetAsync(state, 0, sizeof(HogState), st) != cudaSuccess ||
+        cudaMemcpyAsync(res, dirty, sizeof(double) * n, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(comps, 0, sizeof(double) * n, st) != cudaSuccess) {
+      rc = fail(ARLGPU_ERR_CUDA, "hogbom set-up failed");
+      break;
+    }
+    while (it < niter) {
+      const int batch = niter - it < kCheck ? niter - it : kCheck;
+      for (int k = 0; k < batch; ++k) {
+        k_hog_find<<<fblocks, kFindThreads, 0, st>>>(res, window, n, gain, psf_max, comps, partial, state);
+        k_hog_sub<<<sblocks, 256, 0, st>>>(res, nx, ny, psf, psf_nx, psf_ny, stop_level, state);
+      }
+      count_launch(2 * batch);
+      it += batch;
+      if (cudaGetLastError() != cudaSuccess) {
+        rc = fail(ARLGPU_ERR_CUDA, "hogbom launch failed");
+        break;
+      }
+      if (cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess) {
+        rc = fail(ARLGPU_ERR_CUDA, "hogbom state read failed");
+        break;
+      }
+      if (hs.stop) break;
+    }
+  } while (false);
+  *iterations = hs.iters;
+  cudaFreeAsync(partial, st);
+  cudaFreeAsync(state, st);
+  return rc;
+}

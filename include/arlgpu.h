@@ -260,6 +260,19 @@ int arlgpu_dft_predict(const double *uvw, const int32_t *row_chan, int64_t nvis,
 int arlgpu_dft_adjoint(const double *uvw, int64_t nvis, const double *lmn, int32_t ncomp, int32_t npol,
                        int precision, const void *x, double *image, void *stream);
 
+/* ---- (f4) deconvolution: hogbom (processing_library/arrays/cleaners.py:12-69), as
+ * deconvolve_cube(algorithm='hogbom') (image/deconvolution.py:43-300) calls it ----
+ * One plane: dirty [nx][ny], psf [psf_nx][psf_ny], window [nx][ny] or NULL, all float64
+ * device arrays; comps and res [nx][ny] are written (res starts as a copy of dirty).
+ * dirty_absmax = max|dirty| and psf_max = max(psf) are the caller's (exact maxima).
+ * Stops after niter iterations or when |res[peak]| < 0.9 max(thresh, fracthresh *
+ * dirty_absmax); *iterations (host) receives the count.  FP64 in the reference's
+ * operation order: the result equals NumPy's bit for bit. */
+int arlgpu_hogbom(const double *dirty, const double *psf, const double *window, int32_t nx, int32_t ny,
+                  int32_t psf_nx, int32_t psf_ny, double gain, double thresh, int32_t niter, double fracthresh,
+                  double dirty_absmax, double psf_max, double *comps, double *res, int32_t *iterations,
+                  void *stream);
+
 /* ---- a7/a8: create_pswf_convolutionfunction (griddata/kernels.py:52-97), FP64 ----
  * cf_out: [O][O][S][S] complex128 (one plane; ARL broadcasts it over chan/pol);
  * gcf_out: [ny][nx] float64. */

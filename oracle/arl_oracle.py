@@ -320,6 +320,69 @@ def decoalesce(block, rows, cindex):
 
 
 # ---------------------------------------------------------------------------
+# (f4) deconvolution: Hogbom CLEAN (processing_library/arrays/cleaners.py:12-69,
+#      processing_components/image/deconvolution.py:43-300)
+# ---------------------------------------------------------------------------
+def overlap_indices(res, psf, peakx, peaky):
+    """``overlapIndices`` (``cleaners.py:134-154``)."""
+    nx, ny = res.shape[0], res.shape[1]
+    wx, wy = psf.shape[0] // 2, psf.shape[1] // 2
+    res_lo = (max(0, peakx - wx), max(0, peaky - wy))
+    res_hi = (min(nx, peakx + wx), min(peaky + wy, ny))
+    psf_lo = (max(0, wx + (res_lo[0] - peakx)), max(0, wy + (res_lo[1] - peaky)))
+    psf_hi = (min(psf.shape[0], wx + (res_hi[0] - peakx)), min(wy + (res_hi[1] - peaky), psf.shape[1]))
+    return (res_lo[0], res_hi[0], res_lo[1], res_hi[1]), (psf_lo[0], psf_hi[0], psf_lo[1], psf_hi[1])
+
+
+def hogbom(dirty, psf, window, gain, thresh, niter, fracthresh):
+    """``hogbom`` (``cleaners.py:12-69``): returns (components, residual)."""
+    absolutethresh = max(thresh, fracthresh * np.fabs(dirty).max())
+    comps = np.zeros(dirty.shape)
+    res = np.array(dirty)
+    pmax = psf.max()
+    for i in range(niter):
+        a = np.fabs(res * window) if window is not None else np.fabs(res)
+        mx, my = np.unravel_index(a.argmax(), dirty.shape)
+        mval = res[mx, my] * gain / pmax
+        comps[mx, my] += mval
+        a1o, a2o = overlap_indices(dirty, psf, mx, my)
+        res[a1o[0]:a1o[1], a1o[2]:a1o[3]] -= psf[a2o[0]:a2o[1], a2o[2]:a2o[3]] * mval
+        if np.abs(res[mx, my]) < 0.9 * absolutethresh:
+            break
+    return comps, res
+
+
+def deconvolve_hogbom(dirty, psf, niter=100, gain=0.7, threshold=0.0, fractional_threshold=0.1,
+                      window_shape=None, window_edge=16, psf_support=None):
+    """The 'hogbom' branch of ``deconvolve_cube`` (``deconvolution.py:43-300``)
+    on arrays [nchan, npol, ny, nx]: window shapes, PSF crop, per-plane CLEAN."""
+    ny, nx = dirty.shape[2], dirty.shape[3]
+    if window_shape == 'quarter':
+        qx, qy = nx // 4, ny // 4
+        window = np.zeros_like(dirty)
+        window[..., (qy + 1):3 * qy, (qx + 1):3 * qx] = 1.0
+    elif window_shape == 'no_edge':
+        window = np.zeros_like(dirty)
+        window[..., (window_edge + 1):(ny - window_edge), (window_edge + 1):(nx - window_edge)] = 1.0
+    else:
+        window = None
+    if psf_support is None:
+        psf_support = max(dirty.shape[2] // 2, dirty.shape[3] // 2)
+    if psf_support <= psf.shape[2] // 2 and psf_support <= psf.shape[3] // 2:
+        c = [psf.shape[2] // 2, psf.shape[3] // 2]
+        psf = psf[..., (c[0] - psf_support):(c[0] + psf_support), (c[1] - psf_support):(c[1] + psf_support)]
+    comp = np.zeros(dirty.shape)
+    resid = np.zeros(dirty.shape)
+    for ch in range(dirty.shape[0]):
+        for p in range(dirty.shape[1]):
+            if psf[ch, p].max():
+                comp[ch, p], resid[ch, p] = hogbom(dirty[ch, p], psf[ch, p],
+                                                   None if window is None else window[ch, p], gain, threshold,
+                                                   niter, fractional_threshold)
+    return comp, resid
+
+
+# ---------------------------------------------------------------------------
 # a6: centred FFTs (processing_library/fourier_transforms/fft_support.py:21-89)
 # ---------------------------------------------------------------------------
 def fft(a):

@@ -254,6 +254,40 @@ def case_blocks(out):
     numpy.savez_compressed(out, **res)
 
 
+def case_hogbom(out):
+    """Hogbom CLEAN (``processing_library/arrays/cleaners.py:12-69``) and
+    ``deconvolve_cube(algorithm='hogbom')`` (``processing_components/image/
+    deconvolution.py:43-300``) on a dirty image made from a sampled-uv PSF."""
+    from processing_library.arrays.cleaners import hogbom
+    from processing_components.image.deconvolution import deconvolve_cube
+    rng = numpy.random.default_rng(4747)
+    N = 128
+    # PSF: the transform of a random uv sampling (sidelobes like a real beam)
+    samp = numpy.zeros((N, N))
+    samp[rng.integers(N // 2 - 30, N // 2 + 30, 3000), rng.integers(N // 2 - 30, N // 2 + 30, 3000)] = 1.0
+    samp = samp + samp[::-1, ::-1]
+    psf = numpy.real(numpy.fft.fftshift(numpy.fft.ifft2(numpy.fft.ifftshift(samp))))
+    psf /= psf.max()
+    sky = numpy.zeros((N, N))
+    sky[rng.integers(N // 4, 3 * N // 4, 12), rng.integers(N // 4, 3 * N // 4, 12)] = rng.uniform(0.5, 4.0, 12)
+    dirty = numpy.real(numpy.fft.fftshift(numpy.fft.ifft2(numpy.fft.fft2(numpy.fft.ifftshift(sky)) *
+                                                          numpy.fft.fft2(numpy.fft.ifftshift(psf)))))
+    dirty += 0.01 * rng.normal(size=(N, N))
+    window = numpy.zeros((N, N))
+    window[N // 8:7 * N // 8, N // 8:7 * N // 8] = 1.0
+    c1, r1 = hogbom(dirty, psf, None, 0.1, 0.0, 400, 0.01)
+    c2, r2 = hogbom(dirty, psf, window, 0.7, 0.05, 300, 0.001)
+    im = make_image(N, 0.001, numpy.array([1e8, 1.1e8]), 1e7, 'stokesI')
+    d2 = numpy.stack([dirty, 0.5 * dirty])[:, None]
+    p2 = numpy.stack([psf, psf])[:, None]
+    dim = create_image_from_array(d2, im.wcs, im.polarisation_frame)
+    pim = create_image_from_array(p2.copy(), im.wcs, im.polarisation_frame)
+    comp, resid = deconvolve_cube(dim, pim, algorithm='hogbom', niter=200, gain=0.2, threshold=0.0,
+                                  fractional_threshold=0.05, window_shape='quarter', psf_support=40)
+    numpy.savez_compressed(out, dirty=dirty, psf=psf, window=window, c1=c1, r1=r1, c2=c2, r2=r2, d2=d2, p2=p2,
+                           cube_comp=comp.data, cube_resid=resid.data)
+
+
 if __name__ == '__main__':
     case_2d_pswf(os.path.join(HERE, 'ref_2d_pswf.npz'))
     case_wproj_2chan_2pol(os.path.join(HERE, 'ref_wproj_2chan_2pol.npz'))
@@ -261,6 +295,7 @@ if __name__ == '__main__':
     case_kernels(os.path.join(HERE, 'ref_kernels.npz'))
     case_weighting(os.path.join(HERE, 'ref_weighting.npz'))
     case_blocks(os.path.join(HERE, 'ref_blocks.npz'))
+    case_hogbom(os.path.join(HERE, 'ref_hogbom.npz'))
     for f in sorted(os.listdir(HERE)):
         if f.endswith('.npz'):
             print(f, os.path.getsize(os.path.join(HERE, f)))

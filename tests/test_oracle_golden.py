@@ -110,3 +110,15 @@ def test_block_conversion_matches_reference(oracle, golden, npol):
     for col, scale in (('vis', 2.0 + 1.0j), ('weight', 3.0), ('imaging_weight', 1.0)):
         back = oracle.decoalesce(g['block_' + col], g[col] * scale, g['cindex'])
         assert numpy.array_equal(back, g['back_' + col]), col
+
+
+def test_hogbom_matches_reference(oracle, golden):
+    """Hogbom CLEAN and deconvolve_cube(algorithm='hogbom'), run by the reference."""
+    d = golden('ref_hogbom.npz')
+    c1, r1 = oracle.hogbom(d['dirty'], d['psf'], None, 0.1, 0.0, 400, 0.01)
+    assert numpy.array_equal(c1, d['c1']) and numpy.array_equal(r1, d['r1'])
+    c2, r2 = oracle.hogbom(d['dirty'], d['psf'], d['window'], 0.7, 0.05, 300, 0.001)
+    assert numpy.array_equal(c2, d['c2']) and numpy.array_equal(r2, d['r2'])
+    comp, resid = oracle.deconvolve_hogbom(d['d2'], d['p2'].copy(), niter=200, gain=0.2, threshold=0.0,
+                                           fractional_threshold=0.05, window_shape='quarter', psf_support=40)
+    assert numpy.array_equal(comp, d['cube_comp']) and numpy.array_equal(resid, d['cube_resid'])
