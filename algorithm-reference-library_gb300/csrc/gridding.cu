@@ -52,6 +52,7 @@ static std::atomic<int> g_tune_grid_kernel{4};    // 0: atomics + TwoSum, 1: ban
 static std::atomic<int> g_tune_degrid_kernel{2};  // 0: warp per row, 1: batched rows, 2: lean
 static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automatic)
 static std::atomic<int> g_tune_chunk{512};        // sorted rows per gridder / degridder CTA
+static std::atomic<int> g_tune_persistent{1};     // lean / fixed-point kernels: one resident grid looping over chunks
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // K1: mapping + bin key + histogram.
@@ -946,9 +947,9 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   R *comp = sub + (size_t)2 * NPOL * SG2;
   unsigned char *tab = smraw + (size_t)2 * NPOL * SG2 * ACC::kWords * sizeof(R);
   const uint32_t nvalid = off[g.nbins];
-  const uint32_t c0 = blockIdx.x * chunk;
-  if (c0 >= nvalid) return;
-  const uint32_t c1 = min(c0 + chunk, nvalid);
+  // Chunks of sorted rows: chunk blockIdx.x, then every gridDim.x-th after it
+  // (one chunk per CTA, or a persistent grid of resident CTAs).
+  if ((uint64_t)blockIdx.x * chunk >= nvalid) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int S = g.S, O = g.O;
   const int ps = (int)g.cf_pol_stride;
@@ -959,8 +960,10 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   build_tap_table(tab, S);
   __shared__ int s_red[2][NW * 6];
   __shared__ uint32_t s_next[2];
-  uint32_t pos = c0;
   int parity = 0;
+  for (uint64_t cb = blockIdx.x; cb * chunk < nvalid; cb += gridDim.x) {
+  const uint32_t c0 = (uint32_t)(cb * chunk), c1 = min(c0 + chunk, nvalid);
+  uint32_t pos = c0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
     if (threadIdx.x == 0) s_next[parity] = pos + NW;  // published by the barrier in seg_box
@@ -1080,6 +1083,7 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
     }
     pos = sg.end;
   }
+  }
 }
 
 // K3 (fixed-point variant, FP32C only; grid_kernel 4 and 5).
@@ -1136,9 +1140,9 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   constexpr int kPlanes = RESID ? 4 * NPOL : 2 * NPOL;
   unsigned char *tab = smraw + (size_t)kPlanes * SG2 * 4;
   const uint32_t nvalid = off[g.nbins];
-  const uint32_t c0 = blockIdx.x * chunk;
-  if (c0 >= nvalid) return;
-  const uint32_t c1 = min(c0 + chunk, nvalid);
+  // Chunks of sorted rows: chunk blockIdx.x, then every gridDim.x-th after it
+  // (one chunk per CTA, or a persistent grid of resident CTAs).
+  if ((uint64_t)blockIdx.x * chunk >= nvalid) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int S = g.S, O = g.O;
   const int ps = (int)g.cf_pol_stride;
@@ -1147,8 +1151,10 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   build_tap_table(tab, S);
 
   __shared__ uint32_t s_next[2];
-  uint32_t pos = c0;
   int parity = 0;
+  for (uint64_t cb = blockIdx.x; cb * chunk < nvalid; cb += gridDim.x) {
+  const uint32_t c0 = (uint32_t)(cb * chunk), c1 = min(c0 + chunk, nvalid);
+  uint32_t pos = c0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
     if (threadIdx.x == 0) s_next[parity] = pos + NW;  // published by the barrier in seg_box
@@ -1305,6 +1311,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
     }
     pos = sg.end;
   }
+  }
 }
 
 // K4 (lean variant): warp per row, specialised on the polarisation count,
@@ -1321,16 +1328,11 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   CT *sub = reinterpret_cast<CT *>(smraw);
   unsigned char *tab = smraw + (size_t)NPOL * SG2 * sizeof(CT);
   const uint32_t nvalid = off[g.nbins];
-  const uint32_t c0 = blockIdx.x * chunk;
-  if (c0 >= (uint32_t)nvis) return;
+  // Chunks of sorted rows: chunk blockIdx.x, then every gridDim.x-th after it
+  // (one chunk per CTA, or a persistent grid of resident CTAs).
+  const uint64_t nchunks = ((uint64_t)nvis + chunk - 1) / chunk;
+  if (blockIdx.x >= nchunks) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (c0 + chunk > nvalid) {
-    const uint32_t b = max(c0, nvalid), e = min(c0 + chunk, (uint32_t)nvis);
-    for (uint32_t r = b + threadIdx.x; r < e; r += blockDim.x)
-      for (int p = 0; p < NPOL; ++p) vis_out[(size_t)sidx[r] * NPOL + p] = czero<CT>();
-    if (c0 >= nvalid) return;
-  }
-  const uint32_t c1 = min(c0 + chunk, nvalid);
   const int S = g.S, O = g.O;
   const int ps = (int)g.cf_pol_stride;
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
@@ -1338,8 +1340,17 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   __shared__ int s_red[2][NW * 6];
   __shared__ uint32_t s_next[2];
   build_tap_table(tab, S);  // ordered before first use by the barrier in seg_box
-  uint32_t pos = c0;
   int parity = 0;
+  for (uint64_t cb = blockIdx.x; cb < nchunks; cb += gridDim.x) {
+  const uint32_t c0 = (uint32_t)(cb * chunk);
+  if (c0 + chunk > nvalid) {  // rows the plan rejected: zero output
+    const uint32_t b = max(c0, nvalid), e = (uint32_t)min((uint64_t)c0 + chunk, (uint64_t)nvis);
+    for (uint32_t r = b + threadIdx.x; r < e; r += blockDim.x)
+      for (int p = 0; p < NPOL; ++p) vis_out[(size_t)sidx[r] * NPOL + p] = czero<CT>();
+    if (c0 >= nvalid) continue;
+  }
+  const uint32_t c1 = min(c0 + chunk, nvalid);
+  uint32_t pos = c0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
     if (threadIdx.x == 0) s_next[parity] = pos + NW;  // published by the barrier in seg_box
@@ -1454,6 +1465,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       }
     }
     pos = sg.end;
+  }
   }
 }
 
@@ -1632,6 +1644,24 @@ int plan_build(const double *uvw, const double *freq, int64_t nvis, const Geom &
 static constexpr int kWarps = 8;
 static inline uint32_t chunk_rows() { return (uint32_t)g_tune_chunk.load(); }
 
+// Grid of a chunk-looping kernel: one CTA per chunk, or (persistent) as many
+// CTAs as can be resident, each taking every gridDim.x-th chunk.  The
+// persistent grid builds each CTA's tap table and clears its subgrid once
+// instead of once per chunk.
+template <typename K>
+static unsigned chunk_grid(K kern, size_t smem, int64_t nvis, uint32_t chunk) {
+  const int64_t nchunks = (nvis + chunk - 1) / chunk;
+  if (nchunks <= 0) return 0;
+  if (g_tune_persistent.load()) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kWarps * 32, smem) == cudaSuccess && occ > 0) {
+      const int64_t resident = (int64_t)occ * num_sms();
+      return (unsigned)(nchunks < resident ? nchunks : resident);
+    }
+  }
+  return (unsigned)nchunks;
+}
+
 static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const void *vis, const void *wt,
                           const void *cf, void *grid, double *sumwt, bool resid, cudaStream_t st) {
   const size_t smem = (size_t)(resid ? 4 : 2) * g.npol * g.SG * g.SG * 4 + tap_table_bytes(g.S);
@@ -1646,7 +1676,7 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
                                                                     : k_grid_fx<4, kWarps, false>;
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t chunk = chunk_rows();
-  unsigned blocks = (unsigned)((nvis + chunk - 1) / chunk);
+  const unsigned blocks = chunk_grid(kern, smem, nvis, chunk);
   if (blocks == 0) return ARLGPU_OK;
   kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk, static_cast<const float2 *>(vis),
                                           static_cast<const float *>(wt), static_cast<const float2 *>(cf),
@@ -1687,7 +1717,8 @@ static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const voi
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t chunk = chunk_rows();
-  unsigned blocks = (unsigned)((nvis + chunk - 1) / chunk);
+  const bool loops = g_tune_grid_kernel.load() >= 2;  // the lean kernels loop over chunks
+  const unsigned blocks = loops ? chunk_grid(kern, smem, nvis, chunk) : (unsigned)((nvis + chunk - 1) / chunk);
   if (blocks == 0) return ARLGPU_OK;
   kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk,
                                           static_cast<const typename VisT<R>::C *>(vis),
@@ -1715,7 +1746,8 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "degridder needs %zu bytes of shared memory", smem);
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t chunk = chunk_rows();
-  unsigned blocks = (unsigned)((nvis + chunk - 1) / chunk);
+  const bool loops = g_tune_degrid_kernel.load() == 2;  // the lean kernel loops over chunks
+  const unsigned blocks = loops ? chunk_grid(kern, smem, nvis, chunk) : (unsigned)((nvis + chunk - 1) / chunk);
   if (blocks == 0) return ARLGPU_OK;
   kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk, nvis,
                                           static_cast<const typename Cplx<R>::T *>(cf),
@@ -1855,6 +1887,7 @@ extern "C" int arlgpu_set_tuning(const char *key, int value) {
   else if (k == "degrid_kernel" && value >= 0 && value <= 2) g_tune_degrid_kernel = value;
   else if (k == "subgrid" && (value == 0 || (value >= 16 && value <= 128))) g_tune_subgrid = value;
   else if (k == "chunk" && value >= 32 && value <= (1 << 20)) g_tune_chunk = value;
+  else if (k == "persistent" && (value == 0 || value == 1)) g_tune_persistent = value;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key or value: %s = %d", key, value);
   return ARLGPU_OK;
 }
@@ -1866,6 +1899,7 @@ extern "C" int arlgpu_get_tuning(const char *key, int *value) {
   else if (k == "degrid_kernel") *value = g_tune_degrid_kernel;
   else if (k == "subgrid") *value = g_tune_subgrid;
   else if (k == "chunk") *value = g_tune_chunk;
+  else if (k == "persistent") *value = g_tune_persistent;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key: %s", key);
   return ARLGPU_OK;
 }

@@ -29,7 +29,7 @@ def set_tuning(**kw):
 def get_tuning():
     lib = nat.load()
     out = {}
-    for k in ('grid_kernel', 'degrid_kernel', 'subgrid', 'chunk'):
+    for k in ('grid_kernel', 'degrid_kernel', 'subgrid', 'chunk', 'persistent'):
         v = ctypes.c_int()
         nat.check(lib.arlgpu_get_tuning(k.encode(), ctypes.byref(v)))
         out[k] = v.value
@@ -131,6 +131,15 @@ def autotune(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps=2, subgrids=SUBGR
         if total < best_ms:
             best_ms = total
             best = dict(grid_kernel=gk, degrid_kernel=dk, subgrid=sg, chunk=ch)
+    # persistent grid (resident CTAs looping over chunks) or one CTA per chunk
+    step_ms = {}
+    for pers in (1, 0):
+        set_tuning(persistent=pers, **best)
+        t = stage_times(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps)
+        results['best/persistent%d' % pers] = tuple(round(x, 4) for x in t)
+        step_ms[pers] = sum(t)
+    best['persistent'] = min(step_ms, key=step_ms.get)
+    best_ms = step_ms[best['persistent']]
     set_tuning(**best)
     best['ms_per_step'] = round(best_ms, 4)
     return best, results
