@@ -52,7 +52,7 @@ static std::atomic<int> g_tune_grid_kernel{4};    // 0: atomics + TwoSum, 1: ban
 static std::atomic<int> g_tune_degrid_kernel{2};  // 0: warp per row, 1: batched rows, 2: lean
 static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automatic)
 static std::atomic<int> g_tune_chunk{512};        // sorted rows per gridder / degridder CTA
-static std::atomic<int> g_tune_persistent{1};     // lean / fixed-point kernels: one resident grid looping over chunks
+static std::atomic<int> g_tune_persistent{0};     // lean / fixed-point kernels: 1 = one resident grid looping over chunks
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // K1: mapping + bin key + histogram.

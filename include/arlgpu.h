@@ -100,7 +100,8 @@ unsigned long long arlgpu_kernel_launches(void);
  *   "subgrid"       subgrid edge in cells (16..128), 0 = automatic (48, or 32 when 4 pols)
  *   "chunk"         sorted rows per gridder / degridder CTA (32..2^20, default 512)
  *   "persistent"    1 = the lean and fixed-point kernels run as one grid of resident CTAs,
- *                   each looping over every gridDim-th chunk (default); 0 = one CTA per chunk
+ *                   each looping over every gridDim-th chunk; 0 = one CTA per chunk, which the
+ *                   hardware schedules dynamically (default: measured faster on C2)
  * No reference counterpart (ARL has one Python loop per function). */
 int arlgpu_set_tuning(const char *key, int value);
 int arlgpu_get_tuning(const char *key, int *value);
