@@ -909,6 +909,10 @@ __device__ __forceinline__ void row_step(RowWalk &w) {
   }
 }
 
+// Compile-time integer / boolean arguments for the generic tap-group lambdas.
+template <int V> struct IntC { static constexpr int value = V; };
+template <bool V> struct BoolC { static constexpr bool value = V; };
+
 // Tap walk through a per-CTA byte table.  For an even support sz the taps of
 // a window are numbered t = 0 .. sz^2 - 1 in row-major order and lane l of a
 // warp takes taps l, l + 32, l + 64, ...; tab[tap_base(sz) + t] = t / sz is the
@@ -1242,22 +1246,25 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         continue;
       }
       const int wofs = (wv - sg.v0) * SG + (wu - sg.u0) + lane, dg = SG - sz;
-      // Four warp steps at a time, the last group masked per lane: all tap
-      // loads of a group are in flight before its first atomic.
-      for (int t = 0; t < n; t += 128) {
-        int j[4];
-        bool on[4];
-        float2 tp[NPOL][4];
+      // Groups of K warp steps: all tap loads of a group are in flight before
+      // its first atomic.  Full groups of four run unmasked; the last 1 to 4
+      // steps run as one group of exactly that many, masked per lane only in
+      // its partial last step.
+      auto group = [&](int t, auto kk, auto masked) {
+        constexpr int K = decltype(kk)::value;
+        int j[K];
+        bool on[K];
+        float2 tp[NPOL][K];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          on[u] = t + 32 * u + lane < n;
+        for (int u = 0; u < K; ++u) {
+          on[u] = !decltype(masked)::value || t + 32 * u + lane < n;
           j[u] = on[u] ? tj[t + 32 * u] : 0;
 #pragma unroll
           for (int p = 0; p < NPOL; ++p)
             tp[p][u] = on[u] ? kl[p * ps + t + 32 * u + j[u] * dk] : make_float2(0.f, 0.f);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < K; ++u) {
           if (!on[u]) break;
           const int so = wofs + t + 32 * u + j[u] * dg;
 #pragma unroll
@@ -1268,6 +1275,15 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
             fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
           }
         }
+      };
+      int t = 0;
+      for (; t + 128 <= n; t += 128) group(t, IntC<4>(), BoolC<false>());
+      switch ((n - t + 31) >> 5) {
+        case 1: group(t, IntC<1>(), BoolC<true>()); break;
+        case 2: group(t, IntC<2>(), BoolC<true>()); break;
+        case 3: group(t, IntC<3>(), BoolC<true>()); break;
+        case 4: group(t, IntC<4>(), BoolC<true>()); break;
+        default: break;
       }
     }
 #pragma unroll
@@ -1424,30 +1440,42 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       R ax[NPOL], ay[NPOL];
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = 0;
-      // Four warp steps at a time, the last group masked per lane: all loads
-      // of a group are in flight before the multiply-adds that use them.
-      for (int t = 0; t < n; t += 128) {
-        int j[4];
-        bool on[4];
+      // Groups of K warp steps: every load of a group is in flight before the
+      // multiply-adds that use it.  Full groups of four run unmasked; the
+      // last 1 to 4 steps run as one group of exactly that many steps, masked
+      // per lane only in its partial last step.
+      auto group = [&](int t, auto kk, auto masked) {
+        constexpr int K = decltype(kk)::value;
+        int j[K];
+        bool on[K];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          on[u] = t + 32 * u + lane < n;
+        for (int u = 0; u < K; ++u) {
+          on[u] = !decltype(masked)::value || t + 32 * u + lane < n;
           j[u] = on[u] ? tj[t + 32 * u] : 0;
         }
 #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
-          CT tp[4], gv[4];
+          CT tp[K], gv[K];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < K; ++u) {
             tp[u] = on[u] ? kl[p * ps + t + 32 * u + j[u] * dk] : czero<CT>();
             gv[u] = on[u] ? gl[p * pstride + t + 32 * u + j[u] * dg] : czero<CT>();
           }
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < K; ++u) {
             ax[p] += gv[u].x * tp[u].x - gv[u].y * tp[u].y;
             ay[p] += gv[u].x * tp[u].y + gv[u].y * tp[u].x;
           }
         }
+      };
+      int t = 0;
+      for (; t + 128 <= n; t += 128) group(t, IntC<4>(), BoolC<false>());
+      switch ((n - t + 31) >> 5) {
+        case 1: group(t, IntC<1>(), BoolC<true>()); break;
+        case 2: group(t, IntC<2>(), BoolC<true>()); break;
+        case 3: group(t, IntC<3>(), BoolC<true>()); break;
+        case 4: group(t, IntC<4>(), BoolC<true>()); break;
+        default: break;
       }
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) {
