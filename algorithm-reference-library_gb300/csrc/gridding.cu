@@ -1330,9 +1330,20 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   }
 }
 
-// K4 (lean variant): warp per row, specialised on the polarisation count,
-// 32-bit incremental offsets, two taps per iteration with independent sums.
-template <typename R, int NPOL, int NW>
+// Packed FP32 multiply-add: d = a * b + c on both halves of a float pair.
+__device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsigned long long b,
+                                                   unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// K4 (lean variant): warp per row, specialised on the polarisation count, tap
+// walk through the row table, groups of up to four steps in flight.
+// DUP (FP32 only, degrid_kernel 3): the staged subgrid holds each cell as
+// (re, re, im, im), so a tap is two packed multiply-adds,
+// (sum re t.re, sum re t.im) and (sum im t.re, sum im t.im), instead of four.
+template <typename R, int NPOL, int NW, bool DUP = false>
 __global__ void __launch_bounds__(NW * 32)
 k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
               const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
@@ -1341,8 +1352,10 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   using CT = typename Cplx<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int SG = g.SG, SG2 = SG * SG;
+  static_assert(!DUP || sizeof(R) == 4, "the packed variant is FP32 only");
   CT *sub = reinterpret_cast<CT *>(smraw);
-  unsigned char *tab = smraw + (size_t)NPOL * SG2 * sizeof(CT);
+  float4 *sub4 = reinterpret_cast<float4 *>(smraw);  // DUP layout
+  unsigned char *tab = smraw + (size_t)NPOL * SG2 * (DUP ? sizeof(float4) : sizeof(CT));
   const uint32_t nvalid = off[g.nbins];
   // Chunks of sorted rows: chunk blockIdx.x, then every gridDim.x-th after it
   // (one chunk per CTA, or a persistent grid of resident CTAs).
@@ -1385,9 +1398,13 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
           const int gx = sg.u0 + x;
           const bool in = gy >= 0 && gy < g.ny && gx >= 0 && gx < g.nx;
 #pragma unroll
-          for (int p = 0; p < NPOL; ++p)
-            sub[p * SG2 + y * SG + x] =
-                in ? gplane[(int64_t)p * g.nw * plane_elems + (int64_t)gy * g.nx + gx] : czero<CT>();
+          for (int p = 0; p < NPOL; ++p) {
+            const CT v = in ? gplane[(int64_t)p * g.nw * plane_elems + (int64_t)gy * g.nx + gx] : czero<CT>();
+            if (DUP)
+              sub4[p * SG2 + y * SG + x] = make_float4((float)v.x, (float)v.x, (float)v.y, (float)v.y);
+            else
+              sub[p * SG2 + y * SG + x] = v;
+          }
         }
       }
       __syncthreads();
@@ -1468,14 +1485,65 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
           }
         }
       };
+      // The packed variant: accumulators (sum re t.re, sum re t.im) and
+      // (sum im t.re, sum im t.im) per polarisation.
+      unsigned long long pa[NPOL], pb[NPOL];
+#pragma unroll
+      for (int p = 0; p < NPOL; ++p) pa[p] = pb[p] = 0ull;
+      const int wofs4 = (wv - sg.v0) * SG + (wu - sg.u0) + lane;
+      auto group2 = [&](int t, auto kk, auto masked) {
+        constexpr int K = decltype(kk)::value;
+        int j[K];
+        bool on[K];
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+          on[u] = !decltype(masked)::value || t + 32 * u + lane < n;
+          j[u] = on[u] ? tj[t + 32 * u] : 0;
+        }
+#pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          unsigned long long tp[K];
+          ulonglong2 gv[K];
+#pragma unroll
+          for (int u = 0; u < K; ++u) {
+            tp[u] = on[u] ? *reinterpret_cast<const unsigned long long *>(kl + p * ps + t + 32 * u + j[u] * dk)
+                          : 0ull;
+            gv[u] = on[u] ? *reinterpret_cast<const ulonglong2 *>(sub4 + p * SG2 + wofs4 + t + 32 * u + j[u] * dg)
+                          : make_ulonglong2(0ull, 0ull);
+          }
+#pragma unroll
+          for (int u = 0; u < K; ++u) {
+            pa[p] = ffma2(gv[u].x, tp[u], pa[p]);
+            pb[p] = ffma2(gv[u].y, tp[u], pb[p]);
+          }
+        }
+      };
       int t = 0;
-      for (; t + 128 <= n; t += 128) group(t, IntC<4>(), BoolC<false>());
-      switch ((n - t + 31) >> 5) {
-        case 1: group(t, IntC<1>(), BoolC<true>()); break;
-        case 2: group(t, IntC<2>(), BoolC<true>()); break;
-        case 3: group(t, IntC<3>(), BoolC<true>()); break;
-        case 4: group(t, IntC<4>(), BoolC<true>()); break;
-        default: break;
+      if (DUP && !direct) {
+        for (; t + 128 <= n; t += 128) group2(t, IntC<4>(), BoolC<false>());
+        switch ((n - t + 31) >> 5) {
+          case 1: group2(t, IntC<1>(), BoolC<true>()); break;
+          case 2: group2(t, IntC<2>(), BoolC<true>()); break;
+          case 3: group2(t, IntC<3>(), BoolC<true>()); break;
+          case 4: group2(t, IntC<4>(), BoolC<true>()); break;
+          default: break;
+        }
+#pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          const float2 a2 = *reinterpret_cast<const float2 *>(&pa[p]);
+          const float2 b2 = *reinterpret_cast<const float2 *>(&pb[p]);
+          ax[p] = (R)(a2.x - b2.y);
+          ay[p] = (R)(a2.y + b2.x);
+        }
+      } else {
+        for (; t + 128 <= n; t += 128) group(t, IntC<4>(), BoolC<false>());
+        switch ((n - t + 31) >> 5) {
+          case 1: group(t, IntC<1>(), BoolC<true>()); break;
+          case 2: group(t, IntC<2>(), BoolC<true>()); break;
+          case 3: group(t, IntC<3>(), BoolC<true>()); break;
+          case 4: group(t, IntC<4>(), BoolC<true>()); break;
+          default: break;
+        }
       }
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) {
@@ -1765,16 +1833,22 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
   auto kern = k_degrid<R, kWarps>;
   if (g_tune_degrid_kernel.load() == 1) {
     kern = k_degrid_batch<R, kWarps>;
-  } else if (g_tune_degrid_kernel.load() == 2) {
+  } else if (g_tune_degrid_kernel.load() == 2 || (g_tune_degrid_kernel.load() == 3 && sizeof(R) == 8)) {
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
     kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps> : g.npol == 2 ? k_degrid_lean<R, 2, kWarps>
                                                                     : k_degrid_lean<R, 4, kWarps>;
     smem += tap_table_bytes(g.S);
+  } else if (g_tune_degrid_kernel.load() == 3) {  // FP32: packed multiply-adds
+    if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
+    kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps, sizeof(R) == 4>
+                       : g.npol == 2 ? k_degrid_lean<R, 2, kWarps, sizeof(R) == 4>
+                                     : k_degrid_lean<R, 4, kWarps, sizeof(R) == 4>;
+    smem = (size_t)g.npol * g.SG * g.SG * 16 + tap_table_bytes(g.S);
   }
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "degridder needs %zu bytes of shared memory", smem);
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t chunk = chunk_rows();
-  const bool loops = g_tune_degrid_kernel.load() == 2;  // the lean kernel loops over chunks
+  const bool loops = g_tune_degrid_kernel.load() >= 2;  // the lean kernels loop over chunks
   const unsigned blocks = loops ? chunk_grid(kern, smem, nvis, chunk) : (unsigned)((nvis + chunk - 1) / chunk);
   if (blocks == 0) return ARLGPU_OK;
   kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk, nvis,
@@ -1912,7 +1986,7 @@ extern "C" int arlgpu_set_tuning(const char *key, int value) {
   if (!key) return fail(ARLGPU_ERR_INVALID, "null key");
   const std::string k(key);
   if (k == "grid_kernel" && value >= 0 && value <= 5) g_tune_grid_kernel = value;
-  else if (k == "degrid_kernel" && value >= 0 && value <= 2) g_tune_degrid_kernel = value;
+  else if (k == "degrid_kernel" && value >= 0 && value <= 3) g_tune_degrid_kernel = value;
   else if (k == "subgrid" && (value == 0 || (value >= 16 && value <= 128))) g_tune_subgrid = value;
   else if (k == "chunk" && value >= 32 && value <= (1 << 20)) g_tune_chunk = value;
   else if (k == "persistent" && (value == 0 || value == 1)) g_tune_persistent = value;

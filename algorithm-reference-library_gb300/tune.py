@@ -15,7 +15,7 @@ from . import _native as nat
 from . import device as dv
 
 GRID_KERNELS = (0, 1, 2, 4)  # shared atomics + TwoSum, band owner + Kahan, lean atomics, fixed point
-DEGRID_KERNELS = (0, 1, 2)   # warp per row, 32-row batches, lean warp per row
+DEGRID_KERNELS = (0, 1, 2, 3)  # warp per row, 32-row batches, lean warp per row, lean packed FMA
 SUBGRIDS = (32, 48, 64)
 CHUNKS = (512, 2048)
 
