@@ -49,7 +49,7 @@ static std::atomic<unsigned long long> g_launches{0};
 // Kernel-variant choices (set by the autotuner through arlgpu_set_tuning).
 static std::atomic<int> g_tune_grid_kernel{4};    // 0: atomics + TwoSum, 1: band owner, 2: lean, 3: uncompensated,
                                                   // 4: fixed point + residual, 5: fixed point
-static std::atomic<int> g_tune_degrid_kernel{2};  // 0: warp per row, 1: batched rows, 2: lean
+static std::atomic<int> g_tune_degrid_kernel{3};  // 0: warp per row, 1: batched rows, 2: lean, 3: lean packed FMA
 static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automatic)
 static std::atomic<int> g_tune_chunk{512};        // sorted rows per gridder / degridder CTA
 static std::atomic<int> g_tune_persistent{0};     // lean / fixed-point kernels: 1 = one resident grid looping over chunks

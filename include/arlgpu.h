@@ -96,9 +96,9 @@ unsigned long long arlgpu_kernel_launches(void);
  *                       tap_absmax; FP64 and an unknown bound use 2),
  *                   5 = as 4 without the residual plane (measurement only)
  *   "degrid_kernel" 0 = one warp per row, 1 = 32-row batches per warp,
- *                   2 = one warp per row, specialised on npol, groups of four steps (default),
+ *                   2 = one warp per row, specialised on npol, groups of four steps,
  *                   3 = as 2 with the staged cells duplicated (re, re, im, im) so each tap is
- *                       two packed FP32 multiply-adds (FP32C; FP64 uses 2)
+ *                       two packed FP32 multiply-adds (default; FP32C, FP64 uses 2)
  *   "subgrid"       subgrid edge in cells (16..128), 0 = automatic (48, or 32 when 4 pols)
  *   "chunk"         sorted rows per gridder / degridder CTA (32..2^20, default 512)
  *   "persistent"    1 = the lean and fixed-point kernels run as one grid of resident CTAs,
