@@ -33,6 +33,6 @@ from .coalesce import (convert_blockvisibility_to_visibility, convert_visibility
                        decoalesce_visibility)
 from .data_models import Skycomponent, copy_blockvisibility  # noqa: F401
 from .skycomponents import predict_skycomponent_visibility  # noqa: F401
-from .deconvolution import deconvolve_cube, hogbom  # noqa: F401
+from .deconvolution import deconvolve_cube, hogbom, msclean  # noqa: F401
 
 __version__ = '0.1.0'

@@ -65,6 +65,8 @@ SIGNATURES = {
     'arlgpu_dft_adjoint': (ctypes.c_int, [_vp, _i64, _vp, _i32, _i32, ctypes.c_int, _vp, _vp, _vp]),
     'arlgpu_hogbom': (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _f64, _f64, _i32, _f64, _f64, _f64,
                                      _vp, _vp, _P(_i32), _vp]),
+    'arlgpu_msclean': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _f64, _f64, _i32, _vp,
+                                      _P(_i32), _vp]),
     'arlgpu_wstack_fftbuf_bytes': (ctypes.c_int, [_P(GridDesc), _P(ctypes.c_size_t)]),
     'arlgpu_wstack_image_to_grid': (ctypes.c_int, [_vp, _vp, _vp, _f64, _P(GridDesc), ctypes.c_int, _vp, _vp]),
     'arlgpu_degrid': (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp, _P(CfDesc), _vp, _P(GridDesc), _vp, _vp,

@@ -131,6 +131,138 @@ __global__ void k_hog_sub(double *__restrict__ res, int nx, int ny, const double
   }
 }
 
+// ---------------------------------------------------------------------------
+// Multiscale CLEAN (processing_library/arrays/cleaners.py:165-280): the
+// minor-cycle loop over the scale stack.  The scale images, the twice-
+// convolved PSF stack and the coupling matrix come from the caller (the
+// reference forms them with NumPy FFTs).  Per iteration:
+//   k_ms_find  argmax over scales and pixels of |stack_s * window_s / c_ss|,
+//              ties to the lower scale, then the lower index (the reference
+//              scans scales in order and keeps a strictly larger value); the
+//              last block applies the stopping tests (|stack[peak]| below
+//              0.9 * threshold, or a zero component) and forms mval;
+//   k_ms_sub   stack_s[overlap] -= psf_ss[s, mscale][overlap] * gain * mval for
+//              every scale, comps[overlap] += pscale[mscale][overlap] * gain * mval.
+// ---------------------------------------------------------------------------
+struct MsState {
+  double mval;
+  long long peak;  // flat pixel index
+  int mscale;
+  int stop;
+  int iters;
+  unsigned int counter;
+};
+
+struct BestS {
+  double v;
+  long long key;  // scale * npix + pixel: lower key wins ties
+};
+
+__device__ __forceinline__ BestS better_s(BestS a, BestS b) {
+  if (b.v > a.v || (b.v == a.v && b.key < a.key)) return b;
+  return a;
+}
+
+__global__ void __launch_bounds__(kFindThreads)
+k_ms_find(const double *__restrict__ stack, const double *__restrict__ wstack, const double *__restrict__ coupling,
+          int ns, long long npix, double stop_level, BestS *__restrict__ partial, MsState *__restrict__ st) {
+  if (st->stop) return;
+  __shared__ BestS s_best[kFindThreads / 32];
+  __shared__ bool s_last;
+  BestS b{-1.0, 0x7fffffffffffffffll};
+  const long long total = (long long)ns * npix;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+       k += (long long)gridDim.x * blockDim.x) {
+    const int sc = (int)(k / npix);
+    const double c = coupling[sc * ns + sc];
+    const double v = wstack ? __dmul_rn(stack[k], wstack[k]) : stack[k];
+    b = better_s(b, BestS{fabs(__ddiv_rn(v, c)), k});
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    BestS c;
+    c.v = __shfl_xor_sync(0xffffffffu, b.v, o);
+    c.key = __shfl_xor_sync(0xffffffffu, b.key, o);
+    b = better_s(b, c);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) s_best[warp] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    BestS t = s_best[0];
+    for (int k = 1; k < kFindThreads / 32; ++k) t = better_s(t, s_best[k]);
+    partial[blockIdx.x] = t;
+    __threadfence();
+    s_last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  BestS t{-1.0, 0x7fffffffffffffffll};
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    BestS q;  // other blocks' results: read past L1
+    q.v = __ldcg(&partial[k].v);
+    q.key = __ldcg(&partial[k].key);
+    t = better_s(t, q);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    BestS c;
+    c.v = __shfl_xor_sync(0xffffffffu, t.v, o);
+    c.key = __shfl_xor_sync(0xffffffffu, t.key, o);
+    t = better_s(t, c);
+  }
+  if (lane == 0) s_best[warp] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    BestS f = s_best[0];
+    for (int k = 1; k < kFindThreads / 32; ++k) f = better_s(f, s_best[k]);
+    const int sc = (int)(f.key / npix);
+    const double r = stack[f.key];
+    const double mval = __ddiv_rn(r, coupling[sc * ns + sc]);
+    st->counter = 0;
+    st->iters += 1;
+    if (fabs(r) < stop_level || !(fabs(mval) > 0.0)) {
+      st->stop = 1;
+      return;
+    }
+    st->mval = mval;
+    st->mscale = sc;
+    st->peak = f.key - (long long)sc * npix;
+  }
+}
+
+__global__ void k_ms_sub(double *__restrict__ stack, double *__restrict__ comps, int ns, int nx, int ny,
+                         const double *__restrict__ psf_ss, const double *__restrict__ pscale, int pnx, int pny,
+                         double gain, MsState *__restrict__ st) {
+  if (st->stop) return;
+  const long long peak = st->peak;
+  const int mscale = st->mscale;
+  const int mx = (int)(peak / ny), my = (int)(peak - (long long)mx * ny);
+  const double mval = st->mval;
+  const int wx = pnx / 2, wy = pny / 2;
+  const int r0 = max(0, mx - wx), r1 = min(nx, mx + wx);
+  const int c0 = max(0, my - wy), c1 = min(my + wy, ny);
+  const int p0 = max(0, wx + (r0 - mx)), q0 = max(0, wy + (c0 - my));
+  const int p1 = min(pnx, wx + (r1 - mx)), q1 = min(wy + (c1 - my), pny);
+  const int h = min(r1 - r0, p1 - p0), w = min(c1 - c0, q1 - q0);
+  const long long patch = (long long)h * w, total = patch * (ns + 1);
+  const long long npix = (long long)nx * ny, ppix = (long long)pnx * pny;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+       k += (long long)gridDim.x * blockDim.x) {
+    const int slot = (int)(k / patch);
+    const long long e = k - (long long)slot * patch;
+    const int i = (int)(e / w), j = (int)(e - (long long)i * w);
+    const long long ri = (long long)(r0 + i) * ny + (c0 + j);
+    const long long pi = (long long)(p0 + i) * pny + (q0 + j);
+    if (slot < ns) {
+      const double d = __dmul_rn(__dmul_rn(psf_ss[((long long)slot * ns + mscale) * ppix + pi], gain), mval);
+      stack[slot * npix + ri] = __dsub_rn(stack[slot * npix + ri], d);
+    } else {
+      const double d = __dmul_rn(__dmul_rn(pscale[(long long)mscale * ppix + pi], gain), mval);
+      comps[ri] = __dadd_rn(comps[ri], d);
+    }
+  }
+}
+
 static int nblk(long long n, int cap) {
   long long b = (n + 255) / 256;
   return (int)(b < 1 ? 1 : (b > cap ? cap : b));
@@ -193,6 +325,60 @@ extern "C" int arlgpu_hogbom(const double *dirty, const double *psf, const doubl
       if (hs.stop) break;
     }
   } while (false);
+  *iterations = hs.iters;
+  cudaFreeAsync(partial, st);
+  cudaFreeAsync(state, st);
+  return rc;
+}
+
+extern "C" int arlgpu_msclean(double *stack, const double *psf_ss, const double *pscale, const double *windowstack,
+                              const double *coupling, int32_t nscales, int32_t nx, int32_t ny, int32_t psf_nx,
+                              int32_t psf_ny, double gain, double absthresh, int32_t niter, double *comps,
+                              int32_t *iterations, void *stream) {
+  if (!stack || !psf_ss || !pscale || !coupling || !comps || !iterations)
+    return fail(ARLGPU_ERR_INVALID, "null array argument");
+  if (nscales < 1 || nx < 1 || ny < 1 || psf_nx < 2 || psf_ny < 2) return fail(ARLGPU_ERR_INVALID, "bad shapes");
+  if (!(gain > 0.0 && gain < 2.0)) return fail(ARLGPU_ERR_INVALID, "gain must be in (0, 2)");
+  if (niter < 1) return fail(ARLGPU_ERR_INVALID, "niter must be > 0");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long long npix = (long long)nx * ny;
+  const int fblocks = nblk((long long)nscales * npix, 152 * 4);
+  const int sblocks = nblk((long long)psf_nx * psf_ny * (nscales + 1), 152 * 8);
+  MsState *state = nullptr;
+  BestS *partial = nullptr;
+  ARL_CUDA(cudaMallocAsync(&state, sizeof(MsState), st));
+  if (cudaMallocAsync(&partial, sizeof(BestS) * fblocks, st) != cudaSuccess) {
+    cudaFreeAsync(state, st);
+    return fail(ARLGPU_ERR_CUDA, "cudaMallocAsync failed");
+  }
+  const double stop_level = 0.9 * absthresh;
+  constexpr int kCheck = 64;
+  int rc = ARLGPU_OK;
+  MsState hs{};
+  if (cudaMemsetAsync(state, 0, sizeof(MsState), st) != cudaSuccess ||
+      cudaMemsetAsync(comps, 0, sizeof(double) * npix, st) != cudaSuccess) {
+    rc = fail(ARLGPU_ERR_CUDA, "msclean set-up failed");
+  }
+  for (int it = 0; rc == ARLGPU_OK && it < niter;) {
+    const int batch = niter - it < kCheck ? niter - it : kCheck;
+    for (int k = 0; k < batch; ++k) {
+      k_ms_find<<<fblocks, kFindThreads, 0, st>>>(stack, windowstack, coupling, nscales, npix, stop_level, partial,
+                                                  state);
+      k_ms_sub<<<sblocks, 256, 0, st>>>(stack, comps, nscales, nx, ny, psf_ss, pscale, psf_nx, psf_ny, gain, state);
+    }
+    count_launch(2 * batch);
+    it += batch;
+    if (cudaGetLastError() != cudaSuccess) {
+      rc = fail(ARLGPU_ERR_CUDA, "msclean launch failed");
+      break;
+    }
+    if (cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      rc = fail(ARLGPU_ERR_CUDA, "msclean state read failed");
+      break;
+    }
+    if (hs.stop) break;
+  }
   *iterations = hs.iters;
   cudaFreeAsync(partial, st);
   cudaFreeAsync(state, st);

@@ -1185,9 +1185,11 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       rscale = ldexpf(1.f, f);
       rinv = ldexpf(1.f, -f);
     }
-    double wsum[NPOL];
+    // Per-warp weight sums, kept by lane 0 as an FP32 value plus its TwoSum
+    // error (FP64 issue is scarce on GB300; the pair is exact to ~1e-14).
+    float wsum[NPOL], wcomp[NPOL];
 #pragma unroll
-    for (int p = 0; p < NPOL; ++p) wsum[p] = 0.0;
+    for (int p = 0; p < NPOL; ++p) wsum[p] = wcomp[p] = 0.f;
     // Rows after each warp's first come from a shared counter, one at a
     // time, which balances rows of different support across the warps; each
     // warp holds the next row's index and metadata while it computes the
@@ -1221,7 +1223,11 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         const float w = wt[(size_t)idx * NPOL + p];
         vw[p].x = v.x * w;
         vw[p].y = v.y * w;
-        if (lane == 0) wsum[p] += (double)w;
+        if (lane == 0) {
+          const float s2 = wsum[p] + w, bp = s2 - wsum[p];
+          wcomp[p] += (wsum[p] - (s2 - bp)) + (w - bp);
+          wsum[p] = s2;
+        }
       }
       const float2 *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
                          ((int64_t)(vf * O + uf) * S + toff) * S + toff;
@@ -1286,11 +1292,12 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         default: break;
       }
     }
+    if (lane == 0) {
 #pragma unroll
-    for (int p = 0; p < NPOL; ++p) {
-      double s = wsum[p];
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0 && s != 0.0) atomicAdd(&sumwt[sg.ch * NPOL + p], s);
+      for (int p = 0; p < NPOL; ++p) {
+        const double s = (double)wsum[p] + (double)wcomp[p];
+        if (s != 0.0) atomicAdd(&sumwt[sg.ch * NPOL + p], s);
+      }
     }
     if (!direct) {
       __syncthreads();

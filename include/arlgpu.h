@@ -278,6 +278,16 @@ int arlgpu_hogbom(const double *dirty, const double *psf, const double *window, 
                   double dirty_absmax, double psf_max, double *comps, double *res, int32_t *iterations,
                   void *stream);
 
+/* ---- (f4) msclean (processing_library/arrays/cleaners.py:165-280): the minor cycle ----
+ * stack [nscales][nx][ny] is the scale-convolved residual (updated in place), psf_ss
+ * [nscales][nscales][psf_nx][psf_ny] the twice-convolved PSF stack, pscale [nscales]
+ * [psf_nx][psf_ny] the PSF-sized scale images, windowstack [nscales][nx][ny] or NULL,
+ * coupling [nscales][nscales]; comps [nx][ny] is written.  The caller forms these as
+ * the reference does (NumPy FFTs) and applies the final pmax scaling. */
+int arlgpu_msclean(double *stack, const double *psf_ss, const double *pscale, const double *windowstack,
+                   const double *coupling, int32_t nscales, int32_t nx, int32_t ny, int32_t psf_nx, int32_t psf_ny,
+                   double gain, double absthresh, int32_t niter, double *comps, int32_t *iterations, void *stream);
+
 /* ---- a7/a8: create_pswf_convolutionfunction (griddata/kernels.py:52-97), FP64 ----
  * cf_out: [O][O][S][S] complex128 (one plane; ARL broadcasts it over chan/pol);
  * gcf_out: [ny][nx] float64. */

@@ -382,6 +382,96 @@ def deconvolve_hogbom(dirty, psf, niter=100, gain=0.7, threshold=0.0, fractional
     return comp, resid
 
 
+def _sph_scalar(vnu):
+    """``spheroidal_function`` (``cleaners.py:398-440``), one scalar."""
+    if 0.0 <= vnu < 0.75:
+        part, nuend = 0, 0.75
+    elif 0.75 <= vnu <= 1.0:
+        part, nuend = 1, 1.0
+    else:
+        return 0.0
+    top, bot = _SPH_P[part, 0], _SPH_Q[part, 0]
+    d = vnu ** 2 - nuend ** 2
+    for k in range(1, 5):
+        top += _SPH_P[part, k] * d ** k
+    for k in range(1, 3):
+        bot += _SPH_Q[part, k] * d ** k
+    v = top / bot if bot != 0.0 else 0.0
+    return v if v >= 0.0 else 0.0
+
+
+def scalestack(shape, scales):
+    """``create_scalestack`` (``cleaners.py:283-316``, norm=True)."""
+    basis = np.zeros(shape)
+    nx, ny = shape[1], shape[2]
+    xc, yc = int(np.ceil(float(nx) / 2.0)), int(np.ceil(float(ny) / 2.0))
+    for i in np.arange(len(scales)):
+        h = int(np.ceil(scales[i] / 2.0))
+        if scales[i] > 0.0:
+            rs2 = 1.0 / (float(scales[i]) / 2.0) ** 2
+            for y in range(yc - h - 1, yc + h + 1):
+                for x in range(xc - h - 1, xc + h + 1):
+                    r = np.sqrt(rs2 * (float(x - xc) ** 2 + float(y - yc) ** 2))
+                    basis[i, x, y] = _sph_scalar(r) * (1.0 - r ** 2)
+            basis[basis < 0.0] = 0.0
+            basis[i] /= np.sum(basis[i])
+        else:
+            basis[i, xc, yc] = 1.0
+    return basis
+
+
+def _ft(a):
+    return np.fft.fftshift(np.fft.fft2(np.fft.fftshift(a)))
+
+
+def _ift_real(a):
+    return np.real(np.fft.ifftshift(np.fft.ifft2(np.fft.ifftshift(a))))
+
+
+def msclean(dirty, psf, window, gain, thresh, niter, scales, fracthresh):
+    """``msclean`` (``cleaners.py:165-280``): returns (components, residual)."""
+    comps = np.zeros(dirty.shape)
+    pmax = psf.max()
+    lpsf, ldirty = psf / pmax, dirty / pmax
+    ns = len(scales)
+    ss = scalestack([ns, ldirty.shape[0], ldirty.shape[1]], scales)
+    pss = scalestack([ns, lpsf.shape[0], lpsf.shape[1]], scales)
+    xd = _ft(ldirty)
+    stack = np.stack([_ift_real(xd * np.conjugate(_ft(ss[i]))) for i in range(ns)])
+    xp = _ft(lpsf)
+    xs = [_ft(pss[i]) for i in range(ns)]
+    pp = np.zeros([ns, ns, lpsf.shape[0], lpsf.shape[1]])
+    for a in range(ns):
+        for b in range(ns):
+            pp[a, b] = _ift_real(xp * xs[b] * np.conjugate(xs[a]))
+    cm = np.array([[np.max(pp[a, b]) for b in range(ns)] for a in range(ns)])
+    if window is None:
+        ws = None
+    else:
+        xw = _ft(window)
+        ws = np.zeros_like(ss)
+        ws[np.stack([_ift_real(xw * np.conjugate(_ft(ss[i]))) for i in range(ns)]) > 0.9] = 1.0
+    athresh = max(thresh, fracthresh * np.fabs(stack[0]).max())
+    for _ in range(niter):
+        best, px, py, psc = 0.0, 0, 0, 0
+        for i in range(ns):
+            r = stack[i] * ws[i] / cm[i, i] if ws is not None else stack[i] / cm[i, i]
+            mx, my = np.unravel_index(np.abs(r).argmax(), r.shape)
+            if np.abs(r[mx, my]) > best:
+                best, px, py, psc = np.abs(r[mx, my]), mx, my, i
+        mval = stack[psc, px, py] / cm[psc, psc]
+        if np.fabs(stack[psc, px, py]) < 0.9 * athresh:
+            break
+        lhs, rhs = overlap_indices(dirty, psf, px, py)
+        if np.abs(mval) > 0:
+            for i in range(ns):
+                stack[i, lhs[0]:lhs[1], lhs[2]:lhs[3]] -= pp[i, psc, rhs[0]:rhs[1], rhs[2]:rhs[3]] * gain * mval
+            comps[lhs[0]:lhs[1], lhs[2]:lhs[3]] += pss[psc, rhs[0]:rhs[1], rhs[2]:rhs[3]] * gain * mval
+        else:
+            break
+    return comps, pmax * stack[0]
+
+
 # ---------------------------------------------------------------------------
 # a6: centred FFTs (processing_library/fourier_transforms/fft_support.py:21-89)
 # ---------------------------------------------------------------------------

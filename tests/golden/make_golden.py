@@ -288,6 +288,23 @@ def case_hogbom(out):
                            cube_comp=comp.data, cube_resid=resid.data)
 
 
+def case_msclean(out):
+    """Multiscale CLEAN (``processing_library/arrays/cleaners.py:165-280``) and
+    ``deconvolve_cube(algorithm='msclean')`` on the Hogbom case's dirty image."""
+    from processing_library.arrays.cleaners import msclean
+    from processing_components.image.deconvolution import deconvolve_cube
+    d = numpy.load(os.path.join(HERE, 'ref_hogbom.npz'))
+    dirty, psf, window = d['dirty'], d['psf'], d['window']
+    c1, r1 = msclean(dirty, psf, None, 0.3, 0.0, 150, [0, 3, 10], 0.01)
+    c2, r2 = msclean(dirty, psf[32:96, 32:96], window, 0.7, 0.02, 100, [0, 3], 0.001)
+    im = make_image(128, 0.001, numpy.array([1e8, 1.1e8]), 1e7, 'stokesI')
+    dim = create_image_from_array(d['d2'], im.wcs, im.polarisation_frame)
+    pim = create_image_from_array(d['p2'].copy(), im.wcs, im.polarisation_frame)
+    comp, resid = deconvolve_cube(dim, pim, algorithm='msclean', niter=60, gain=0.5, threshold=0.0,
+                                  fractional_threshold=0.05, scales=[0, 4, 8], psf_support=32)
+    numpy.savez_compressed(out, c1=c1, r1=r1, c2=c2, r2=r2, cube_comp=comp.data, cube_resid=resid.data)
+
+
 if __name__ == '__main__':
     case_2d_pswf(os.path.join(HERE, 'ref_2d_pswf.npz'))
     case_wproj_2chan_2pol(os.path.join(HERE, 'ref_wproj_2chan_2pol.npz'))
@@ -296,6 +313,7 @@ if __name__ == '__main__':
     case_weighting(os.path.join(HERE, 'ref_weighting.npz'))
     case_blocks(os.path.join(HERE, 'ref_blocks.npz'))
     case_hogbom(os.path.join(HERE, 'ref_hogbom.npz'))
+    case_msclean(os.path.join(HERE, 'ref_msclean.npz'))
     for f in sorted(os.listdir(HERE)):
         if f.endswith('.npz'):
             print(f, os.path.getsize(os.path.join(HERE, f)))

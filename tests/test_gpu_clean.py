@@ -52,3 +52,24 @@ def test_hogbom_larger_image_vs_oracle(arl, oracle):
     c, r = arl.hogbom(dirty, psf, None, 0.1, 0.0, 1500, 0.001)
     c0, r0 = oracle.hogbom(dirty, psf, None, 0.1, 0.0, 1500, 0.001)
     assert numpy.array_equal(c, c0) and numpy.array_equal(r, r0)
+
+
+def test_msclean_matches_reference(arl, golden):
+    h = golden('ref_hogbom.npz')
+    d = golden('ref_msclean.npz')
+    c1, r1 = arl.msclean(h['dirty'], h['psf'], None, 0.3, 0.0, 150, [0, 3, 10], 0.01)
+    assert numpy.array_equal(c1, d['c1']) and numpy.array_equal(r1, d['r1'])
+    c2, r2 = arl.msclean(h['dirty'], h['psf'][32:96, 32:96], h['window'], 0.7, 0.02, 100, [0, 3], 0.001)
+    assert numpy.array_equal(c2, d['c2']) and numpy.array_equal(r2, d['r2'])
+
+
+def test_deconvolve_cube_msclean_matches_reference(arl, golden):
+    h = golden('ref_hogbom.npz')
+    d = golden('ref_msclean.npz')
+    im = arl.create_image(npixel=128, cellsize=0.001, frequency=numpy.array([1e8, 1.1e8]),
+                          channel_bandwidth=numpy.array([1e7]))
+    dim = arl.create_image_from_array(h['d2'], im.wcs, im.polarisation_frame)
+    pim = arl.create_image_from_array(h['p2'].copy(), im.wcs, im.polarisation_frame)
+    comp, resid = arl.deconvolve_cube(dim, pim, algorithm='msclean', niter=60, gain=0.5, threshold=0.0,
+                                      fractional_threshold=0.05, scales=[0, 4, 8], psf_support=32)
+    assert numpy.array_equal(comp.data, d['cube_comp']) and numpy.array_equal(resid.data, d['cube_resid'])

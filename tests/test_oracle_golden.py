@@ -122,3 +122,13 @@ def test_hogbom_matches_reference(oracle, golden):
     comp, resid = oracle.deconvolve_hogbom(d['d2'], d['p2'].copy(), niter=200, gain=0.2, threshold=0.0,
                                            fractional_threshold=0.05, window_shape='quarter', psf_support=40)
     assert numpy.array_equal(comp, d['cube_comp']) and numpy.array_equal(resid, d['cube_resid'])
+
+
+def test_msclean_matches_reference(oracle, golden):
+    """Multiscale CLEAN, run by the reference."""
+    h = golden('ref_hogbom.npz')
+    d = golden('ref_msclean.npz')
+    c1, r1 = oracle.msclean(h['dirty'], h['psf'], None, 0.3, 0.0, 150, [0, 3, 10], 0.01)
+    assert numpy.array_equal(c1, d['c1']) and numpy.array_equal(r1, d['r1'])
+    c2, r2 = oracle.msclean(h['dirty'], h['psf'][32:96, 32:96], h['window'], 0.7, 0.02, 100, [0, 3], 0.001)
+    assert numpy.array_equal(c2, d['c2']) and numpy.array_equal(r2, d['r2'])
