@@ -54,13 +54,25 @@ def test_hogbom_larger_image_vs_oracle(arl, oracle):
     assert numpy.array_equal(c, c0) and numpy.array_equal(r, r0)
 
 
-def test_msclean_matches_reference(arl, golden):
+def _close(a, b, tol=1e-12):
+    return numpy.max(numpy.abs(a - b)) <= tol * numpy.max(numpy.abs(b))
+
+
+def test_msclean_matches_reference(arl, oracle, golden):
+    """Multiscale CLEAN.  Its set-up convolves with NumPy FFTs, whose last bits
+    depend on the host's SIMD code path (the fixtures come from an x86 host):
+    against the fixtures the check is 1e-12 relative; against the oracle run on
+    this host, whose set-up is the same NumPy code, it is bit for bit."""
     h = golden('ref_hogbom.npz')
     d = golden('ref_msclean.npz')
     c1, r1 = arl.msclean(h['dirty'], h['psf'], None, 0.3, 0.0, 150, [0, 3, 10], 0.01)
-    assert numpy.array_equal(c1, d['c1']) and numpy.array_equal(r1, d['r1'])
+    assert _close(c1, d['c1']) and _close(r1, d['r1'])
+    o1, q1 = oracle.msclean(h['dirty'], h['psf'], None, 0.3, 0.0, 150, [0, 3, 10], 0.01)
+    assert numpy.array_equal(c1, o1) and numpy.array_equal(r1, q1)
     c2, r2 = arl.msclean(h['dirty'], h['psf'][32:96, 32:96], h['window'], 0.7, 0.02, 100, [0, 3], 0.001)
-    assert numpy.array_equal(c2, d['c2']) and numpy.array_equal(r2, d['r2'])
+    assert _close(c2, d['c2']) and _close(r2, d['r2'])
+    o2, q2 = oracle.msclean(h['dirty'], h['psf'][32:96, 32:96], h['window'], 0.7, 0.02, 100, [0, 3], 0.001)
+    assert numpy.array_equal(c2, o2) and numpy.array_equal(r2, q2)
 
 
 def test_deconvolve_cube_msclean_matches_reference(arl, golden):
@@ -72,4 +84,4 @@ def test_deconvolve_cube_msclean_matches_reference(arl, golden):
     pim = arl.create_image_from_array(h['p2'].copy(), im.wcs, im.polarisation_frame)
     comp, resid = arl.deconvolve_cube(dim, pim, algorithm='msclean', niter=60, gain=0.5, threshold=0.0,
                                       fractional_threshold=0.05, scales=[0, 4, 8], psf_support=32)
-    assert numpy.array_equal(comp.data, d['cube_comp']) and numpy.array_equal(resid.data, d['cube_resid'])
+    assert _close(comp.data, d['cube_comp']) and _close(resid.data, d['cube_resid'])
