@@ -615,6 +615,72 @@ def arm_gb300(args, torch, world, rank, local):
     return line
 
 
+def arm_wstack(args, torch, world, rank, local):
+    """The w-stacking workloads (C3: 4 pols, 64 flagged channels, 20 slices,
+    4096^2; C5: 1e8 rows, 32 slices, 8192^2): vis/s of the batched w-stack
+    invert (plan + grid + FP64 FFTs + w-beam combine) and predict (w-beam +
+    FFTs + degrid) through WStackImager, and of the invert replayed as one
+    CUDA graph.  Inputs and grids exceed L2, so no flush is needed."""
+    arl = importlib.import_module('algorithm-reference-library_gb300')
+    sim = arl.simulation
+    device = torch.device('cuda', local)
+    w = sim.make_workload(args.workload, device=device)
+    n = w['uvw'].shape[0]
+    im = sim.workload_image(arl, w)
+    gcfcf = arl.create_pswf_convolutionfunction(im, oversampling=w['oversampling'], support=w['support'])
+    model = torch.zeros((1, w['npol'], w['npixel'], w['npixel']), dtype=torch.float64, device=device)
+    c = w['npixel'] // 2
+    model[..., c - 200:c + 200:37, c - 200:c + 200:41] = 1.0
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e = _events(torch, 2)
+        e[0].record(stream)
+        for _ in range(steps):
+            fn()
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]) / steps
+
+    res = {}
+    for prec in (('fp32c',) if args.no_fp64 else ('fp32c', 'fp64')):
+        dvis = arl.DeviceVisibility(torch.as_tensor(w['uvw'], device=device),
+                                    torch.as_tensor(w['frequency'], device=device),
+                                    w['vis'].to(arl.device.CDTYPE[prec]),
+                                    torch.ones((n, w['npol']), dtype=arl.device.RDTYPE[prec], device=device))
+        imager = arl.WStackImager(dvis, im, w['vis_slices'], gcfcf=gcfcf, precision=prec)
+        imager.set_model(model)
+        lib = arl._native.load()
+        l0 = lib.arlgpu_kernel_launches()
+        t_inv = timed(lambda: imager.invert(replan=True), args.steps, args.warmup)
+        t_pred = timed(lambda: imager.predict(replan=True), args.steps, args.warmup)
+        r = {'invert_ms': t_inv, 'predict_ms': t_pred, 'invert_vis_s': n / (t_inv / 1e3),
+             'predict_vis_s': n / (t_pred / 1e3), 'launches': int(lib.arlgpu_kernel_launches() - l0)}
+        if prec == 'fp32c':
+            imager.capture('invert')
+            r['invert_graph_ms'] = timed(lambda: imager.replay('invert'), args.steps, 2)
+        res[prec] = r
+        del imager, dvis
+        torch.cuda.empty_cache()
+    f = res['fp32c']
+    ms = f['invert_ms'] + f['predict_ms']
+    line = {'metric': 'vis/s w-stack invert + predict (%s)' % args.workload, 'value': n / (ms / 1e3),
+            'unit': 'vis/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded)',
+            'config': {'workload': args.workload, 'nvis': n, 'npol': w['npol'], 'npixel': w['npixel'],
+                       'vis_slices': w['vis_slices'], 'kernel': 'PSWF S=%d O=%d' % (w['support'], w['oversampling']),
+                       'l2': 'rows and grids exceed L2'},
+            'fp32c': f}
+    if 'fp64' in res:
+        line['fp64'] = res['fp64']
+        line['fp32c_speedup'] = (res['fp64']['invert_ms'] + res['fp64']['predict_ms']) / ms
+    return line
+
+
 def arm_reference(args, torch, world, rank):
     """The reference's CPU algorithm (the oracle's faithful per-row loops; the
     reference itself is Python needing astropy, absent on the box) on all host
@@ -686,6 +752,8 @@ def main():
     world, rank, local = dist_setup(torch)
     if args.impl == 'reference':
         line = arm_reference(args, torch, world, rank)
+    elif args.workload in ('C3', 'C5'):
+        line = arm_wstack(args, torch, world, rank, local)
     else:
         line = arm_gb300(args, torch, world, rank, local)
     if rank == 0 and line is not None:
