@@ -54,6 +54,9 @@ struct Geom {
   double Xlim_u, Xlim_v, tolX_u, tolX_v;
   // Nearest-plane axes (WW grid, WW cf, FREQ): |P| < Plim uses the fixed tolerance
   double Plim_w, tol_w, Plim_z, tol_z, Plim_f, tol_f;
+  // Fixed-point decisions (pow2O and every limit below 2^29): the tolerances
+  // above in units of 2^-20, plus one.
+  int32_t fixmap, tq_u, tq_v, tq_w, tq_z, tq_f;
   // binning
   int32_t T;       // tile edge (grid pixels)
   int32_t SG;      // staged subgrid edge = T + S
@@ -71,7 +74,9 @@ struct PlanBufs {
   RowMap *smap;
   uint32_t *hist;     // nbins + 1
   uint32_t *offsets;  // nbins + 2
+  double *wpart;      // per-plane partial w sums (plan_wpart_items entries)
 };
+uint32_t plan_wpart_items(const Geom &g);
 size_t plan_bytes(int64_t nvis, const Geom &g);
 int plan_carve(void *ws, size_t bytes, int64_t nvis, const Geom &g, PlanBufs *b);
 int plan_build(const double *uvw, const double *freq, int64_t nvis, const Geom &g, const PlanBufs &b,

@@ -1,0 +1,498 @@
+// Double-single inverse 2-D FFT for the FP32C path (K5 / K9 transforms).
+//
+// Reference behaviour:
+//   ifft (centred inverse transform)  processing_library/fourier_transforms/fft_support.py:41-89
+//   fft_griddata_to_image             processing_components/griddata/gridding.py:270-289
+//   w-stack slice sum                 processing_components/imaging/wstack_single.py:26-60 with
+//                                     workflows/serial/imaging/imaging_serial.py:186-197
+//
+// The grid correction multiplies transform rounding by up to max(gcf)/min(gcf)
+// (~6e4 at the edge of a PSWF-corrected field), so the inverse transform must
+// be much more accurate than FP32.  GB300 runs FP64 at 1/64 of its FP32 rate,
+// which makes cuFFT's FP64 transform of an 8192^2 plane compute-bound at
+// ~14 ms.  Here every complex value is a pair of double-single numbers
+// (float4: re.hi, re.lo, im.hi, im.lo; ~48-bit significands) and all
+// arithmetic runs on the FP32 pipes.
+//
+// Layout: a plane of ny x nx points, row-major.  Three passes per plane:
+//   rows   one CTA per 8192 points (8192 / nx rows): FP32 grid (w-planes
+//          summed, chk sign) -> row DFTs in shared memory -> DS buffer
+//   cols1  ny = N1 * N2: DFTs of length N1 over rows n2 + N2 n1 of 32 or 64
+//          adjacent columns, times exp(2 pi i n2 k1 / ny), in place
+//   cols2  DFTs of length N2 over rows N2 k1 + n2 -> row k1 + N1 k2, with the
+//          epilogue fused: image write (invert_2d) or the w-screen product
+//          summed over the slices of the group (w-stacking)
+// Each DFT is a Stockham radix-4 (one radix-2 pass for odd log2) sequence in
+// shared memory: the first pass reads global memory, the last writes the
+// epilogue, both coalesced.  Twiddles come from one DS table of
+// exp(2 pi i m / 16384) computed once per device in FP64.
+#include <atomic>
+
+#include "common.cuh"
+#include "dsmath.cuh"
+
+namespace arlgpu {
+
+void count_launch(unsigned n);
+
+constexpr int kLog2Tw = 14;
+constexpr int kTw = 1 << kLog2Tw;
+__device__ float4 g_tw[kTw];  // exp(+2 pi i m / 16384): (cos hi, cos lo, sin hi, sin lo)
+
+__global__ void k_tw_init() {
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < kTw; m += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi((double)m / (double)(kTw / 2), &s, &c);
+    const dsf cc = ds_from_double(c), ss = ds_from_double(s);
+    g_tw[m] = make_float4(cc.hi, cc.lo, ss.hi, ss.lo);
+  }
+}
+
+static std::atomic<unsigned> g_tw_ready{0};
+
+// The table is filled once per device on a stream that is not capturing
+// (synchronised so that every later stream sees it); under capture the fill
+// is recorded into the graph instead, every time, so a graph never relies on
+// a fill that did not run.
+static int ensure_twiddles(cudaStream_t st) {
+  int dev = 0;
+  ARL_CUDA(cudaGetDevice(&dev));
+  const unsigned bit = 1u << (dev & 31);
+  if (g_tw_ready.load() & bit) return ARLGPU_OK;
+  k_tw_init<<<16, 256, 0, st>>>();
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  ARL_CUDA(cudaStreamIsCapturing(st, &cs));
+  if (cs == cudaStreamCaptureStatusNone) {
+    ARL_CUDA(cudaStreamSynchronize(st));
+    g_tw_ready.fetch_or(bit);
+  }
+  return ARLGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Complex double-single arithmetic on float4 (re.hi, re.lo, im.hi, im.lo).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float4 c_add_nr(float4 a, float4 b) {  // unnormalised sum
+  const dsf r = two_sum(a.x, b.x), i = two_sum(a.z, b.z);
+  return make_float4(r.hi, __fadd_rn(r.lo, __fadd_rn(a.y, b.y)), i.hi, __fadd_rn(i.lo, __fadd_rn(a.w, b.w)));
+}
+__device__ __forceinline__ float4 c_neg(float4 a) { return make_float4(-a.x, -a.y, -a.z, -a.w); }
+__device__ __forceinline__ float4 c_norm(float4 a) {
+  const dsf r = quick_two_sum(a.x, a.y), i = quick_two_sum(a.z, a.w);
+  return make_float4(r.hi, r.lo, i.hi, i.lo);
+}
+// i * a
+__device__ __forceinline__ float4 c_muli(float4 a) { return make_float4(-a.z, -a.w, a.x, a.y); }
+
+// a * w (w a unit twiddle).
+__device__ __forceinline__ float4 c_mul(float4 a, float4 w) {
+  const dsf p1 = two_prod(a.x, w.x), p2 = two_prod(a.z, w.z);
+  const dsf s1 = two_sum(p1.hi, -p2.hi);
+  float e1 = __fadd_rn(s1.lo, __fsub_rn(p1.lo, p2.lo));
+  e1 = __fmaf_rn(a.x, w.y, e1);
+  e1 = __fmaf_rn(a.y, w.x, e1);
+  e1 = __fmaf_rn(-a.z, w.w, e1);
+  e1 = __fmaf_rn(-a.w, w.z, e1);
+  const dsf p3 = two_prod(a.x, w.z), p4 = two_prod(a.z, w.x);
+  const dsf s2 = two_sum(p3.hi, p4.hi);
+  float e2 = __fadd_rn(s2.lo, __fadd_rn(p3.lo, p4.lo));
+  e2 = __fmaf_rn(a.x, w.w, e2);
+  e2 = __fmaf_rn(a.y, w.z, e2);
+  e2 = __fmaf_rn(a.z, w.y, e2);
+  e2 = __fmaf_rn(a.w, w.x, e2);
+  const dsf r = quick_two_sum(s1.hi, e1), i = quick_two_sum(s2.hi, e2);
+  return make_float4(r.hi, r.lo, i.hi, i.lo);
+}
+
+// exp(+2 pi i m / 2^log2n) for 0 <= m < 2^log2n <= 16384
+__device__ __forceinline__ float4 twiddle(int m, int log2n) { return __ldg(&g_tw[m << (kLog2Tw - log2n)]); }
+
+// ---------------------------------------------------------------------------
+// In-place radix-2^2 decimation-in-frequency transform (inverse sign) of
+// S = 2^log2S sequences of L = 2^log2L points held in shared memory at
+// pos(n, q): natural order in, bit-reversed order out.  Each butterfly reads
+// and writes the same four slots, so a thread holds one butterfly at a time
+// and a pass needs one barrier.  Two radix-2 stages of spans h and h/2 fuse
+// into one butterfly on the points n0 + {0, h/2, h, 3h/2} of a block of 2h:
+//   a = x0 + x2, b = x0 - x2, c = x1 + x3, d = i (x1 - x3), w = exp(2 pi i j / 2h)
+//   y0 = a + c, y1 = (a - c) w^2, y2 = (b + d) w, y3 = (b - d) w^3
+// and an odd log2 L ends with one radix-2 stage of span 1.
+// ---------------------------------------------------------------------------
+template <int T, typename Pos>
+__device__ __forceinline__ void ds_dif_cta(float4 *sm, int log2L, int log2S, bool seqfast, Pos pos) {
+  const int S1 = (1 << log2S) - 1;
+  const int nb4 = 1 << (log2L - 2 + log2S);
+  int log2h = log2L - 1;
+  for (; log2h >= 1; log2h -= 2) {
+    const int lq = log2h - 1, J1 = (1 << lq) - 1;
+    const int lblk = log2L - log2h - 1;  // log2 of the blocks per sequence
+    for (int bb = threadIdx.x; bb < nb4; bb += T) {
+      int q, jp, blk;
+      if (seqfast) {
+        q = bb & S1;
+        const int rest = bb >> log2S;
+        jp = rest & J1;
+        blk = rest >> lq;
+      } else {
+        jp = bb & J1;
+        const int rest = bb >> lq;
+        blk = rest & ((1 << lblk) - 1);
+        q = rest >> lblk;
+      }
+      const int n0 = (blk << (log2h + 1)) + jp, hh = 1 << lq;
+      const int i0 = pos(n0, q), i1 = pos(n0 + hh, q), i2 = pos(n0 + 2 * hh, q), i3 = pos(n0 + 3 * hh, q);
+      const float4 x0 = sm[i0], x1 = sm[i1], x2 = sm[i2], x3 = sm[i3];
+      const float4 a = c_add_nr(x0, x2), b = c_add_nr(x0, c_neg(x2));
+      const float4 c = c_add_nr(x1, x3), d = c_muli(c_add_nr(x1, c_neg(x3)));
+      float4 y0 = c_norm(c_add_nr(a, c)), y1 = c_norm(c_add_nr(a, c_neg(c)));
+      float4 y2 = c_norm(c_add_nr(b, d)), y3 = c_norm(c_add_nr(b, c_neg(d)));
+      if (jp) {
+        const int lw = log2h + 1;
+        y2 = c_mul(y2, twiddle(jp, lw));
+        y1 = c_mul(y1, twiddle(2 * jp, lw));
+        y3 = c_mul(y3, twiddle(3 * jp, lw));
+      }
+      sm[i0] = y0;
+      sm[i1] = y1;
+      sm[i2] = y2;
+      sm[i3] = y3;
+    }
+    __syncthreads();
+  }
+  if (log2h == 0) {
+    const int nb2 = 1 << (log2L - 1 + log2S), lb = log2L - 1, B1 = (1 << lb) - 1;
+    for (int bb = threadIdx.x; bb < nb2; bb += T) {
+      const int q = seqfast ? (bb & S1) : (bb >> lb), i = seqfast ? (bb >> log2S) : (bb & B1);
+      const int i0 = pos(2 * i, q), i1 = pos(2 * i + 1, q);
+      const float4 x0 = sm[i0], x1 = sm[i1];
+      sm[i0] = c_norm(c_add_nr(x0, x1));
+      sm[i1] = c_norm(c_add_nr(x0, c_neg(x1)));
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ int brev(int k, int log2L) { return (int)(__brev((unsigned)k) >> (32 - log2L)); }
+
+// ---------------------------------------------------------------------------
+// Pass 1: row transforms.  Logical plane q of the input is the sum over
+// z < nsum of grid[q * qstride + z * plane]; rows of planes [q0, q0 + np) go to
+// buf[(q - q0) * plane + y * nx + x] with the chk sign applied on input.  The
+// shared-memory rows are padded by one slot per L/8 so that the bit-reversed
+// read of the epilogue is free of bank conflicts.
+// ---------------------------------------------------------------------------
+constexpr int kRowT = 1024, kRowPts = 8192, kRowSmem = (kRowPts + kRowPts / 8) * 16;
+constexpr int kColT = 512, kColPts = 4096, kColNPT = kColPts / kColT, kColSmem = kColPts * 16;
+
+__global__ void __launch_bounds__(kRowT, 1)
+k_dsfft_rows(const float2 *__restrict__ grid, int64_t qstride, int nsum, int64_t q0, int np, int log2ny, int log2nx,
+             float4 *__restrict__ buf) {
+  extern __shared__ float4 sm[];
+  const int ny = 1 << log2ny;
+  const int64_t plane = (int64_t)ny << log2nx;
+  const int log2S = 13 - log2nx;  // rows per CTA
+  const int64_t row0 = (int64_t)blockIdx.x << log2S;
+  const int64_t nrows = (int64_t)np << log2ny;
+  const int lpad = log2nx - 3;
+  auto pos = [&](int n, int q) {
+    const int i = (q << log2nx) + n;
+    return i + (i >> lpad);
+  };
+  for (int t = threadIdx.x; t < kRowPts; t += kRowT) {
+    const int q = t >> log2nx, x = t & ((1 << log2nx) - 1);
+    const int64_t R = row0 + q;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (R < nrows) {
+      const int64_t pl = R >> log2ny;
+      const int y = (int)(R & (ny - 1));
+      const float2 *src = grid + (q0 + pl) * qstride + ((int64_t)y << log2nx) + x;
+      float2 g = src[0];
+      dsf re = {g.x, 0.f}, im = {g.y, 0.f};
+      for (int z = 1; z < nsum; ++z) {
+        g = src[z * plane];
+        re = ds_add(re, {g.x, 0.f});
+        im = ds_add(im, {g.y, 0.f});
+      }
+      const float sg = ((x + y) & 1) ? -1.f : 1.f;
+      v = make_float4(sg * re.hi, sg * re.lo, sg * im.hi, sg * im.lo);
+    }
+    sm[pos(x, q)] = v;
+  }
+  __syncthreads();
+  ds_dif_cta<kRowT>(sm, log2nx, log2S, false, pos);
+  for (int t = threadIdx.x; t < kRowPts; t += kRowT) {
+    const int q = t >> log2nx, x = t & ((1 << log2nx) - 1);
+    const int64_t R = row0 + q;
+    if (R < nrows) buf[(R << log2nx) + x] = sm[pos(brev(x, log2nx), q)];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Column decomposition ny = N1 N2 (N1 <= N2 <= 128) and the CTA tiles.
+// ---------------------------------------------------------------------------
+struct ColGeom {
+  int log2N1, log2N2;
+  int log2G1, log2WC1;  // cols1: n2 values x columns per CTA
+  int log2G2, log2WC2;  // cols2: k1 values x columns per CTA
+};
+
+static bool col_geom(int log2ny, int log2nx, ColGeom *c) {
+  c->log2N1 = log2ny / 2;
+  c->log2N2 = log2ny - c->log2N1;
+  if (c->log2N2 > 7 || c->log2N1 < 2) return false;
+  const int lp = 12;  // log2 of the points per column CTA
+  c->log2G1 = std::min(7 - c->log2N1, c->log2N2);
+  c->log2WC1 = lp - c->log2N1 - c->log2G1;
+  c->log2G2 = std::min(7 - c->log2N2, c->log2N1);
+  c->log2WC2 = lp - c->log2N2 - c->log2G2;
+  return c->log2WC1 <= log2nx && c->log2WC2 <= log2nx && c->log2WC1 >= 5 && c->log2WC2 >= 5;
+}
+
+// Pass 2: length-N1 DFTs over rows n2 + N2 n1, twiddled, in place.
+__global__ void __launch_bounds__(kColT)
+k_dsfft_cols1(float4 *__restrict__ buf, int log2ny, int log2nx, ColGeom cg, int64_t ntile_pl) {
+  extern __shared__ float4 sm[];
+  const int64_t pl = blockIdx.x / ntile_pl;
+  const int64_t t0 = blockIdx.x - pl * ntile_pl;
+  const int ntx = 1 << (log2nx - cg.log2WC1);
+  const int n2_0 = (int)(t0 / ntx) << cg.log2G1, x0 = (int)(t0 % ntx) << cg.log2WC1;
+  float4 *p = buf + (pl << (log2ny + log2nx));
+  const int WC1 = (1 << cg.log2WC1) - 1, log2S = cg.log2G1 + cg.log2WC1;
+  auto addr = [&](int n1, int q) {
+    const int n2 = n2_0 + (q >> cg.log2WC1);
+    return ((int64_t)(n2 + (n1 << cg.log2N2)) << log2nx) + x0 + (q & WC1);
+  };
+  auto pos = [&](int n, int q) { return (n << log2S) + q; };
+  for (int t = threadIdx.x; t < kColPts; t += kColT) sm[t] = p[addr(t >> log2S, t & ((1 << log2S) - 1))];
+  __syncthreads();
+  ds_dif_cta<kColT>(sm, cg.log2N1, log2S, true, pos);
+  for (int t = threadIdx.x; t < kColPts; t += kColT) {
+    const int k1 = t >> log2S, q = t & ((1 << log2S) - 1);
+    const int n2 = n2_0 + (q >> cg.log2WC1);
+    const float4 v = sm[pos(brev(k1, cg.log2N1), q)];
+    p[addr(k1, q)] = (n2 && k1) ? c_mul(v, twiddle(n2 * k1, log2ny)) : v;
+  }
+}
+
+// Pass 3 for invert_2d: length-N2 DFTs over rows N2 k1 + n2 -> row k1 + N1 k2;
+// image = part(v * chk * s0) * gcf [/ sumwt].  Plane pl is image b = b0 + pl.
+__global__ void __launch_bounds__(kColT)
+k_dsfft_cols2_image(const float4 *__restrict__ buf, int log2ny, int log2nx, ColGeom cg, int64_t ntile_pl, int64_t b0,
+                    float s0, const double *__restrict__ gcf, const double *__restrict__ sumwt,
+                    double *__restrict__ im_re, double *__restrict__ im_im) {
+  extern __shared__ float4 sm[];
+  const int64_t pl = blockIdx.x / ntile_pl;
+  const int64_t t0 = blockIdx.x - pl * ntile_pl;
+  const int ntx = 1 << (log2nx - cg.log2WC2);
+  const int k1_0 = (int)(t0 / ntx) << cg.log2G2, x0 = (int)(t0 % ntx) << cg.log2WC2;
+  const float4 *p = buf + (pl << (log2ny + log2nx));
+  const int WC2 = (1 << cg.log2WC2) - 1, log2S = cg.log2G2 + cg.log2WC2, S1 = (1 << log2S) - 1;
+  const int64_t b = b0 + pl;
+  const int64_t obase = b << (log2ny + log2nx);
+  auto pos = [&](int n, int q) { return (n << log2S) + q; };
+  for (int t = threadIdx.x; t < kColPts; t += kColT) {
+    const int n2 = t >> log2S, q = t & S1;
+    const int k1 = k1_0 + (q >> cg.log2WC2);
+    sm[t] = p[((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2)];
+  }
+  __syncthreads();
+  ds_dif_cta<kColT>(sm, cg.log2N2, log2S, true, pos);
+  double inv = 1.0;
+  bool zero = false;
+  if (sumwt) {
+    const double w = sumwt[b];
+    zero = !(w > 0.0);
+    inv = zero ? 0.0 : 1.0 / w;
+  }
+  for (int t = threadIdx.x; t < kColPts; t += kColT) {
+    const int k2 = t >> log2S, q = t & S1;
+    const float4 v = sm[pos(brev(k2, cg.log2N2), q)];
+    const int k = k1_0 + (q >> cg.log2WC2) + (k2 << cg.log2N1), x = x0 + (q & WC2);
+    const int64_t o = obase + ((int64_t)k << log2nx) + x;
+    const double f = (double)((((x + k) & 1) ? -1.f : 1.f) * s0) * gcf[o];
+    double re = ds_to_double({v.x, v.y}) * f, im = ds_to_double({v.z, v.w}) * f;
+    if (sumwt) {
+      re = zero ? 0.0 : re * inv;
+      im = zero ? 0.0 : im * inv;
+    }
+    im_re[o] = re;
+    if (im_im) im_im[o] = im;
+  }
+}
+
+// Pass 3 for w-stacking: planes [p0, p1) of the flattened (image b, slice s)
+// order, buf holding them from p0.  Each CTA sums Re(wb_s v) over the slices
+// of its tile into double-single accumulators and adds them to the image's DS
+// slots (image memory viewed as float2; the group holding slice 0 of image b
+// writes them).
+__global__ void __launch_bounds__(kColT)
+k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, ColGeom cg, int64_t p0, int64_t p1,
+                     int K, double fov, const double *__restrict__ wmean, float2 *__restrict__ slots) {
+  extern __shared__ float4 sm[];
+  const int ntx = 1 << (log2nx - cg.log2WC2);
+  const int k1_0 = (int)(blockIdx.x / ntx) << cg.log2G2, x0 = (int)(blockIdx.x % ntx) << cg.log2WC2;
+  const int WC2 = (1 << cg.log2WC2) - 1, log2S = cg.log2G2 + cg.log2WC2, S1 = (1 << log2S) - 1;
+  const int n = 1 << log2nx;
+  const dsf fov2 = ds_from_double(fov * fov), nn = ds_from_i64((long long)n * n);
+  auto pos = [&](int k, int q) { return (k << log2S) + q; };
+  dsf acc[kColNPT];
+#pragma unroll
+  for (int m = 0; m < kColNPT; ++m) acc[m] = {0.f, 0.f};
+  for (int64_t pp = p0; pp < p1; ++pp) {
+    const int64_t b = pp / K;
+    const int s = (int)(pp - b * K);
+    const float4 *p = buf + ((pp - p0) << (log2ny + log2nx));
+    for (int t = threadIdx.x; t < kColPts; t += kColT) {
+      const int n2 = t >> log2S, q = t & S1;
+      const int k1 = k1_0 + (q >> cg.log2WC2);
+      sm[t] = p[((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2)];
+    }
+    __syncthreads();
+    ds_dif_cta<kColT>(sm, cg.log2N2, log2S, true, pos);
+    const dsf w = ds_from_double(wmean[s]);
+#pragma unroll
+    for (int m = 0; m < kColNPT; ++m) {
+      const int t = threadIdx.x + m * kColT;
+      const int k2 = t >> log2S, q = t & S1;
+      const float4 v = sm[pos(brev(k2, cg.log2N2), q)];
+      const int k = k1_0 + (q >> cg.log2WC2) + (k2 << cg.log2N1), x = x0 + (q & WC2);
+      const float2 wb = ds_wbeam(ds_wpix(k, x, n, fov2, nn), w);
+      // Re(wb v) = wb.re v.re - wb.im v.im
+      acc[m] = ds_add(acc[m], ds_sub(ds_mul_f({v.x, v.y}, wb.x), ds_mul_f({v.z, v.w}, wb.y)));
+    }
+    __syncthreads();  // shared memory is reloaded by the next plane
+    if (pp + 1 == p1 || (pp + 1) / K != b) {
+      const bool first = p0 <= b * K;
+      float2 *out = slots + (b << (log2ny + log2nx));
+#pragma unroll
+      for (int m = 0; m < kColNPT; ++m) {
+        const int t = threadIdx.x + m * kColT;
+        const int k2 = t >> log2S, q = t & S1;
+        const int k = k1_0 + (q >> cg.log2WC2) + (k2 << cg.log2N1), x = x0 + (q & WC2);
+        float2 *o = out + ((int64_t)k << log2nx) + x;
+        dsf v = acc[m];
+        if (!first) {
+          const float2 old = *o;
+          v = ds_add(v, {old.x, old.y});
+        }
+        *o = make_float2(v.hi, v.lo);
+        acc[m] = {0.f, 0.f};
+      }
+    }
+  }
+}
+
+// image[b, y, x] = DS slot * chk * s0 * gcf / sumwt[b] (0 where sumwt <= 0), in
+// place over the slots.
+__global__ void k_ds_wstack_finish(double *image, int64_t nb, int log2ny, int log2nx, float s0,
+                                   const double *__restrict__ gcf, const double *__restrict__ sumwt) {
+  const int64_t plane = (int64_t)1 << (log2ny + log2nx), tot = nb * plane;
+  const int nx1 = (1 << log2nx) - 1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i >> (log2ny + log2nx);
+    const int y = (int)((i >> log2nx) & ((1 << log2ny) - 1)), x = (int)(i & nx1);
+    const float2 sl = reinterpret_cast<const float2 *>(image)[i];
+    const double w = sumwt[b];
+    const double sg = (double)((((x + y) & 1) ? -1.f : 1.f) * s0);
+    image[i] = w > 0.0 ? ds_to_double({sl.x, sl.y}) * sg * gcf[i] / w : 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static int ilog2_exact(int n) {
+  if (n <= 0 || (n & (n - 1))) return -1;
+  int l = 0;
+  while ((1 << l) < n) ++l;
+  return l;
+}
+
+bool dsfft_supported(int ny, int nx) {
+  const int ly = ilog2_exact(ny), lx = ilog2_exact(nx);
+  if (ly < 6 || lx < 6 || lx > 13 || ly > 14) return false;
+  ColGeom cg;
+  return col_geom(ly, lx, &cg);
+}
+
+static int set_smem() {
+  static std::atomic<int> done{0};
+  if (done.load()) return ARLGPU_OK;
+  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kRowSmem));
+  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols1, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
+  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_image, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
+  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_wstack, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
+  done.store(1);
+  return ARLGPU_OK;
+}
+
+// Rows and first column pass of logical planes [q0, q0 + np) into buf.
+static int rows_cols1(const float2 *grid, int64_t qstride, int nsum, int64_t q0, int64_t np, int ly, int lx,
+                      const ColGeom &cg, float4 *buf, cudaStream_t st) {
+  const int64_t nrows = np << ly;
+  const int log2S = 13 - lx;
+  const int64_t rblocks = (nrows + ((int64_t)1 << log2S) - 1) >> log2S;
+  k_dsfft_rows<<<(unsigned)rblocks, kRowT, kRowSmem, st>>>(grid, qstride, nsum, q0, (int)np, ly, lx, buf);
+  ARL_LAUNCH_CHECK();
+  const int64_t ntile = ((int64_t)1 << (cg.log2N2 - cg.log2G1)) << (lx - cg.log2WC1);
+  k_dsfft_cols1<<<(unsigned)(np * ntile), kColT, kColSmem, st>>>(buf, ly, lx, cg, ntile);
+  ARL_LAUNCH_CHECK();
+  count_launch(2);
+  return ARLGPU_OK;
+}
+
+// invert_2d: grid [nb][nw][ny][nx] FP32 complex -> image (real part, and the
+// imaginary part when im_im is set); buf holds nb planes of float4.
+int dsfft_g2i_2d(const float2 *grid, int nb, int nw, int ny, int nx, const double *gcf, const double *sumwt,
+                 double *im_re, double *im_im, void *buf, cudaStream_t st) {
+  const int ly = ilog2_exact(ny), lx = ilog2_exact(nx);
+  ColGeom cg;
+  if (!dsfft_supported(ny, nx) || !col_geom(ly, lx, &cg)) return fail(ARLGPU_ERR_UNSUPPORTED, "dsfft size");
+  ARL_TRY(ensure_twiddles(st));
+  ARL_TRY(set_smem());
+  const int64_t plane = (int64_t)ny * nx;
+  float4 *b4 = static_cast<float4 *>(buf);
+  ARL_TRY(rows_cols1(grid, plane * nw, nw, 0, nb, ly, lx, cg, b4, st));
+  const int64_t ntile = ((int64_t)1 << (cg.log2N1 - cg.log2G2)) << (lx - cg.log2WC2);
+  const float s0 = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
+  k_dsfft_cols2_image<<<(unsigned)(nb * ntile), kColT, kColSmem, st>>>(b4, ly, lx, cg, ntile, 0, s0, gcf, sumwt,
+                                                                          im_re, im_im);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
+}
+
+// w-stacking: grid [nb][K][ny][nx] FP32 complex; planes go through buf
+// (room for G planes of float4) a group at a time; the image accumulates in
+// double-single slots and is finished in place.
+int dsfft_g2i_wstack(const float2 *grid, int nb, int K, int ny, int nx, double fov, const double *wmean,
+                     const double *gcf, const double *sumwt, double *image, void *buf, int64_t G, cudaStream_t st) {
+  const int ly = ilog2_exact(ny), lx = ilog2_exact(nx);
+  ColGeom cg;
+  if (!dsfft_supported(ny, nx) || !col_geom(ly, lx, &cg)) return fail(ARLGPU_ERR_UNSUPPORTED, "dsfft size");
+  if (G < 1) return fail(ARLGPU_ERR_INVALID, "empty FFT group");
+  ARL_TRY(ensure_twiddles(st));
+  ARL_TRY(set_smem());
+  const int64_t plane = (int64_t)ny * nx, nplanes = (int64_t)nb * K;
+  float4 *b4 = static_cast<float4 *>(buf);
+  const int64_t ntile = ((int64_t)1 << (cg.log2N1 - cg.log2G2)) << (lx - cg.log2WC2);
+  for (int64_t p0 = 0; p0 < nplanes; p0 += G) {
+    const int64_t np = std::min(G, nplanes - p0);
+    ARL_TRY(rows_cols1(grid, plane, 1, p0, np, ly, lx, cg, b4, st));
+    k_dsfft_cols2_wstack<<<(unsigned)ntile, kColT, kColSmem, st>>>(b4, ly, lx, cg, p0, p0 + np, K, fov, wmean,
+                                                                      reinterpret_cast<float2 *>(image));
+    ARL_LAUNCH_CHECK();
+    count_launch(1);
+  }
+  const float s0 = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
+  const int64_t tot = nb * plane;
+  const int blocks = (int)std::min<int64_t>((tot + 255) / 256, 152 * 32);
+  k_ds_wstack_finish<<<blocks, 256, 0, st>>>(image, nb, ly, lx, s0, gcf, sumwt);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
+}
+
+}  // namespace arlgpu

@@ -22,6 +22,10 @@
 namespace arlgpu {
 
 void count_launch(unsigned n);
+bool tune_dsfft();
+bool dsfft_supported(int ny, int nx);
+int dsfft_g2i_2d(const float2 *grid, int nb, int nw, int ny, int nx, const double *gcf, const double *sumwt,
+                 double *im_re, double *im_im, void *buf, cudaStream_t st);
 
 static int cufft_fail(cufftResult r, const char *what) {
   return fail(ARLGPU_ERR_CUFFT, "%s failed with cufftResult %d", what, (int)r);
@@ -159,14 +163,18 @@ int exec_c2c<double2>(cufftHandle h, double2 *data, int dir) {
   return r == CUFFT_SUCCESS ? ARLGPU_OK : cufft_fail(r, "cufftExecZ2Z");
 }
 
-// The inverse transform runs in FP64 for both precisions: the grid correction
-// multiplies the transform's rounding error by up to max(gcf) / min(gcf)
-// (~6e4 at the edge of a PSWF-corrected image), so an FP32 transform would
-// leave ~1e-3 relative errors in the image whatever the gridder's accuracy.
+// The inverse transform is never FP32: the grid correction multiplies the
+// transform's rounding error by up to max(gcf) / min(gcf) (~6e4 at the edge
+// of a PSWF-corrected image), so an FP32 transform would leave ~1e-3 relative
+// errors in the image whatever the gridder's accuracy.  FP64 path: cuFFT Z2Z.
+// FP32C path: the double-single transform (dsfft.cu) for power-of-two sizes
+// 64..8192, else cuFFT Z2Z.
 template <typename CT>
 static int g2i(const CT *grid, const arlgpu_grid_desc *gd, const double *gcf, const double *sumwt, double *re,
                double *im, double2 *buf, cudaStream_t st) {
   const int nb = gd->nchan * gd->npol, ny = gd->ny, nx = gd->nx;
+  if (sizeof(CT) == 8 && tune_dsfft() && dsfft_supported(ny, nx))
+    return dsfft_g2i_2d(reinterpret_cast<const float2 *>(grid), nb, gd->nw, ny, nx, gcf, sumwt, re, im, buf, st);
   const int64_t total = (int64_t)nb * ny * nx;
   cufftHandle h;
   ARL_TRY(get_plan(ny, nx, nb, (long long)ny * nx, CUFFT_Z2Z, &h));

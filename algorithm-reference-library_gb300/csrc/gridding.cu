@@ -53,7 +53,9 @@ static std::atomic<int> g_tune_degrid_kernel{3};  // 0: warp per row, 1: batched
 static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automatic)
 static std::atomic<int> g_tune_chunk{512};        // sorted rows per gridder / degridder CTA
 static std::atomic<int> g_tune_persistent{0};     // lean / fixed-point kernels: 1 = one resident grid looping over chunks
+static std::atomic<int> g_tune_dsfft{1};          // FP32C inverse transforms: 1 = double-single FFT, 0 = cuFFT FP64
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+bool tune_dsfft() { return g_tune_dsfft.load() != 0; }
 
 // K1: mapping + bin key + histogram.
 __global__ void k_map(const double *__restrict__ uvw, const double *__restrict__ freq, int64_t nvis,
@@ -151,28 +153,42 @@ __global__ void k_scatter(const uint32_t *__restrict__ keys, const RowMap *__res
 }
 
 // Mean w of the rows of each grid w-plane (over all channels), from a built
-// plan: block z sums uvw[sidx[r]].w over the sorted row ranges of every
-// (channel, plane z) bin run, in a fixed order.  Planes without rows get 0.
-__global__ void k_plane_mean_w(const double *__restrict__ uvw, const uint32_t *__restrict__ sidx,
-                               const uint32_t *__restrict__ off, Geom g, double *__restrict__ wmean) {
+// plan, in two deterministic steps.  The sorted rows of bin run (c, z) (all
+// uv-tiles of channel c, plane z) are split into P equal shares; block
+// (c, z, p) sums w over its share (fixed per-thread order, fixed tree), then
+// one thread per plane adds its shares in (c, p) order and divides by the
+// row count.  Planes without rows get 0.
+__global__ void k_plane_wsum(const double *__restrict__ uvw, const uint32_t *__restrict__ sidx,
+                             const uint32_t *__restrict__ off, Geom g, uint32_t P, double *__restrict__ part) {
   __shared__ double ssum[256];
-  const int z = blockIdx.x;
+  const uint32_t item = blockIdx.x, p = item % P, cz = item / P;
   const uint32_t tiles = (uint32_t)g.ntv * g.ntu;
+  const uint32_t r0 = off[cz * tiles], len = off[(cz + 1) * tiles] - r0;
+  const uint32_t a = r0 + (uint32_t)(((uint64_t)len * p) / P), b = r0 + (uint32_t)(((uint64_t)len * (p + 1)) / P);
   double sum = 0.0;
-  unsigned long long cnt = 0;
-  for (int c = 0; c < g.nchan; ++c) {
-    const uint32_t b0 = ((uint32_t)c * g.nw + z) * tiles;
-    const uint32_t r0 = off[b0], r1 = off[b0 + tiles];
-    for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) sum += uvw[3 * (size_t)sidx[r] + 2];
-    cnt += r1 - r0;
-  }
+  for (uint32_t r = a + threadIdx.x; r < b; r += blockDim.x) sum += uvw[3 * (size_t)sidx[r] + 2];
   ssum[threadIdx.x] = sum;
   __syncthreads();
   for (int d = blockDim.x / 2; d > 0; d >>= 1) {
     if (threadIdx.x < d) ssum[threadIdx.x] += ssum[threadIdx.x + d];
     __syncthreads();
   }
-  if (threadIdx.x == 0) wmean[z] = cnt ? ssum[0] / (double)cnt : 0.0;
+  if (threadIdx.x == 0) part[item] = ssum[0];
+}
+
+__global__ void k_plane_wmean(const double *__restrict__ part, const uint32_t *__restrict__ off, Geom g, uint32_t P,
+                              double *__restrict__ wmean) {
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  if (z >= g.nw) return;
+  const uint32_t tiles = (uint32_t)g.ntv * g.ntu;
+  double sum = 0.0;
+  uint64_t cnt = 0;
+  for (int c = 0; c < g.nchan; ++c) {
+    const uint32_t cz = (uint32_t)c * g.nw + z;
+    for (uint32_t p = 0; p < P; ++p) sum += part[cz * P + p];
+    cnt += off[(cz + 1) * tiles] - off[cz * tiles];
+  }
+  wmean[z] = cnt ? sum / (double)cnt : 0.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1659,6 +1675,18 @@ int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precisio
   g->tol_z = 1e-14 * (g->Plim_z + fabs(cd->z.crpix) + 2.0);
   g->Plim_f = (double)gd->nchan + 2.0;
   g->tol_f = 1e-14 * (g->Plim_f + fabs(gd->f.crpix) + 2.0);
+  {
+    auto tq = [](double tol) { return (int32_t)std::min(ceil(tol * 1048576.0) + 1.0, 1e9); };
+    g->tq_u = tq(g->tolX_u);
+    g->tq_v = tq(g->tolX_v);
+    g->tq_w = tq(g->tol_w);
+    g->tq_z = tq(g->tol_z);
+    g->tq_f = tq(g->tol_f);
+    const double lim = 536870912.0;  // 2^29
+    g->fixmap = g->pow2O && g->Xlim_u < lim && g->Xlim_v < lim && g->Plim_w < lim && g->Plim_z < lim &&
+                g->Plim_f < lim && g->tq_u < (1 << 18) && g->tq_v < (1 << 18) && g->tq_w < (1 << 18) &&
+                g->tq_z < (1 << 18) && g->tq_f < (1 << 18);
+  }
   // Subgrid edge: 64 cells when npol planes of it (with the FP32 compensation
   // words) fit in 64 KiB of shared memory, else 32.
   const size_t cell = precision == ARLGPU_FP64 ? 16 : 16;  // c128, or c64 sum + c64 comp
@@ -1684,10 +1712,19 @@ int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precisio
 
 static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Shares per (channel, plane) run for the plane-mean sums: about 4096 blocks
+// in all.
+static uint32_t wpart_shares(const Geom &g) {
+  const uint64_t runs = (uint64_t)g.nchan * g.nw;
+  return runs >= 4096 ? 1u : (uint32_t)(4096 / runs);
+}
+uint32_t plan_wpart_items(const Geom &g) { return (uint32_t)g.nchan * g.nw * wpart_shares(g); }
+
 size_t plan_bytes(int64_t nvis, const Geom &g) {
   size_t n = (size_t)nvis;
   return align_up(n * 4) + align_up(n * sizeof(RowMap)) + align_up(n * 4) + align_up(n * sizeof(RowMap)) +
-         align_up(((size_t)g.nbins + 1) * 4) + align_up(((size_t)g.nbins + 2) * 4);
+         align_up(((size_t)g.nbins + 1) * 4) + align_up(((size_t)g.nbins + 2) * 4) +
+         align_up((size_t)plan_wpart_items(g) * 8);
 }
 
 int plan_carve(void *ws, size_t bytes, int64_t nvis, const Geom &g, PlanBufs *b) {
@@ -1707,6 +1744,8 @@ int plan_carve(void *ws, size_t bytes, int64_t nvis, const Geom &g, PlanBufs *b)
   b->hist = reinterpret_cast<uint32_t *>(p);
   p += align_up(((size_t)g.nbins + 1) * 4);
   b->offsets = reinterpret_cast<uint32_t *>(p);
+  p += align_up(((size_t)g.nbins + 2) * 4);
+  b->wpart = reinterpret_cast<double *>(p);
   return ARLGPU_OK;
 }
 
@@ -1975,17 +2014,21 @@ extern "C" int arlgpu_degrid(const double *uvw, const double *frequency, int64_t
 }
 
 extern "C" int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const arlgpu_grid_desc *gd,
-                                        const arlgpu_cf_desc *cd, const void *workspace, size_t workspace_bytes,
+                                        const arlgpu_cf_desc *cd, void *workspace, size_t workspace_bytes,
                                         double *wmean, void *stream) {
   Geom g;
   ARL_TRY(make_geom(gd, cd, ARLGPU_FP32C, &g));
   ARL_TRY(check_rows(nvis));
   if (!wmean || (nvis > 0 && !uvw)) return fail(ARLGPU_ERR_INVALID, "null array argument");
   PlanBufs b;
-  ARL_TRY(plan_carve(const_cast<void *>(workspace), workspace_bytes, nvis, g, &b));
-  k_plane_mean_w<<<g.nw, 256, 0, static_cast<cudaStream_t>(stream)>>>(uvw, b.sidx, b.offsets, g, wmean);
+  ARL_TRY(plan_carve(workspace, workspace_bytes, nvis, g, &b));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const uint32_t P = wpart_shares(g);
+  k_plane_wsum<<<plan_wpart_items(g), 256, 0, st>>>(uvw, b.sidx, b.offsets, g, P, b.wpart);
   ARL_LAUNCH_CHECK();
-  count_launch(1);
+  k_plane_wmean<<<(g.nw + 127) / 128, 128, 0, st>>>(b.wpart, b.offsets, g, P, wmean);
+  ARL_LAUNCH_CHECK();
+  count_launch(2);
   return ARLGPU_OK;
 }
 
@@ -1997,6 +2040,7 @@ extern "C" int arlgpu_set_tuning(const char *key, int value) {
   else if (k == "subgrid" && (value == 0 || (value >= 16 && value <= 128))) g_tune_subgrid = value;
   else if (k == "chunk" && value >= 32 && value <= (1 << 20)) g_tune_chunk = value;
   else if (k == "persistent" && (value == 0 || value == 1)) g_tune_persistent = value;
+  else if (k == "dsfft" && (value == 0 || value == 1)) g_tune_dsfft = value;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key or value: %s = %d", key, value);
   return ARLGPU_OK;
 }
@@ -2009,6 +2053,7 @@ extern "C" int arlgpu_get_tuning(const char *key, int *value) {
   else if (k == "subgrid") *value = g_tune_subgrid;
   else if (k == "chunk") *value = g_tune_chunk;
   else if (k == "persistent") *value = g_tune_persistent;
+  else if (k == "dsfft") *value = g_tune_dsfft;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key: %s", key);
   return ARLGPU_OK;
 }

@@ -143,20 +143,76 @@ __device__ __forceinline__ RawMap map_raw(double u, double v, double w, double f
   return r;
 }
 
+// Fixed-point view of a double |X| < 2^30 with 20 fraction bits: X + 1.5 2^32
+// lies in [2^32, 2^33) where the ulp is 2^-20, so its bit pattern minus that
+// of 1.5 2^32 is X * 2^20 rounded to an integer.  One FP64 add replaces a
+// floor, a subtraction, two comparisons and a conversion.
+__device__ __forceinline__ long long fix20(double X) {
+  return __double_as_longlong(__dadd_rn(X, 6442450944.0)) - 0x41F8000000000000LL;
+}
+
+// Pixel and sub-pixel index of one axis from X = P * O (power-of-two O), as
+// map_axis_x, with the integer-boundary test in fixed point: the fraction of
+// X rounded to 2^-20 lies at least tq units from an integer, so X and NumPy's
+// value (within tol of X) have the same floor.
+__device__ __forceinline__ bool fix_axis_x(double x, double rO, double cO, double Xlim, int tq, int O, int log2O,
+                                           int *pix, int *sub) {
+  const double X = fma(x, rO, cO);
+  if (!(fabs(X) < Xlim)) return false;
+  const long long F = fix20(X);
+  const int fr = (int)(F & 0xFFFFF);
+  if (fr < tq || fr > (1 << 20) - tq) return false;
+  const int a = (int)(F >> 20) + (O >> 1);
+  *pix = a >> log2O;
+  *sub = a - (*pix << log2O);
+  return true;
+}
+
+// Nearest-plane index as round_w2p_tol, with the half-integer test in fixed
+// point (F = (P + 1/2) 2^20: the index is F >> 20 when F's fraction is at
+// least tq units from an integer).
+__device__ __forceinline__ bool fix_round(double x, const arlgpu_axis &a, double rcp, double Plim, int tq, int *idx) {
+  const double p = fma(__dsub_rn(x, a.crval), rcp, a.crpix - 1.0);
+  if (!(fabs(p) < Plim)) return false;
+  const long long F = fix20(p) + (1LL << 19);
+  const int fr = (int)(F & 0xFFFFF);
+  if (fr < tq || fr > (1 << 20) - tq) return false;
+  *idx = (int)(F >> 20);
+  return true;
+}
+
 __device__ __forceinline__ Mapped map_row(double u, double v, double w, double f, const Geom &g) {
   Mapped m;
-  const RawMap r = map_raw(u, v, w, f, g);
-  // Range checks in double so huge values cannot wrap when narrowed.
-  bool ok = r.pu >= 0.0 && r.pu < g.nx && r.pv >= 0.0 && r.pv < g.ny && r.uf >= 0.0 && r.uf < g.O &&
-            r.vf >= 0.0 && r.vf < g.O && r.zg >= 0.0 && r.zg < g.nw && r.zc >= 0.0 && r.zc < g.nz &&
-            r.ch >= 0.0 && r.ch < g.nchan && r.ch < g.cf_nchan;
-  m.pu = ok ? (int32_t)r.pu : -1;
-  m.pv = ok ? (int32_t)r.pv : -1;
-  m.uf = ok ? (int32_t)r.uf : 0;
-  m.vf = ok ? (int32_t)r.vf : 0;
-  m.zg = ok ? (int32_t)r.zg : 0;
-  m.zc = ok ? (int32_t)r.zc : 0;
-  m.ch = ok ? (int32_t)r.ch : 0;
+  bool ok;
+  int pu, pv, uf, vf, zg, zc, ch;
+  if (g.fixmap && fix_axis_x(u, g.rOu, g.cOu, g.Xlim_u, g.tq_u, g.O, g.log2O, &pu, &uf) &&
+      fix_axis_x(v, g.rOv, g.cOv, g.Xlim_v, g.tq_v, g.O, g.log2O, &pv, &vf) &&
+      fix_round(w, g.gw, g.rcp_gw, g.Plim_w, g.tq_w, &zg) && fix_round(w, g.cz, g.rcp_cz, g.Plim_z, g.tq_z, &zc) &&
+      fix_round(f, g.gf, g.rcp_gf, g.Plim_f, g.tq_f, &ch)) {
+    // uf, vf lie in [0, O) by construction
+    ok = pu >= 0 && pu < g.nx && pv >= 0 && pv < g.ny && zg >= 0 && zg < g.nw && zc >= 0 && zc < g.nz && ch >= 0 &&
+         ch < g.nchan && ch < g.cf_nchan;
+  } else {
+    const RawMap r = map_raw(u, v, w, f, g);
+    // Range checks in double so huge values cannot wrap when narrowed.
+    ok = r.pu >= 0.0 && r.pu < g.nx && r.pv >= 0.0 && r.pv < g.ny && r.uf >= 0.0 && r.uf < g.O && r.vf >= 0.0 &&
+         r.vf < g.O && r.zg >= 0.0 && r.zg < g.nw && r.zc >= 0.0 && r.zc < g.nz && r.ch >= 0.0 && r.ch < g.nchan &&
+         r.ch < g.cf_nchan;
+    pu = ok ? (int32_t)r.pu : 0;
+    pv = ok ? (int32_t)r.pv : 0;
+    uf = ok ? (int32_t)r.uf : 0;
+    vf = ok ? (int32_t)r.vf : 0;
+    zg = ok ? (int32_t)r.zg : 0;
+    zc = ok ? (int32_t)r.zc : 0;
+    ch = ok ? (int32_t)r.ch : 0;
+  }
+  m.pu = ok ? pu : -1;
+  m.pv = ok ? pv : -1;
+  m.uf = ok ? uf : 0;
+  m.vf = ok ? vf : 0;
+  m.zg = ok ? zg : 0;
+  m.zc = ok ? zc : 0;
+  m.ch = ok ? ch : 0;
   if (ok) {
     int h = plane_sz(g, m.zc) >> 1;
     ok = (m.pu - h >= 0) && (m.pu + h <= g.nx) && (m.pv - h >= 0) && (m.pv + h <= g.ny);

@@ -23,11 +23,16 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "dsmath.cuh"
 
 namespace arlgpu {
 
 void count_launch(unsigned n);
 int get_plan(int ny, int nx, int batch, long long dist, cufftType type, cufftHandle *out);
+bool tune_dsfft();
+bool dsfft_supported(int ny, int nx);
+int dsfft_g2i_wstack(const float2 *grid, int nb, int K, int ny, int nx, double fov, const double *wmean,
+                     const double *gcf, const double *sumwt, double *image, void *buf, int64_t G, cudaStream_t st);
 
 // w-screen of create_w_term_like at one pixel of an n x n image centred on
 // (n/2, n/2): exp(-2 pi i w (1 - sqrt(1 - r^2))), zero for r^2 >= 1, one at
@@ -122,11 +127,12 @@ __global__ void k_wstack_combine(const double2 *__restrict__ buf, int64_t p0, in
   }
 }
 
-// grid[b, s] = chk * conj(wb_s) * image * gcf  (complex), for every slice s
-template <typename CT>
-__global__ void k_wstack_pre_predict(const double *__restrict__ image, const double *__restrict__ gcf, int nb, int K,
-                                     int ny, int nx, double fov, const double *__restrict__ wmean,
-                                     CT *__restrict__ grid) {
+// grid[b, s] = chk * conj(wb_s) * image * gcf  (complex), for every slice s.
+// FP64 path: FP64 w-screen.  FP32C path: double-single w-screen (no FP64
+// square root or per-slice FP64 phase), FP32 sincospi.
+__global__ void k_wstack_pre_predict64(const double *__restrict__ image, const double *__restrict__ gcf, int nb, int K,
+                                       int ny, int nx, double fov, const double *__restrict__ wmean,
+                                       double2 *__restrict__ grid) {
   const int64_t plane = (int64_t)ny * nx, tot = (int64_t)nb * plane;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / plane, yx = i - b * plane;
@@ -134,11 +140,28 @@ __global__ void k_wstack_pre_predict(const double *__restrict__ image, const dou
     const double m = image[i] * gcf[i] * (((x + y) & 1) ? -1.0 : 1.0);
     const Pix px = wpix(y, x, nx, fov);
     for (int s = 0; s < K; ++s) {
-      const double2 wb = WB<CT>::at(px, wmean[s]);
-      CT v;
-      v.x = wb.x * m;
-      v.y = -wb.y * m;
-      grid[(b * K + s) * plane + yx] = v;
+      const double2 wb = wb64(px, wmean[s]);
+      grid[(b * K + s) * plane + yx] = make_double2(wb.x * m, -wb.y * m);
+    }
+  }
+}
+
+__global__ void k_wstack_pre_predict32(const double *__restrict__ image, const double *__restrict__ gcf, int nb, int K,
+                                       int ny, int nx, double fov, const double *__restrict__ wmean,
+                                       float2 *__restrict__ grid) {
+  extern __shared__ dsf s_w[];
+  for (int s = threadIdx.x; s < K; s += blockDim.x) s_w[s] = ds_from_double(wmean[s]);
+  __syncthreads();
+  const dsf fov2 = ds_from_double(fov * fov), n2 = ds_from_i64((long long)nx * nx);
+  const int64_t plane = (int64_t)ny * nx, tot = (int64_t)nb * plane;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / plane, yx = i - b * plane;
+    const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
+    const float m = (float)(image[i] * gcf[i]) * (((x + y) & 1) ? -1.f : 1.f);
+    const DsPix px = ds_wpix(y, x, nx, fov2, n2);
+    for (int s = 0; s < K; ++s) {
+      const float2 wb = ds_wbeam(px, s_w[s]);
+      grid[(b * K + s) * plane + yx] = make_float2(wb.x * m, -wb.y * m);
     }
   }
 }
@@ -195,6 +218,9 @@ static int g2i(const CT *grid, const arlgpu_grid_desc *gd, const double *gcf, co
   if (nplanes > 0x7fffffff) return fail(ARLGPU_ERR_UNSUPPORTED, "too many planes");
   const bool inplace = (const void *)grid == (const void *)fftbuf;
   const int64_t G = group_planes(nplanes, ny, nx);
+  if (sizeof(CT) == 8 && !inplace && tune_dsfft() && dsfft_supported(ny, nx))
+    return dsfft_g2i_wstack(reinterpret_cast<const float2 *>(grid), nb, K, ny, nx, fov, wmean, gcf, sumwt, image,
+                            fftbuf, G, st);
   const float s0 = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
   for (int64_t p0 = 0; p0 < nplanes; p0 += G) {
     const int64_t np = std::min(G, nplanes - p0);
@@ -222,7 +248,12 @@ static int i2g(const double *image, const double *gcf, const double *wmean, doub
   const int nb = gd->nchan * gd->npol, K = gd->nw, ny = gd->ny, nx = gd->nx;
   const int64_t nplanes = (int64_t)nb * K, plane = (int64_t)ny * nx;
   if (nplanes > 0x7fffffff) return fail(ARLGPU_ERR_UNSUPPORTED, "too many planes");
-  k_wstack_pre_predict<CT><<<nblk((int64_t)nb * plane), 256, 0, st>>>(image, gcf, nb, K, ny, nx, fov, wmean, grid);
+  if (sizeof(CT) == 16)
+    k_wstack_pre_predict64<<<nblk((int64_t)nb * plane), 256, 0, st>>>(image, gcf, nb, K, ny, nx, fov, wmean,
+                                                                      reinterpret_cast<double2 *>(grid));
+  else
+    k_wstack_pre_predict32<<<nblk((int64_t)nb * plane), 256, K * sizeof(dsf), st>>>(
+        image, gcf, nb, K, ny, nx, fov, wmean, reinterpret_cast<float2 *>(grid));
   ARL_LAUNCH_CHECK();
   count_launch(1);
   const int64_t G = group_planes(nplanes, ny, nx);

@@ -104,6 +104,9 @@ unsigned long long arlgpu_kernel_launches(void);
  *   "persistent"    1 = the lean and fixed-point kernels run as one grid of resident CTAs,
  *                   each looping over every gridDim-th chunk; 0 = one CTA per chunk, which the
  *                   hardware schedules dynamically (default: measured faster on C2)
+ *   "dsfft"         FP32C inverse transforms (invert_2d and w-stacking): 1 = double-single
+ *                   FFT on the FP32 pipes for power-of-two sizes 64..8192 (default),
+ *                   0 = cuFFT complex128
  * No reference counterpart (ARL has one Python loop per function). */
 int arlgpu_set_tuning(const char *key, int value);
 int arlgpu_get_tuning(const char *key, int *value);
@@ -148,9 +151,11 @@ int arlgpu_degrid_planned(int64_t nvis, int precision, const void *cf, const arl
 
 /* Mean w of the rows that a plan assigned to each grid w-plane (the slice mean
  * numpy.average(vis.w) of invert/predict_wstack_single, wstack_single.py:43,83);
- * wmean: [gd->nw] float64 (0 for empty planes).  Same nvis / gd / cd as the plan. */
+ * wmean: [gd->nw] float64 (0 for empty planes).  Same nvis / gd / cd as the plan.
+ * The plan's row order is read, and a small partial-sum area of the workspace is
+ * written; the result is deterministic (fixed summation order). */
 int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd,
-                             const void *workspace, size_t workspace_bytes, double *wmean, void *stream);
+                             void *workspace, size_t workspace_bytes, double *wmean, void *stream);
 
 /* ---- Gridding without any device allocation (no counterpart in the reference,
  * whose gridder is a NumPy loop) ----

@@ -69,10 +69,13 @@ def test_wstack_single_matches_oracle(arl, oracle, golden, precision):
     assert rel(pv.vis, vr - 1j * vi) < TOL[precision]
 
 
-def test_wstack_many_slices_vs_oracle(arl, oracle):
-    """12 slices, 2 channels imaged together (MFS through one wide image channel)."""
+@pytest.mark.parametrize('N', [96, 128])
+def test_wstack_many_slices_vs_oracle(arl, oracle, N):
+    """12 slices, 2 channels imaged together (MFS through one wide image channel).
+    N = 96 takes the complex128 cuFFT transforms on both precisions, N = 128 the
+    double-single transform on FP32C."""
     rng = numpy.random.default_rng(8)
-    N, cell, O, S, K, n = 96, 6e-3, 8, 8, 12, 4000
+    cell, O, S, K, n = 6e-3 * 96 / N, 8, 8, 12, 4000
     im = arl.create_image(npixel=N, cellsize=cell, frequency=numpy.array([1.05e8]), channel_bandwidth=numpy.array([1e8]),
                           phasecentre=arl.PhaseCentre(0.0, -45.0))
     gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=O, support=S)
