@@ -15,8 +15,9 @@
 // arithmetic runs on the FP32 pipes.
 //
 // Layout: a plane of ny x nx points, row-major.  Three passes per plane:
-//   rows   one CTA per 8192 points (8192 / nx rows): FP32 grid (w-planes
-//          summed, chk sign) -> row DFTs in shared memory -> DS buffer
+//   rows   one CTA per 4096 points (4096 / nx rows; one 8192-point row):
+//          FP32 grid (w-planes summed, chk sign) -> row DFTs in shared
+//          memory -> DS buffer
 //   cols1  ny = N1 * N2: DFTs of length N1 over rows n2 + N2 n1 of 32 or 64
 //          adjacent columns, times exp(2 pi i n2 k1 / ny), in place
 //   cols2  DFTs of length N2 over rows N2 k1 + n2 -> row k1 + N1 k2, with the
@@ -179,28 +180,36 @@ __device__ __forceinline__ int brev(int k, int log2L) { return (int)(__brev((uns
 // ---------------------------------------------------------------------------
 // Pass 1: row transforms.  Logical plane q of the input is the sum over
 // z < nsum of grid[q * qstride + z * plane]; rows of planes [q0, q0 + np) go to
-// buf[(q - q0) * plane + y * nx + x] with the chk sign applied on input.  The
-// shared-memory rows are padded by one slot per L/8 so that the bit-reversed
-// read of the epilogue is free of bank conflicts.
+// buf[(q - q0) * plane + y * nx + x] with the chk sign applied on input.  One
+// CTA holds PTS points (PTS / nx rows).  For rows of 512 points or more the
+// slot of point n within its row has its low three bits XORed with a function
+// of bits 3-5 and of the top three bits of n: the small-span butterflies
+// (strides 2, 4 and 16 slots) and the bit-reversed reads of the epilogue then
+// touch eight different 16-byte bank groups per quarter warp.
 // ---------------------------------------------------------------------------
-constexpr int kRowT = 1024, kRowPts = 8192, kRowSmem = (kRowPts + kRowPts / 8) * 16;
 constexpr int kColT = 512, kColPts = 4096, kColNPT = kColPts / kColT, kColSmem = kColPts * 16;
 
-__global__ void __launch_bounds__(kRowT, 1)
+template <int PTS, int T>
+__global__ void __launch_bounds__(T, 1)
 k_dsfft_rows(const float2 *__restrict__ grid, int64_t qstride, int nsum, int64_t q0, int np, int log2ny, int log2nx,
              float4 *__restrict__ buf) {
   extern __shared__ float4 sm[];
+  constexpr int LOG2PTS = PTS == 8192 ? 13 : 12;
   const int ny = 1 << log2ny;
   const int64_t plane = (int64_t)ny << log2nx;
-  const int log2S = 13 - log2nx;  // rows per CTA
+  const int log2S = LOG2PTS - log2nx;  // rows per CTA
   const int64_t row0 = (int64_t)blockIdx.x << log2S;
   const int64_t nrows = (int64_t)np << log2ny;
-  const int lpad = log2nx - 3;
+  const bool swz = log2nx >= 9;
   auto pos = [&](int n, int q) {
-    const int i = (q << log2nx) + n;
-    return i + (i >> lpad);
+    int m = n;
+    if (swz) {
+      const int j = (n >> 3) & 7;
+      m = n ^ ((j & 3) | ((j & 2) << 1)) ^ ((n >> (log2nx - 3)) & 7);
+    }
+    return (q << log2nx) + m;
   };
-  for (int t = threadIdx.x; t < kRowPts; t += kRowT) {
+  for (int t = threadIdx.x; t < PTS; t += T) {
     const int q = t >> log2nx, x = t & ((1 << log2nx) - 1);
     const int64_t R = row0 + q;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -221,8 +230,8 @@ k_dsfft_rows(const float2 *__restrict__ grid, int64_t qstride, int nsum, int64_t
     sm[pos(x, q)] = v;
   }
   __syncthreads();
-  ds_dif_cta<kRowT>(sm, log2nx, log2S, false, pos);
-  for (int t = threadIdx.x; t < kRowPts; t += kRowT) {
+  ds_dif_cta<T>(sm, log2nx, log2S, false, pos);
+  for (int t = threadIdx.x; t < PTS; t += T) {
     const int q = t >> log2nx, x = t & ((1 << log2nx) - 1);
     const int64_t R = row0 + q;
     if (R < nrows) buf[(R << log2nx) + x] = sm[pos(brev(x, log2nx), q)];
@@ -335,7 +344,7 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
   const int k1_0 = (int)(blockIdx.x / ntx) << cg.log2G2, x0 = (int)(blockIdx.x % ntx) << cg.log2WC2;
   const int WC2 = (1 << cg.log2WC2) - 1, log2S = cg.log2G2 + cg.log2WC2, S1 = (1 << log2S) - 1;
   const int n = 1 << log2nx;
-  const dsf fov2 = ds_from_double(fov * fov), nn = ds_from_i64((long long)n * n);
+  const dsf c2 = ds_from_double(fov * fov / ((double)n * n));
   auto pos = [&](int k, int q) { return (k << log2S) + q; };
   dsf acc[kColNPT];
 #pragma unroll
@@ -358,7 +367,7 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
       const int k2 = t >> log2S, q = t & S1;
       const float4 v = sm[pos(brev(k2, cg.log2N2), q)];
       const int k = k1_0 + (q >> cg.log2WC2) + (k2 << cg.log2N1), x = x0 + (q & WC2);
-      const float2 wb = ds_wbeam(ds_wpix(k, x, n, fov2, nn), w);
+      const float2 wb = ds_wbeam(ds_wpix(k, x, n, c2), w);
       // Re(wb v) = wb.re v.re - wb.im v.im
       acc[m] = ds_add(acc[m], ds_sub(ds_mul_f({v.x, v.y}, wb.x), ds_mul_f({v.z, v.w}, wb.y)));
     }
@@ -420,7 +429,8 @@ bool dsfft_supported(int ny, int nx) {
 static int set_smem() {
   static std::atomic<int> done{0};
   if (done.load()) return ARLGPU_OK;
-  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kRowSmem));
+  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows<8192, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8192 * 16));
+  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows<4096, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols1, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_image, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_wstack, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
@@ -432,9 +442,13 @@ static int set_smem() {
 static int rows_cols1(const float2 *grid, int64_t qstride, int nsum, int64_t q0, int64_t np, int ly, int lx,
                       const ColGeom &cg, float4 *buf, cudaStream_t st) {
   const int64_t nrows = np << ly;
-  const int log2S = 13 - lx;
-  const int64_t rblocks = (nrows + ((int64_t)1 << log2S) - 1) >> log2S;
-  k_dsfft_rows<<<(unsigned)rblocks, kRowT, kRowSmem, st>>>(grid, qstride, nsum, q0, (int)np, ly, lx, buf);
+  if (lx == 13) {
+    k_dsfft_rows<8192, 1024><<<(unsigned)nrows, 1024, 8192 * 16, st>>>(grid, qstride, nsum, q0, (int)np, ly, lx, buf);
+  } else {
+    const int log2S = 12 - lx;
+    const int64_t rblocks = (nrows + ((int64_t)1 << log2S) - 1) >> log2S;
+    k_dsfft_rows<4096, 512><<<(unsigned)rblocks, 512, 4096 * 16, st>>>(grid, qstride, nsum, q0, (int)np, ly, lx, buf);
+  }
   ARL_LAUNCH_CHECK();
   const int64_t ntile = ((int64_t)1 << (cg.log2N2 - cg.log2G1)) << (lx - cg.log2WC1);
   k_dsfft_cols1<<<(unsigned)(np * ntile), kColT, kColSmem, st>>>(buf, ly, lx, cg, ntile);

@@ -152,13 +152,13 @@ __global__ void k_wstack_pre_predict32(const double *__restrict__ image, const d
   extern __shared__ dsf s_w[];
   for (int s = threadIdx.x; s < K; s += blockDim.x) s_w[s] = ds_from_double(wmean[s]);
   __syncthreads();
-  const dsf fov2 = ds_from_double(fov * fov), n2 = ds_from_i64((long long)nx * nx);
+  const dsf c2 = ds_from_double(fov * fov / ((double)nx * nx));
   const int64_t plane = (int64_t)ny * nx, tot = (int64_t)nb * plane;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / plane, yx = i - b * plane;
     const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
     const float m = (float)(image[i] * gcf[i]) * (((x + y) & 1) ? -1.f : 1.f);
-    const DsPix px = ds_wpix(y, x, nx, fov2, n2);
+    const DsPix px = ds_wpix(y, x, nx, c2);
     for (int s = 0; s < K; ++s) {
       const float2 wb = ds_wbeam(px, s_w[s]);
       grid[(b * K + s) * plane + yx] = make_float2(wb.x * m, -wb.y * m);

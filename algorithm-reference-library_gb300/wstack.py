@@ -15,8 +15,9 @@ slice is one plane of a [nchan, npol, K, ny, nx] grid:
 
   invert   plan (FP64 map + bin rows by channel, slice and uv-tile) -> one
            gridder launch over all channels, polarisations and slices ->
-           FP64 inverse transforms of the planes -> one pass applying each
-           slice's w-beam and summing the slices into the image.
+           inverse transforms of the planes (double-single on FP32C,
+           complex128 on FP64), the last pass applying each slice's w-beam
+           and summing the slices into the image.
   predict  one pass writing conj(w-beam_s) * model * gcf into every plane ->
            forward transforms -> one degridder launch over all rows (each row
            reads its own slice's plane).

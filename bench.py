@@ -56,6 +56,9 @@ def parse():
     ap.add_argument('--profile-rows', type=int, default=0,
                     help='profiling case for ncu: the workload subsampled to this many rows, --warmup + --steps '
                          'untimed steps with the library defaults, no other arms')
+    ap.add_argument('--transform', type=int, default=0, metavar='N',
+                    help='time the FP32C inverse 2-D transform with grid correction alone on two random N^2 '
+                         'planes: the double-single FFT against cuFFT complex128 (also a small ncu case)')
     return ap.parse_args()
 
 
@@ -288,8 +291,8 @@ def _events(torch, n):
 
 
 def stage_rates(arl, torch, ctx, steps, warmup, flush):
-    """vis/s of invert_2d (plan + grid + FP64 inverse FFT with grid correction
-    and sumwt normalisation) and predict_2d (gcf multiply + forward FFT +
+    """vis/s of invert_2d (plan + grid + inverse transform with grid correction
+    and sumwt normalisation: double-single on FP32C, complex128 on FP64) and predict_2d (gcf multiply + forward FFT +
     degrid) on the bench's device-resident rows; L2 flushed between steps."""
     nat = arl._native
     P = nat.PRECISIONS[ctx['precision']]
@@ -618,9 +621,10 @@ def arm_gb300(args, torch, world, rank, local):
 def arm_wstack(args, torch, world, rank, local):
     """The w-stacking workloads (C3: 4 pols, 64 flagged channels, 20 slices,
     4096^2; C5: 1e8 rows, 32 slices, 8192^2): vis/s of the batched w-stack
-    invert (plan + grid + FP64 FFTs + w-beam combine) and predict (w-beam +
-    FFTs + degrid) through WStackImager, and of the invert replayed as one
-    CUDA graph.  Inputs and grids exceed L2, so no flush is needed."""
+    invert (plan + grid + inverse transforms with the w-screen sum: double-single
+    on FP32C, complex128 on FP64) and predict (w-screens + FFTs + degrid)
+    through WStackImager, of the invert replayed as one CUDA graph, and one
+    staged pass.  Inputs and grids exceed L2, so no flush is needed."""
     arl = importlib.import_module('algorithm-reference-library_gb300')
     sim = arl.simulation
     device = torch.device('cuda', local)
@@ -662,6 +666,7 @@ def arm_wstack(args, torch, world, rank, local):
         if prec == 'fp32c':
             imager.capture('invert')
             r['invert_graph_ms'] = timed(lambda: imager.replay('invert'), args.steps, 2)
+            r['stages_ms'] = wstack_stages(torch, imager, stream)
         res[prec] = r
         del imager, dvis
         torch.cuda.empty_cache()
@@ -679,6 +684,76 @@ def arm_wstack(args, torch, world, rank, local):
         line['fp64'] = res['fp64']
         line['fp32c_speedup'] = (res['fp64']['invert_ms'] + res['fp64']['predict_ms']) / ms
     return line
+
+
+def wstack_stages(torch, imager, stream):
+    """One staged pass of the imager: plan, grid, transforms + w-screens into
+    the image (g2i), w-screens + transforms of the model (i2g), degrid."""
+    nat = importlib.import_module('algorithm-reference-library_gb300._native')
+    e = _events(torch, 6)
+    e[0].record(stream)
+    imager.plan()
+    e[1].record(stream)
+    imager.grid()
+    e[2].record(stream)
+    imager.grid_to_image()
+    e[3].record(stream)
+    nat.call('arlgpu_wstack_image_to_grid', nat.ptr(imager.model), nat.ptr(imager.gcf_t), nat.ptr(imager.wmean),
+             imager.cellsize, ctypes.byref(imager.gd), nat.PRECISIONS[imager.precision], nat.ptr(imager.grid_t),
+             nat.stream_ptr())
+    e[4].record(stream)
+    nat.call('arlgpu_degrid_planned', imager.n, nat.PRECISIONS[imager.precision], nat.ptr(imager.cf_t),
+             ctypes.byref(imager.cd), nat.ptr(imager.grid_t), ctypes.byref(imager.gd), nat.ptr(imager.out),
+             nat.ptr(imager.ws), imager.ws.numel(), nat.stream_ptr())
+    e[5].record(stream)
+    torch.cuda.synchronize()
+    names = ('plan', 'grid', 'g2i', 'i2g', 'degrid')
+    return {k: round(e[i].elapsed_time(e[i + 1]), 3) for i, k in enumerate(names)}
+
+
+def arm_transform(args, torch):
+    """ms per call of the FP32C inverse transform (grid correction and sumwt
+    normalisation fused) on two random N^2 planes: the double-single FFT
+    (tuning dsfft=1) and cuFFT complex128 (dsfft=0).  The grid (8 B/cell) and
+    the FFT scratch (16 B/cell) exceed L2 from N = 2048."""
+    arl = importlib.import_module('algorithm-reference-library_gb300')
+    dv = arl.device
+    dev = torch.device('cuda', 0)
+    N, nb = args.transform, 2
+    g = torch.Generator(device='cpu').manual_seed(N)
+    shape = (1, nb, 1, N, N)
+    grid = torch.complex(torch.randn(shape, generator=g), torch.randn(shape, generator=g)).to(dev)
+    gcf = (1.0 + torch.rand((1, nb, N, N), generator=g, dtype=torch.float64)).to(dev)
+    sumwt = torch.ones((1, nb), dtype=torch.float64, device=dev)
+    im = arl.create_image(npixel=64, cellsize=1e-3, frequency=numpy.array([1e8]), channel_bandwidth=numpy.array([1e6]),
+                          phasecentre=arl.PhaseCentre(0.0, -45.0))
+    gd = dv.grid_desc(arl.kernels._grid_wcs(im, 1, 1e15), shape)
+    buf = torch.empty(nb * N * N, dtype=torch.complex128, device=dev)
+    re = torch.empty((1, nb, N, N), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+    old = arl.tune.get_tuning()['dsfft']
+    out = {}
+    for ds in (1, 0):
+        arl.tune.set_tuning(dsfft=ds)
+        for _ in range(args.warmup):
+            dv.fft_grid_to_image(grid, gd, gcf, 'fp32c', sumwt=sumwt, buf=buf)
+        torch.cuda.synchronize()
+        e = _events(torch, 2)
+        e[0].record(stream)
+        for _ in range(args.steps):
+            dv.fft_grid_to_image(grid, gd, gcf, 'fp32c', sumwt=sumwt, buf=buf)
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        out[ds] = e[0].elapsed_time(e[1]) / args.steps
+    arl.tune.set_tuning(dsfft=old)
+    cells = nb * N * N
+    return {'metric': 'ms per FP32C inverse 2-D transform with grid correction (%d planes of %d^2)' % (nb, N),
+            'value': out[1], 'unit': 'ms', 'higher_is_better': False, 'steps': args.steps, 'warmup': args.warmup,
+            'n_gpus': 1, 'dtype': 'f32 pairs (double-single)', 'data': 'synthetic (random grid)',
+            'config': {'workload': 'transform %dx%d^2' % (nb, N)},
+            'cufft_complex128_ms': out[0], 'speedup_vs_complex128': out[0] / out[1],
+            'bytes_per_cell': {'grid_in': 8, 'gcf_in': 8, 'image_out': 8, 'ds_scratch_rw': 64},
+            'gcells_per_s': cells / (out[1] * 1e-3) / 1e9}
 
 
 def arm_reference(args, torch, world, rank):
@@ -748,6 +823,9 @@ def main():
     import torch
     if args.profile_rows:
         profile_case(args, torch)
+        return
+    if args.transform:
+        print(json.dumps(arm_transform(args, torch)), flush=True)
         return
     world, rank, local = dist_setup(torch)
     if args.impl == 'reference':
