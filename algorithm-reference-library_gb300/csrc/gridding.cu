@@ -1129,6 +1129,16 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
 // segments of up to 512 rows) plus the final FP32 rounding.  Without RESID
 // (grid_kernel 5, measurement only) each contribution carries a quantisation
 // error of up to half a unit, 2^-e-1.
+// int32 -> FP32 with round-to-nearest, without the conversion instruction
+// (GB300 issues conversions to its narrow FP64/conversion pipe): the two
+// 16-bit halves of q are exact FP32 values through the 1.5 * 2^23 shift, and
+// one FMA rounds hi * 2^16 + lo once, as the conversion would.
+__device__ __forceinline__ float i2f_rn(int q) {
+  const float fh = __int_as_float((q >> 16) + 0x4B400000) - 12582912.0f;
+  const float fl = __int_as_float((q & 0xffff) + 0x4B400000) - 12582912.0f;
+  return fmaf(fh, 65536.0f, fl);
+}
+
 template <bool RESID>
 __device__ __forceinline__ void fx_add(int *q, int *r, float x, float scale, float rscale) {
   const float t = fmaf(x, scale, 12582912.0f);
@@ -1339,8 +1349,8 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
             // inv and rinv * inv are powers of two: one rounding in the FMA
             // (and in the int -> float conversions of sums beyond 2^24)
             float2 val;
-            val.x = fmaf((float)rx, rinv * inv, (float)qx * inv);
-            val.y = fmaf((float)ry, rinv * inv, (float)qy * inv);
+            val.x = fmaf(i2f_rn(rx), rinv * inv, i2f_rn(qx) * inv);
+            val.y = fmaf(i2f_rn(ry), rinv * inv, i2f_rn(qy) * inv);
             red_global<float2>(grid + ((int64_t)(sg.ch * NPOL + p) * g.nw + sg.zg) * plane_elems +
                                    (int64_t)gy * g.nx + gx,
                                val);

@@ -143,38 +143,43 @@ __device__ __forceinline__ RawMap map_raw(double u, double v, double w, double f
   return r;
 }
 
-// Fixed-point view of a double |X| < 2^30 with 20 fraction bits: X + 1.5 2^32
-// lies in [2^32, 2^33) where the ulp is 2^-20, so its bit pattern minus that
-// of 1.5 2^32 is X * 2^20 rounded to an integer.  One FP64 add replaces a
-// floor, a subtraction, two comparisons and a conversion.
-__device__ __forceinline__ long long fix20(double X) {
-  return __double_as_longlong(__dadd_rn(X, 6442450944.0)) - 0x41F8000000000000LL;
+// Fixed-point view of a double with 20 fraction bits: for |X| < 2^31,
+// y = X + 1.5 2^32 lies in [2^32, 2^33) where the ulp is 2^-20, so y's bit
+// pattern minus that of 1.5 2^32 is X * 2^20 rounded to an integer.  One FP64
+// add replaces a floor, a subtraction, comparisons and a conversion; the
+// range test is y's exponent field (false for |X| >= 2^31 and NaN).
+__device__ __forceinline__ bool fix20(double X, long long *F) {
+  const long long b = __double_as_longlong(__dadd_rn(X, 6442450944.0));
+  *F = b - 0x41F8000000000000LL;
+  return (b >> 52) == 0x41F;
 }
 
 // Pixel and sub-pixel index of one axis from X = P * O (power-of-two O), as
 // map_axis_x, with the integer-boundary test in fixed point: the fraction of
 // X rounded to 2^-20 lies at least tq units from an integer, so X and NumPy's
-// value (within tol of X) have the same floor.
-__device__ __forceinline__ bool fix_axis_x(double x, double rO, double cO, double Xlim, int tq, int O, int log2O,
-                                           int *pix, int *sub) {
-  const double X = fma(x, rO, cO);
-  if (!(fabs(X) < Xlim)) return false;
-  const long long F = fix20(X);
+// value (within tol of X) have the same floor.  Beyond the range where tol is
+// valid (|X| >= Xlim) the index is out of the grid whichever way it rounds,
+// so no separate range test is needed.
+__device__ __forceinline__ bool fix_axis_x(double x, double rO, double cO, int tq, int O, int log2O, int *pix,
+                                           int *sub) {
+  long long F;
+  if (!fix20(fma(x, rO, cO), &F)) return false;
   const int fr = (int)(F & 0xFFFFF);
   if (fr < tq || fr > (1 << 20) - tq) return false;
-  const int a = (int)(F >> 20) + (O >> 1);
-  *pix = a >> log2O;
-  *sub = a - (*pix << log2O);
+  const long long a = (F >> 20) + (O >> 1);
+  const long long pl = a >> log2O;
+  *pix = (int)max(min(pl, 0x3fffffffLL), -0x3fffffffLL);
+  *sub = (int)(a - (pl << log2O));
   return true;
 }
 
 // Nearest-plane index as round_w2p_tol, with the half-integer test in fixed
 // point (F = (P + 1/2) 2^20: the index is F >> 20 when F's fraction is at
 // least tq units from an integer).
-__device__ __forceinline__ bool fix_round(double x, const arlgpu_axis &a, double rcp, double Plim, int tq, int *idx) {
-  const double p = fma(__dsub_rn(x, a.crval), rcp, a.crpix - 1.0);
-  if (!(fabs(p) < Plim)) return false;
-  const long long F = fix20(p) + (1LL << 19);
+__device__ __forceinline__ bool fix_round(double x, const arlgpu_axis &a, double rcp, int tq, int *idx) {
+  long long F;
+  if (!fix20(fma(__dsub_rn(x, a.crval), rcp, a.crpix - 1.0), &F)) return false;
+  F += 1LL << 19;
   const int fr = (int)(F & 0xFFFFF);
   if (fr < tq || fr > (1 << 20) - tq) return false;
   *idx = (int)(F >> 20);
@@ -185,10 +190,9 @@ __device__ __forceinline__ Mapped map_row(double u, double v, double w, double f
   Mapped m;
   bool ok;
   int pu, pv, uf, vf, zg, zc, ch;
-  if (g.fixmap && fix_axis_x(u, g.rOu, g.cOu, g.Xlim_u, g.tq_u, g.O, g.log2O, &pu, &uf) &&
-      fix_axis_x(v, g.rOv, g.cOv, g.Xlim_v, g.tq_v, g.O, g.log2O, &pv, &vf) &&
-      fix_round(w, g.gw, g.rcp_gw, g.Plim_w, g.tq_w, &zg) && fix_round(w, g.cz, g.rcp_cz, g.Plim_z, g.tq_z, &zc) &&
-      fix_round(f, g.gf, g.rcp_gf, g.Plim_f, g.tq_f, &ch)) {
+  if (g.fixmap && fix_axis_x(u, g.rOu, g.cOu, g.tq_u, g.O, g.log2O, &pu, &uf) &&
+      fix_axis_x(v, g.rOv, g.cOv, g.tq_v, g.O, g.log2O, &pv, &vf) && fix_round(w, g.gw, g.rcp_gw, g.tq_w, &zg) &&
+      fix_round(w, g.cz, g.rcp_cz, g.tq_z, &zc) && fix_round(f, g.gf, g.rcp_gf, g.tq_f, &ch)) {
     // uf, vf lie in [0, O) by construction
     ok = pu >= 0 && pu < g.nx && pv >= 0 && pv < g.ny && zg >= 0 && zg < g.nw && zc >= 0 && zc < g.nz && ch >= 0 &&
          ch < g.nchan && ch < g.cf_nchan;
