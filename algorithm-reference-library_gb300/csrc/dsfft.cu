@@ -15,9 +15,9 @@
 // arithmetic runs on the FP32 pipes.
 //
 // Layout: a plane of ny x nx points, row-major.  Three passes per plane:
-//   rows   one CTA per 4096 points (4096 / nx rows; one 8192-point row):
-//          FP32 grid (w-planes summed, chk sign) -> row DFTs in shared
-//          memory -> DS buffer
+//   rows   one CTA per 4096 points (4096 / nx rows, or half of an
+//          8192-point row): FP32 grid (w-planes summed, chk sign) -> row
+//          DFTs in shared memory -> DS buffer
 //   cols1  ny = N1 * N2: DFTs of length N1 over rows n2 + N2 n1 of 32 or 64
 //          adjacent columns, times exp(2 pi i n2 k1 / ny), in place
 //   cols2  DFTs of length N2 over rows N2 k1 + n2 -> row k1 + N1 k2, with the
@@ -119,10 +119,14 @@ __device__ __forceinline__ float4 twiddle(int m, int log2n) { return __ldg(&g_tw
 // into one butterfly on the points n0 + {0, h/2, h, 3h/2} of a block of 2h:
 //   a = x0 + x2, b = x0 - x2, c = x1 + x3, d = i (x1 - x3), w = exp(2 pi i j / 2h)
 //   y0 = a + c, y1 = (a - c) w^2, y2 = (b + d) w, y3 = (b - d) w^3
-// and an odd log2 L ends with one radix-2 stage of span 1.
+// and an odd log2 L ends with one radix-2 stage of span 1.  Sums are left
+// unnormalised (hi + lo still equals the value; the next error-free sum or
+// twiddle product absorbs it), which NumPy float32 emulation shows costs
+// nothing measurable (7.9e-15 against 7.4e-15 of the scale at 8192 points).
+// tw(m, lw) = exp(2 pi i m / 2^lw).
 // ---------------------------------------------------------------------------
-template <int T, typename Pos>
-__device__ __forceinline__ void ds_dif_cta(float4 *sm, int log2L, int log2S, bool seqfast, Pos pos) {
+template <int T, typename Pos, typename Tw>
+__device__ __forceinline__ void ds_dif_cta(float4 *sm, int log2L, int log2S, bool seqfast, Pos pos, Tw tw) {
   const int S1 = (1 << log2S) - 1;
   const int nb4 = 1 << (log2L - 2 + log2S);
   int log2h = log2L - 1;
@@ -147,15 +151,14 @@ __device__ __forceinline__ void ds_dif_cta(float4 *sm, int log2L, int log2S, boo
       const float4 x0 = sm[i0], x1 = sm[i1], x2 = sm[i2], x3 = sm[i3];
       const float4 a = c_add_nr(x0, x2), b = c_add_nr(x0, c_neg(x2));
       const float4 c = c_add_nr(x1, x3), d = c_muli(c_add_nr(x1, c_neg(x3)));
-      float4 y0 = c_norm(c_add_nr(a, c)), y1 = c_norm(c_add_nr(a, c_neg(c)));
-      float4 y2 = c_norm(c_add_nr(b, d)), y3 = c_norm(c_add_nr(b, c_neg(d)));
+      float4 y1 = c_add_nr(a, c_neg(c)), y2 = c_add_nr(b, d), y3 = c_add_nr(b, c_neg(d));
       if (jp) {
         const int lw = log2h + 1;
-        y2 = c_mul(y2, twiddle(jp, lw));
-        y1 = c_mul(y1, twiddle(2 * jp, lw));
-        y3 = c_mul(y3, twiddle(3 * jp, lw));
+        y2 = c_mul(y2, tw(jp, lw));
+        y1 = c_mul(y1, tw(2 * jp, lw));
+        y3 = c_mul(y3, tw(3 * jp, lw));
       }
-      sm[i0] = y0;
+      sm[i0] = c_add_nr(a, c);
       sm[i1] = y1;
       sm[i2] = y2;
       sm[i3] = y3;
@@ -168,11 +171,26 @@ __device__ __forceinline__ void ds_dif_cta(float4 *sm, int log2L, int log2S, boo
       const int q = seqfast ? (bb & S1) : (bb >> lb), i = seqfast ? (bb >> log2S) : (bb & B1);
       const int i0 = pos(2 * i, q), i1 = pos(2 * i + 1, q);
       const float4 x0 = sm[i0], x1 = sm[i1];
-      sm[i0] = c_norm(c_add_nr(x0, x1));
-      sm[i1] = c_norm(c_add_nr(x0, c_neg(x1)));
+      sm[i0] = c_add_nr(x0, x1);
+      sm[i1] = c_add_nr(x0, c_neg(x1));
     }
     __syncthreads();
   }
+}
+
+// Global table lookup, for the row transforms.
+struct TwGlobal {
+  __device__ __forceinline__ float4 operator()(int m, int lw) const { return twiddle(m, lw); }
+};
+// exp(2 pi i m / L) for m < L <= 128 staged in shared memory by the column
+// kernels (the only twiddles their transforms use).
+struct TwShared {
+  const float4 *t;
+  int log2L;
+  __device__ __forceinline__ float4 operator()(int m, int lw) const { return t[m << (log2L - lw)]; }
+};
+__device__ __forceinline__ void stage_twiddles(float4 *t, int log2L) {
+  for (int m = threadIdx.x; m < (1 << log2L); m += blockDim.x) t[m] = twiddle(m, log2L);
 }
 
 __device__ __forceinline__ int brev(int k, int log2L) { return (int)(__brev((unsigned)k) >> (32 - log2L)); }
@@ -187,10 +205,10 @@ __device__ __forceinline__ int brev(int k, int log2L) { return (int)(__brev((uns
 // (strides 2, 4 and 16 slots) and the bit-reversed reads of the epilogue then
 // touch eight different 16-byte bank groups per quarter warp.
 // ---------------------------------------------------------------------------
-constexpr int kColT = 512, kColPts = 4096, kColNPT = kColPts / kColT, kColSmem = kColPts * 16;
+constexpr int kColT = 512, kColPts = 4096, kColNPT = kColPts / kColT, kColSmem = (kColPts + 128) * 16;
 
 template <int PTS, int T>
-__global__ void __launch_bounds__(T, 1)
+__global__ void __launch_bounds__(T, 1024 / T)
 k_dsfft_rows(const float2 *__restrict__ grid, int64_t qstride, int nsum, int64_t q0, int np, int log2ny, int log2nx,
              float4 *__restrict__ buf) {
   extern __shared__ float4 sm[];
@@ -230,12 +248,62 @@ k_dsfft_rows(const float2 *__restrict__ grid, int64_t qstride, int nsum, int64_t
     sm[pos(x, q)] = v;
   }
   __syncthreads();
-  ds_dif_cta<T>(sm, log2nx, log2S, false, pos);
+  ds_dif_cta<T>(sm, log2nx, log2S, false, pos, TwGlobal());
   for (int t = threadIdx.x; t < PTS; t += T) {
     const int q = t >> log2nx, x = t & ((1 << log2nx) - 1);
     const int64_t R = row0 + q;
     if (R < nrows) buf[(R << log2nx) + x] = sm[pos(brev(x, log2nx), q)];
   }
+}
+
+// 8192-point rows as two 4096-point halves on two CTAs (64 KiB of shared
+// memory each, so that two CTAs share an SM): the first decimation-in-
+// frequency stage, span 4096, is done while loading, CTA h = 0 taking
+// x[n] + x[n + 4096] (whose DFT is X[2k]) and h = 1 taking
+// (x[n] - x[n + 4096]) exp(2 pi i n / 8192) (DFT X[2k + 1]); each writes its
+// 4096 outputs to the even or odd positions of the row.
+__global__ void __launch_bounds__(512, 2)
+k_dsfft_rows_split(const float2 *__restrict__ grid, int64_t qstride, int nsum, int64_t q0, int np, int log2ny,
+                   float4 *__restrict__ buf) {
+  extern __shared__ float4 sm[];
+  constexpr int LX = 13, LH = 12, H = 1 << LH;
+  const int ny = 1 << log2ny;
+  const int64_t plane = (int64_t)ny << LX;
+  const int64_t R = blockIdx.x >> 1;
+  const int half = blockIdx.x & 1;
+  auto pos = [&](int n, int) {
+    const int j = (n >> 3) & 7;
+    return n ^ ((j & 3) | ((j & 2) << 1)) ^ ((n >> (LH - 3)) & 7);
+  };
+  const int64_t pl = R >> log2ny;
+  const int y = (int)(R & (ny - 1));
+  const float2 *src = grid + (q0 + pl) * qstride + ((int64_t)y << LX);
+  auto in = [&](int x) -> float4 {
+    float2 g = src[x];
+    dsf re = {g.x, 0.f}, im = {g.y, 0.f};
+    for (int z = 1; z < nsum; ++z) {
+      g = src[z * plane + x];
+      re = ds_add(re, {g.x, 0.f});
+      im = ds_add(im, {g.y, 0.f});
+    }
+    const float sg = ((x + y) & 1) ? -1.f : 1.f;
+    return make_float4(sg * re.hi, sg * re.lo, sg * im.hi, sg * im.lo);
+  };
+  for (int n = threadIdx.x; n < H; n += 512) {
+    const float4 a = in(n), b = in(n + H);
+    float4 v;
+    if (half == 0) {
+      v = c_add_nr(a, b);
+    } else {
+      v = c_add_nr(a, c_neg(b));
+      if (n) v = c_mul(v, twiddle(n, LX));
+    }
+    sm[pos(n, 0)] = v;
+  }
+  __syncthreads();
+  ds_dif_cta<512>(sm, LH, 0, false, pos, TwGlobal());
+  float4 *out = buf + (R << LX) + half;
+  for (int k = threadIdx.x; k < H; k += 512) out[2 * k] = sm[pos(brev(k, LH), 0)];
 }
 
 // ---------------------------------------------------------------------------
@@ -274,9 +342,11 @@ k_dsfft_cols1(float4 *__restrict__ buf, int log2ny, int log2nx, ColGeom cg, int6
     return ((int64_t)(n2 + (n1 << cg.log2N2)) << log2nx) + x0 + (q & WC1);
   };
   auto pos = [&](int n, int q) { return (n << log2S) + q; };
+  float4 *stw = sm + kColPts;
+  stage_twiddles(stw, cg.log2N1);
   for (int t = threadIdx.x; t < kColPts; t += kColT) sm[t] = p[addr(t >> log2S, t & ((1 << log2S) - 1))];
   __syncthreads();
-  ds_dif_cta<kColT>(sm, cg.log2N1, log2S, true, pos);
+  ds_dif_cta<kColT>(sm, cg.log2N1, log2S, true, pos, TwShared{stw, cg.log2N1});
   for (int t = threadIdx.x; t < kColPts; t += kColT) {
     const int k1 = t >> log2S, q = t & ((1 << log2S) - 1);
     const int n2 = n2_0 + (q >> cg.log2WC1);
@@ -306,8 +376,10 @@ k_dsfft_cols2_image(const float4 *__restrict__ buf, int log2ny, int log2nx, ColG
     const int k1 = k1_0 + (q >> cg.log2WC2);
     sm[t] = p[((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2)];
   }
+  float4 *stw = sm + kColPts;
+  stage_twiddles(stw, cg.log2N2);
   __syncthreads();
-  ds_dif_cta<kColT>(sm, cg.log2N2, log2S, true, pos);
+  ds_dif_cta<kColT>(sm, cg.log2N2, log2S, true, pos, TwShared{stw, cg.log2N2});
   double inv = 1.0;
   bool zero = false;
   if (sumwt) {
@@ -346,6 +418,8 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
   const int n = 1 << log2nx;
   const dsf c2 = ds_from_double(fov * fov / ((double)n * n));
   auto pos = [&](int k, int q) { return (k << log2S) + q; };
+  float4 *stw = sm + kColPts;
+  stage_twiddles(stw, cg.log2N2);  // ordered before first use by the barrier after the first load
   dsf acc[kColNPT];
 #pragma unroll
   for (int m = 0; m < kColNPT; ++m) acc[m] = {0.f, 0.f};
@@ -359,7 +433,7 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
       sm[t] = p[((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2)];
     }
     __syncthreads();
-    ds_dif_cta<kColT>(sm, cg.log2N2, log2S, true, pos);
+    ds_dif_cta<kColT>(sm, cg.log2N2, log2S, true, pos, TwShared{stw, cg.log2N2});
     const dsf w = ds_from_double(wmean[s]);
 #pragma unroll
     for (int m = 0; m < kColNPT; ++m) {
@@ -429,7 +503,7 @@ bool dsfft_supported(int ny, int nx) {
 static int set_smem() {
   static std::atomic<int> done{0};
   if (done.load()) return ARLGPU_OK;
-  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows<8192, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8192 * 16));
+  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows_split, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows<4096, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols1, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_image, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
@@ -443,7 +517,7 @@ static int rows_cols1(const float2 *grid, int64_t qstride, int nsum, int64_t q0,
                       const ColGeom &cg, float4 *buf, cudaStream_t st) {
   const int64_t nrows = np << ly;
   if (lx == 13) {
-    k_dsfft_rows<8192, 1024><<<(unsigned)nrows, 1024, 8192 * 16, st>>>(grid, qstride, nsum, q0, (int)np, ly, lx, buf);
+    k_dsfft_rows_split<<<(unsigned)(2 * nrows), 512, 4096 * 16, st>>>(grid, qstride, nsum, q0, (int)np, ly, buf);
   } else {
     const int log2S = 12 - lx;
     const int64_t rblocks = (nrows + ((int64_t)1 << log2S) - 1) >> log2S;
