@@ -110,6 +110,16 @@ __device__ __forceinline__ float4 c_mul(float4 a, float4 w) {
 // exp(+2 pi i m / 2^log2n) for 0 <= m < 2^log2n <= 16384
 __device__ __forceinline__ float4 twiddle(int m, int log2n) { return __ldg(&g_tw[m << (kLog2Tw - log2n)]); }
 
+// 16-byte global -> shared copies that bypass the registers, all in flight
+// before one wait (the column passes stage their 64 KiB tiles this way).
+__device__ __forceinline__ void cp_async16(float4 *smem, const float4 *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // In-place radix-2^2 decimation-in-frequency transform (inverse sign) of
 // S = 2^log2S sequences of L = 2^log2L points held in shared memory at
@@ -227,6 +237,28 @@ k_dsfft_rows(const float2 *__restrict__ grid, int64_t qstride, int nsum, int64_t
     }
     return (q << log2nx) + m;
   };
+  if (nsum == 1) {
+    // all loads of the thread in flight before the first shared store
+    constexpr int K = PTS / T;
+    float2 gv[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int t = threadIdx.x + k * T;
+      const int q = t >> log2nx, x = t & ((1 << log2nx) - 1);
+      const int64_t R = row0 + q;
+      gv[k] = make_float2(0.f, 0.f);
+      if (R < nrows)
+        gv[k] = grid[(q0 + (R >> log2ny)) * qstride + ((int64_t)(R & (ny - 1)) << log2nx) + x];
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int t = threadIdx.x + k * T;
+      const int q = t >> log2nx, x = t & ((1 << log2nx) - 1);
+      const int y = (int)((row0 + q) & (ny - 1));
+      const float sg = ((x + y) & 1) ? -1.f : 1.f;
+      sm[pos(x, q)] = make_float4(sg * gv[k].x, 0.f, sg * gv[k].y, 0.f);
+    }
+  } else {
   for (int t = threadIdx.x; t < PTS; t += T) {
     const int q = t >> log2nx, x = t & ((1 << log2nx) - 1);
     const int64_t R = row0 + q;
@@ -246,6 +278,7 @@ k_dsfft_rows(const float2 *__restrict__ grid, int64_t qstride, int nsum, int64_t
       v = make_float4(sg * re.hi, sg * re.lo, sg * im.hi, sg * im.lo);
     }
     sm[pos(x, q)] = v;
+  }
   }
   __syncthreads();
   ds_dif_cta<T>(sm, log2nx, log2S, false, pos, TwGlobal());
@@ -289,6 +322,30 @@ k_dsfft_rows_split(const float2 *__restrict__ grid, int64_t qstride, int nsum, i
     const float sg = ((x + y) & 1) ? -1.f : 1.f;
     return make_float4(sg * re.hi, sg * re.lo, sg * im.hi, sg * im.lo);
   };
+  if (nsum == 1) {
+    constexpr int K = H / 512;
+    float2 ga[K], gb[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      ga[k] = src[threadIdx.x + k * 512];
+      gb[k] = src[threadIdx.x + k * 512 + H];
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int n = threadIdx.x + k * 512;
+      const float sg = ((n + y) & 1) ? -1.f : 1.f;  // n and n + 4096 have the same parity
+      const float4 a = make_float4(sg * ga[k].x, 0.f, sg * ga[k].y, 0.f);
+      const float4 b = make_float4(sg * gb[k].x, 0.f, sg * gb[k].y, 0.f);
+      float4 v;
+      if (half == 0) {
+        v = c_add_nr(a, b);
+      } else {
+        v = c_add_nr(a, c_neg(b));
+        if (n) v = c_mul(v, twiddle(n, LX));
+      }
+      sm[pos(n, 0)] = v;
+    }
+  } else {
   for (int n = threadIdx.x; n < H; n += 512) {
     const float4 a = in(n), b = in(n + H);
     float4 v;
@@ -299,6 +356,7 @@ k_dsfft_rows_split(const float2 *__restrict__ grid, int64_t qstride, int nsum, i
       if (n) v = c_mul(v, twiddle(n, LX));
     }
     sm[pos(n, 0)] = v;
+  }
   }
   __syncthreads();
   ds_dif_cta<512>(sm, LH, 0, false, pos, TwGlobal());
@@ -344,7 +402,8 @@ k_dsfft_cols1(float4 *__restrict__ buf, int log2ny, int log2nx, ColGeom cg, int6
   auto pos = [&](int n, int q) { return (n << log2S) + q; };
   float4 *stw = sm + kColPts;
   stage_twiddles(stw, cg.log2N1);
-  for (int t = threadIdx.x; t < kColPts; t += kColT) sm[t] = p[addr(t >> log2S, t & ((1 << log2S) - 1))];
+  for (int t = threadIdx.x; t < kColPts; t += kColT) cp_async16(sm + t, p + addr(t >> log2S, t & ((1 << log2S) - 1)));
+  cp_async_wait_all();
   __syncthreads();
   ds_dif_cta<kColT>(sm, cg.log2N1, log2S, true, pos, TwShared{stw, cg.log2N1});
   for (int t = threadIdx.x; t < kColPts; t += kColT) {
@@ -374,8 +433,9 @@ k_dsfft_cols2_image(const float4 *__restrict__ buf, int log2ny, int log2nx, ColG
   for (int t = threadIdx.x; t < kColPts; t += kColT) {
     const int n2 = t >> log2S, q = t & S1;
     const int k1 = k1_0 + (q >> cg.log2WC2);
-    sm[t] = p[((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2)];
+    cp_async16(sm + t, p + ((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2));
   }
+  cp_async_wait_all();
   float4 *stw = sm + kColPts;
   stage_twiddles(stw, cg.log2N2);
   __syncthreads();
@@ -430,8 +490,9 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
     for (int t = threadIdx.x; t < kColPts; t += kColT) {
       const int n2 = t >> log2S, q = t & S1;
       const int k1 = k1_0 + (q >> cg.log2WC2);
-      sm[t] = p[((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2)];
+      cp_async16(sm + t, p + ((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2));
     }
+    cp_async_wait_all();
     __syncthreads();
     ds_dif_cta<kColT>(sm, cg.log2N2, log2S, true, pos, TwShared{stw, cg.log2N2});
     const dsf w = ds_from_double(wmean[s]);
