@@ -215,7 +215,8 @@ __device__ __forceinline__ int brev(int k, int log2L) { return (int)(__brev((uns
 // (strides 2, 4 and 16 slots) and the bit-reversed reads of the epilogue then
 // touch eight different 16-byte bank groups per quarter warp.
 // ---------------------------------------------------------------------------
-constexpr int kColT = 512, kColPts = 4096, kColNPT = kColPts / kColT, kColSmem = (kColPts + 128) * 16;
+constexpr int kColT = 512, kColPts = 4096, kColNPT = kColPts / kColT, kColSmem = (kColPts + 256) * 16,
+              kColSmem2 = (2 * kColPts + 128) * 16;
 
 template <int PTS, int T>
 __global__ void __launch_bounds__(T, 1024 / T)
@@ -402,15 +403,19 @@ k_dsfft_cols1(float4 *__restrict__ buf, int log2ny, int log2nx, ColGeom cg, int6
   auto pos = [&](int n, int q) { return (n << log2S) + q; };
   float4 *stw = sm + kColPts;
   stage_twiddles(stw, cg.log2N1);
+  // the 4-step twiddles exp(2 pi i n2 k1 / ny) of this CTA's G1 x N1 outputs
+  float4 *stw2 = stw + 128;
+  for (int e = threadIdx.x; e < (1 << (cg.log2G1 + cg.log2N1)); e += kColT)
+    stw2[e] = twiddle((n2_0 + (e >> cg.log2N1)) * (e & ((1 << cg.log2N1) - 1)), log2ny);
   for (int t = threadIdx.x; t < kColPts; t += kColT) cp_async16(sm + t, p + addr(t >> log2S, t & ((1 << log2S) - 1)));
   cp_async_wait_all();
   __syncthreads();
   ds_dif_cta<kColT>(sm, cg.log2N1, log2S, true, pos, TwShared{stw, cg.log2N1});
   for (int t = threadIdx.x; t < kColPts; t += kColT) {
     const int k1 = t >> log2S, q = t & ((1 << log2S) - 1);
-    const int n2 = n2_0 + (q >> cg.log2WC1);
+    const int g = q >> cg.log2WC1;
     const float4 v = sm[pos(brev(k1, cg.log2N1), q)];
-    p[addr(k1, q)] = (n2 && k1) ? c_mul(v, twiddle(n2 * k1, log2ny)) : v;
+    p[addr(k1, q)] = (n2_0 + g && k1) ? c_mul(v, stw2[(g << cg.log2N1) + k1]) : v;
   }
 }
 
@@ -478,35 +483,42 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
   const int n = 1 << log2nx;
   const dsf c2 = ds_from_double(fov * fov / ((double)n * n));
   auto pos = [&](int k, int q) { return (k << log2S) + q; };
-  float4 *stw = sm + kColPts;
+  // Two tiles: the next slice's tile is copied in while this one is
+  // transformed.
+  float4 *stw = sm + 2 * kColPts;
   stage_twiddles(stw, cg.log2N2);  // ordered before first use by the barrier after the first load
-  dsf acc[kColNPT];
-#pragma unroll
-  for (int m = 0; m < kColNPT; ++m) acc[m] = {0.f, 0.f};
-  for (int64_t pp = p0; pp < p1; ++pp) {
-    const int64_t b = pp / K;
-    const int s = (int)(pp - b * K);
+  auto issue = [&](int64_t pp, float4 *dst) {
     const float4 *p = buf + ((pp - p0) << (log2ny + log2nx));
     for (int t = threadIdx.x; t < kColPts; t += kColT) {
       const int n2 = t >> log2S, q = t & S1;
       const int k1 = k1_0 + (q >> cg.log2WC2);
-      cp_async16(sm + t, p + ((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2));
+      cp_async16(dst + t, p + ((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2));
     }
-    cp_async_wait_all();
-    __syncthreads();
-    ds_dif_cta<kColT>(sm, cg.log2N2, log2S, true, pos, TwShared{stw, cg.log2N2});
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  dsf acc[kColNPT];
+#pragma unroll
+  for (int m = 0; m < kColNPT; ++m) acc[m] = {0.f, 0.f};
+  issue(p0, sm);
+  for (int64_t pp = p0; pp < p1; ++pp) {
+    const int64_t b = pp / K;
+    const int s = (int)(pp - b * K);
+    float4 *cur = ((pp - p0) & 1) ? sm + kColPts : sm;
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();  // this tile has landed, and every thread is done with the other one
+    if (pp + 1 < p1) issue(pp + 1, ((pp - p0) & 1) ? sm : sm + kColPts);
+    ds_dif_cta<kColT>(cur, cg.log2N2, log2S, true, pos, TwShared{stw, cg.log2N2});
     const dsf w = ds_from_double(wmean[s]);
 #pragma unroll
     for (int m = 0; m < kColNPT; ++m) {
       const int t = threadIdx.x + m * kColT;
       const int k2 = t >> log2S, q = t & S1;
-      const float4 v = sm[pos(brev(k2, cg.log2N2), q)];
+      const float4 v = cur[pos(brev(k2, cg.log2N2), q)];
       const int k = k1_0 + (q >> cg.log2WC2) + (k2 << cg.log2N1), x = x0 + (q & WC2);
       const float2 wb = ds_wbeam(ds_wpix(k, x, n, c2), w);
       // Re(wb v) = wb.re v.re - wb.im v.im
       acc[m] = ds_add(acc[m], ds_sub(ds_mul_f({v.x, v.y}, wb.x), ds_mul_f({v.z, v.w}, wb.y)));
     }
-    __syncthreads();  // shared memory is reloaded by the next plane
     if (pp + 1 == p1 || (pp + 1) / K != b) {
       const bool first = p0 <= b * K;
       float2 *out = slots + (b << (log2ny + log2nx));
@@ -568,7 +580,7 @@ static int set_smem() {
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows<4096, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols1, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_image, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
-  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_wstack, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
+  ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_wstack, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem2));
   done.store(1);
   return ARLGPU_OK;
 }
@@ -630,7 +642,7 @@ int dsfft_g2i_wstack(const float2 *grid, int nb, int K, int ny, int nx, double f
   for (int64_t p0 = 0; p0 < nplanes; p0 += G) {
     const int64_t np = std::min(G, nplanes - p0);
     ARL_TRY(rows_cols1(grid, plane, 1, p0, np, ly, lx, cg, b4, st));
-    k_dsfft_cols2_wstack<<<(unsigned)ntile, kColT, kColSmem, st>>>(b4, ly, lx, cg, p0, p0 + np, K, fov, wmean,
+    k_dsfft_cols2_wstack<<<(unsigned)ntile, kColT, kColSmem2, st>>>(b4, ly, lx, cg, p0, p0 + np, K, fov, wmean,
                                                                       reinterpret_cast<float2 *>(image));
     ARL_LAUNCH_CHECK();
     count_launch(1);
