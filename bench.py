@@ -178,9 +178,14 @@ def launch_traffic(kernel, nrows):
 # ---------------------------------------------------------------------------
 def build_context(arl, torch, w, precision, device):
     dv = arl.device
-    im = arl.create_image(npixel=w['npixel'], cellsize=w['cellsize'], frequency=numpy.asarray(w['freqs']),
-                          channel_bandwidth=numpy.array([w['channel_bandwidth']]),
-                          phasecentre=arl.PhaseCentre(0.0, -45.0))
+    if w['kernel'] == 'wproj':
+        # C2: one image channel per visibility channel
+        im = arl.create_image(npixel=w['npixel'], cellsize=w['cellsize'], frequency=numpy.asarray(w['freqs']),
+                              channel_bandwidth=numpy.array([w['channel_bandwidth']]),
+                              phasecentre=arl.PhaseCentre(0.0, -45.0))
+    else:
+        # PSWF workloads: the workload's own (MFS) image with its polarisations
+        im = arl.simulation.workload_image(arl, w)
     if w['kernel'] == 'wproj':
         gcf, cf = arl.create_awterm_convolutionfunction(im, nw=w['nwplanes'], wstep=w['wstep'],
                                                         oversampling=w['oversampling'], support=w['support'],
