@@ -1153,7 +1153,7 @@ __device__ __forceinline__ void fx_add(int *q, int *r, float x, float scale, flo
   }
 }
 
-template <int NPOL, int NW, bool RESID>
+template <int NPOL, int NW, bool RESID, int LPR = 32>
 __global__ void __launch_bounds__(NW * 32)
 k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
           const uint32_t *__restrict__ off, uint32_t chunk, const float2 *__restrict__ vis,
@@ -1174,6 +1174,10 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   // (one chunk per CTA, or a persistent grid of resident CTAs).
   if ((uint64_t)blockIdx.x * chunk >= nvalid) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // LPR lanes per row: 32, or 16 (two rows per warp) for supports <= 8,
+  // where the per-row scalar work would otherwise dominate the taps.
+  constexpr int RPW = 32 / LPR;
+  const int hl = lane & (LPR - 1), half = lane / LPR;
   const int S = g.S, O = g.O;
   const int ps = (int)g.cf_pol_stride;
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
@@ -1187,7 +1191,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   uint32_t pos = c0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
-    if (threadIdx.x == 0) s_next[parity] = pos + NW;  // published by the barrier in seg_box
+    if (threadIdx.x == 0) s_next[parity] = pos + NW * RPW;  // published by the barrier in seg_box
     uint32_t *next_row = &s_next[parity];
     const SegBox box = seg_box<NW, NPOL, true>(sg, pos, smap, sidx, vis, wt, g, s_red[parity]);
     parity ^= 1;
@@ -1211,8 +1215,9 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       rscale = ldexpf(1.f, f);
       rinv = ldexpf(1.f, -f);
     }
-    // Per-warp weight sums, kept by lane 0 as an FP32 value plus its TwoSum
-    // error (FP64 issue is scarce on GB300; the pair is exact to ~1e-14).
+    // Weight sums per row slot (lane 0, and lane 16 with two rows per warp),
+    // kept as an FP32 value plus its TwoSum error (FP64 issue is scarce on
+    // GB300; the pair is exact to ~1e-14).
     float wsum[NPOL], wcomp[NPOL];
 #pragma unroll
     for (int p = 0; p < NPOL; ++p) wsum[p] = wcomp[p] = 0.f;
@@ -1220,24 +1225,28 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
     // time, which balances rows of different support across the warps; each
     // warp holds the next row's index and metadata while it computes the
     // current one.
-    uint32_t r = pos + warp;
+    // rbase is the warp's first row (warp-uniform); this lane's row is
+    // rbase + half.
+    uint32_t rbase = pos + warp * RPW;
     RowMap mnext;
     uint32_t inext = 0;
-    if (r < sg.end) {
-      mnext = smap[r];
-      inext = sidx[r];
+    if (rbase + half < sg.end) {
+      mnext = smap[rbase + half];
+      inext = sidx[rbase + half];
     }
-    while (r < sg.end) {
+    while (rbase < sg.end) {
       const RowMap m = mnext;
       const uint32_t idx = inext;
+      const bool act = rbase + half < sg.end;
       uint32_t rn = 0;
-      if (lane == 0) rn = atomicAdd(next_row, 1u);
+      if (lane == 0) rn = atomicAdd(next_row, (uint32_t)RPW);
       rn = __shfl_sync(0xffffffffu, rn, 0);
-      if (rn < sg.end) {
-        mnext = smap[rn];
-        inext = sidx[rn];
+      if (rn + half < sg.end) {
+        mnext = smap[rn + half];
+        inext = sidx[rn + half];
       }
-      r = rn;
+      rbase = rn;
+      if (!act) continue;
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
       const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
@@ -1249,7 +1258,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         const float w = wt[(size_t)idx * NPOL + p];
         vw[p].x = v.x * w;
         vw[p].y = v.y * w;
-        if (lane == 0) {
+        if (hl == 0) {
           const float s2 = wsum[p] + w, bp = s2 - wsum[p];
           wcomp[p] += (wsum[p] - (s2 - bp)) + (w - bp);
           wsum[p] = s2;
@@ -1258,13 +1267,13 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       const float2 *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
                          ((int64_t)(vf * O + uf) * S + toff) * S + toff;
       const int n = sz * sz, dk = S - sz;
-      const unsigned char *tj = tab + tap_base(sz) + lane;
-      const float2 *kl = kb + lane;
+      const unsigned char *tj = tab + tap_base(sz) + hl;
+      const float2 *kl = kb + hl;
       if (direct) {
         float2 *gl = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
-                     (int64_t)wv * g.nx + wu + lane;
+                     (int64_t)wv * g.nx + wu + hl;
         const int dg = (int)g.nx - sz;
-        for (int t = 0; t + lane < n; t += 32) {
+        for (int t = 0; t + hl < n; t += LPR) {
           const int j = tj[t];
 #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
@@ -1277,7 +1286,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         }
         continue;
       }
-      const int wofs = (wv - sg.v0) * SG + (wu - sg.u0) + lane, dg = SG - sz;
+      const int wofs = (wv - sg.v0) * SG + (wu - sg.u0) + hl, dg = SG - sz;
       // Groups of K warp steps: all tap loads of a group are in flight before
       // its first atomic.  Full groups of four run unmasked; the last 1 to 4
       // steps run as one group of exactly that many, masked per lane only in
@@ -1289,16 +1298,16 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         float2 tp[NPOL][K];
 #pragma unroll
         for (int u = 0; u < K; ++u) {
-          on[u] = !decltype(masked)::value || t + 32 * u + lane < n;
-          j[u] = on[u] ? tj[t + 32 * u] : 0;
+          on[u] = !decltype(masked)::value || t + LPR * u + hl < n;
+          j[u] = on[u] ? tj[t + LPR * u] : 0;
 #pragma unroll
           for (int p = 0; p < NPOL; ++p)
-            tp[p][u] = on[u] ? kl[p * ps + t + 32 * u + j[u] * dk] : make_float2(0.f, 0.f);
+            tp[p][u] = on[u] ? kl[p * ps + t + LPR * u + j[u] * dk] : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < K; ++u) {
           if (!on[u]) break;
-          const int so = wofs + t + 32 * u + j[u] * dg;
+          const int so = wofs + t + LPR * u + j[u] * dg;
 #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
             const float cx = tp[p][u].x * vw[p].x + tp[p][u].y * vw[p].y;  // conj(tap) * vw
@@ -1309,8 +1318,8 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         }
       };
       int t = 0;
-      for (; t + 128 <= n; t += 128) group(t, IntC<4>(), BoolC<false>());
-      switch ((n - t + 31) >> 5) {
+      for (; t + 4 * LPR <= n; t += 4 * LPR) group(t, IntC<4>(), BoolC<false>());
+      switch ((n - t + LPR - 1) / LPR) {
         case 1: group(t, IntC<1>(), BoolC<true>()); break;
         case 2: group(t, IntC<2>(), BoolC<true>()); break;
         case 3: group(t, IntC<3>(), BoolC<true>()); break;
@@ -1318,7 +1327,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         default: break;
       }
     }
-    if (lane == 0) {
+    if (hl == 0) {  // one weight sum per row slot of the warp
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) {
         const double s = (double)wsum[p] + (double)wcomp[p];
@@ -1376,7 +1385,7 @@ __device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsign
 // DUP (FP32 only, degrid_kernel 3): the staged subgrid holds each cell as
 // (re, re, im, im), so a tap is two packed multiply-adds,
 // (sum re t.re, sum re t.im) and (sum im t.re, sum im t.im), instead of four.
-template <typename R, int NPOL, int NW, bool DUP = false>
+template <typename R, int NPOL, int NW, bool DUP = false, int LPR = 32>
 __global__ void __launch_bounds__(NW * 32)
 k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
               const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
@@ -1395,6 +1404,9 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   const uint64_t nchunks = ((uint64_t)nvis + chunk - 1) / chunk;
   if (blockIdx.x >= nchunks) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // LPR lanes per row: 32, or 16 (two rows per warp) for supports <= 8.
+  constexpr int RPW = 32 / LPR;
+  const int hl = lane & (LPR - 1), half = lane / LPR;
   const int S = g.S, O = g.O;
   const int ps = (int)g.cf_pol_stride;
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
@@ -1415,7 +1427,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   uint32_t pos = c0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
-    if (threadIdx.x == 0) s_next[parity] = pos + NW;  // published by the barrier in seg_box
+    if (threadIdx.x == 0) s_next[parity] = pos + NW * RPW;  // published by the barrier in seg_box
     uint32_t *next_row = &s_next[parity];
     // The footprint pass ends in a barrier, which also orders the previous
     // segment's reads of the subgrid before this segment's staging.
@@ -1448,24 +1460,31 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
     // time, which balances rows of different support across the warps; each
     // warp holds the next row's index and metadata while it computes the
     // current one.
-    uint32_t r = pos + warp;
+    // rbase is the warp's first row (warp-uniform); this lane's row is
+    // rbase + half.
+    uint32_t rbase = pos + warp * RPW;
     RowMap mnext;
     uint32_t inext = 0;
-    if (r < sg.end) {
-      mnext = smap[r];
-      inext = sidx[r];
+    if (rbase + half < sg.end) {
+      mnext = smap[rbase + half];
+      inext = sidx[rbase + half];
     }
-    while (r < sg.end) {
+    while (rbase < sg.end) {
       const RowMap m = mnext;
       const uint32_t idx = inext;
+      const bool act = rbase + half < sg.end;
       uint32_t rn = 0;
-      if (lane == 0) rn = atomicAdd(next_row, 1u);
+      if (lane == 0) rn = atomicAdd(next_row, (uint32_t)RPW);
       rn = __shfl_sync(0xffffffffu, rn, 0);
-      if (rn < sg.end) {
-        mnext = smap[rn];
-        inext = sidx[rn];
+      if (rn + half < sg.end) {
+        mnext = smap[rn + half];
+        inext = sidx[rn + half];
       }
-      r = rn;
+      rbase = rn;
+      R ax[NPOL], ay[NPOL];
+#pragma unroll
+      for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = 0;
+      if (act) {
       const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
       const int sz = plane_sz(g, zc);
       const int toff = (S - sz) >> 1;
@@ -1476,20 +1495,17 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       int64_t pstride;
       int dg;
       if (direct) {
-        gl = gplane + (int64_t)wv * g.nx + wu + lane;
+        gl = gplane + (int64_t)wv * g.nx + wu + hl;
         pstride = (int64_t)g.nw * plane_elems;
         dg = (int)g.nx - sz;
       } else {
-        gl = sub + (wv - sg.v0) * SG + (wu - sg.u0) + lane;
+        gl = sub + (wv - sg.v0) * SG + (wu - sg.u0) + hl;
         pstride = SG2;
         dg = SG - sz;
       }
       const int n = sz * sz, dk = S - sz;
-      const unsigned char *tj = tab + tap_base(sz) + lane;
-      const CT *kl = kb + lane;
-      R ax[NPOL], ay[NPOL];
-#pragma unroll
-      for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = 0;
+      const unsigned char *tj = tab + tap_base(sz) + hl;
+      const CT *kl = kb + hl;
       // Groups of K warp steps: every load of a group is in flight before the
       // multiply-adds that use it.  Full groups of four run unmasked; the
       // last 1 to 4 steps run as one group of exactly that many steps, masked
@@ -1500,16 +1516,16 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
         bool on[K];
 #pragma unroll
         for (int u = 0; u < K; ++u) {
-          on[u] = !decltype(masked)::value || t + 32 * u + lane < n;
-          j[u] = on[u] ? tj[t + 32 * u] : 0;
+          on[u] = !decltype(masked)::value || t + LPR * u + hl < n;
+          j[u] = on[u] ? tj[t + LPR * u] : 0;
         }
 #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
           CT tp[K], gv[K];
 #pragma unroll
           for (int u = 0; u < K; ++u) {
-            tp[u] = on[u] ? kl[p * ps + t + 32 * u + j[u] * dk] : czero<CT>();
-            gv[u] = on[u] ? gl[p * pstride + t + 32 * u + j[u] * dg] : czero<CT>();
+            tp[u] = on[u] ? kl[p * ps + t + LPR * u + j[u] * dk] : czero<CT>();
+            gv[u] = on[u] ? gl[p * pstride + t + LPR * u + j[u] * dg] : czero<CT>();
           }
 #pragma unroll
           for (int u = 0; u < K; ++u) {
@@ -1523,15 +1539,15 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       unsigned long long pa[NPOL], pb[NPOL];
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) pa[p] = pb[p] = 0ull;
-      const int wofs4 = (wv - sg.v0) * SG + (wu - sg.u0) + lane;
+      const int wofs4 = (wv - sg.v0) * SG + (wu - sg.u0) + hl;
       auto group2 = [&](int t, auto kk, auto masked) {
         constexpr int K = decltype(kk)::value;
         int j[K];
         bool on[K];
 #pragma unroll
         for (int u = 0; u < K; ++u) {
-          on[u] = !decltype(masked)::value || t + 32 * u + lane < n;
-          j[u] = on[u] ? tj[t + 32 * u] : 0;
+          on[u] = !decltype(masked)::value || t + LPR * u + hl < n;
+          j[u] = on[u] ? tj[t + LPR * u] : 0;
         }
 #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
@@ -1539,9 +1555,9 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
           ulonglong2 gv[K];
 #pragma unroll
           for (int u = 0; u < K; ++u) {
-            tp[u] = on[u] ? *reinterpret_cast<const unsigned long long *>(kl + p * ps + t + 32 * u + j[u] * dk)
+            tp[u] = on[u] ? *reinterpret_cast<const unsigned long long *>(kl + p * ps + t + LPR * u + j[u] * dk)
                           : 0ull;
-            gv[u] = on[u] ? *reinterpret_cast<const ulonglong2 *>(sub4 + p * SG2 + wofs4 + t + 32 * u + j[u] * dg)
+            gv[u] = on[u] ? *reinterpret_cast<const ulonglong2 *>(sub4 + p * SG2 + wofs4 + t + LPR * u + j[u] * dg)
                           : make_ulonglong2(0ull, 0ull);
           }
 #pragma unroll
@@ -1553,8 +1569,8 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       };
       int t = 0;
       if (DUP && !direct) {
-        for (; t + 128 <= n; t += 128) group2(t, IntC<4>(), BoolC<false>());
-        switch ((n - t + 31) >> 5) {
+        for (; t + 4 * LPR <= n; t += 4 * LPR) group2(t, IntC<4>(), BoolC<false>());
+        switch ((n - t + LPR - 1) / LPR) {
           case 1: group2(t, IntC<1>(), BoolC<true>()); break;
           case 2: group2(t, IntC<2>(), BoolC<true>()); break;
           case 3: group2(t, IntC<3>(), BoolC<true>()); break;
@@ -1569,8 +1585,8 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
           ay[p] = (R)(a2.y + b2.x);
         }
       } else {
-        for (; t + 128 <= n; t += 128) group(t, IntC<4>(), BoolC<false>());
-        switch ((n - t + 31) >> 5) {
+        for (; t + 4 * LPR <= n; t += 4 * LPR) group(t, IntC<4>(), BoolC<false>());
+        switch ((n - t + LPR - 1) / LPR) {
           case 1: group(t, IntC<1>(), BoolC<true>()); break;
           case 2: group(t, IntC<2>(), BoolC<true>()); break;
           case 3: group(t, IntC<3>(), BoolC<true>()); break;
@@ -1578,14 +1594,16 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
           default: break;
         }
       }
+      }  // act
+      // Reduce over each row's LPR lanes (all lanes take part).
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) {
         R sx = ax[p], sy = ay[p];
-        for (int o = 16; o > 0; o >>= 1) {
+        for (int o = LPR / 2; o > 0; o >>= 1) {
           sx += __shfl_xor_sync(0xffffffffu, sx, o);
           sy += __shfl_xor_sync(0xffffffffu, sy, o);
         }
-        if (lane == p) {
+        if (act && hl == p) {
           CT out;
           out.x = sx;
           out.y = sy;
@@ -1820,12 +1838,18 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
   void (*kern)(Geom, const RowMap *, const uint32_t *, const uint32_t *, uint32_t, const float2 *, const float *,
                const float2 *, float2 *, double *);
+  // Supports up to 8 (64 taps): two rows per warp, 16 lanes each.
+  const bool two = g.S <= 8;
   if (resid)
-    kern = g.npol == 1 ? k_grid_fx<1, kWarps, true> : g.npol == 2 ? k_grid_fx<2, kWarps, true>
-                                                                   : k_grid_fx<4, kWarps, true>;
+    kern = two ? (g.npol == 1 ? k_grid_fx<1, kWarps, true, 16> : g.npol == 2 ? k_grid_fx<2, kWarps, true, 16>
+                                                                            : k_grid_fx<4, kWarps, true, 16>)
+               : (g.npol == 1 ? k_grid_fx<1, kWarps, true> : g.npol == 2 ? k_grid_fx<2, kWarps, true>
+                                                                        : k_grid_fx<4, kWarps, true>);
   else
-    kern = g.npol == 1 ? k_grid_fx<1, kWarps, false> : g.npol == 2 ? k_grid_fx<2, kWarps, false>
-                                                                    : k_grid_fx<4, kWarps, false>;
+    kern = two ? (g.npol == 1 ? k_grid_fx<1, kWarps, false, 16> : g.npol == 2 ? k_grid_fx<2, kWarps, false, 16>
+                                                                             : k_grid_fx<4, kWarps, false, 16>)
+               : (g.npol == 1 ? k_grid_fx<1, kWarps, false> : g.npol == 2 ? k_grid_fx<2, kWarps, false>
+                                                                         : k_grid_fx<4, kWarps, false>);
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t chunk = chunk_rows();
   const unsigned blocks = chunk_grid(kern, smem, nvis, chunk);
@@ -1896,9 +1920,15 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
     smem += tap_table_bytes(g.S);
   } else if (g_tune_degrid_kernel.load() == 3) {  // FP32: packed multiply-adds
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
-    kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps, sizeof(R) == 4>
-                       : g.npol == 2 ? k_degrid_lean<R, 2, kWarps, sizeof(R) == 4>
-                                     : k_degrid_lean<R, 4, kWarps, sizeof(R) == 4>;
+    // Supports up to 8 (64 taps): two rows per warp, 16 lanes each.
+    if (g.S <= 8)
+      kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps, sizeof(R) == 4, 16>
+                         : g.npol == 2 ? k_degrid_lean<R, 2, kWarps, sizeof(R) == 4, 16>
+                                       : k_degrid_lean<R, 4, kWarps, sizeof(R) == 4, 16>;
+    else
+      kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps, sizeof(R) == 4>
+                         : g.npol == 2 ? k_degrid_lean<R, 2, kWarps, sizeof(R) == 4>
+                                       : k_degrid_lean<R, 4, kWarps, sizeof(R) == 4>;
     smem = (size_t)g.npol * g.SG * g.SG * 16 + tap_table_bytes(g.S);
   }
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "degridder needs %zu bytes of shared memory", smem);
