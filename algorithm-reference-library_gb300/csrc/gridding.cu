@@ -54,6 +54,8 @@ static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automat
 static std::atomic<int> g_tune_chunk{512};        // sorted rows per gridder / degridder CTA
 static std::atomic<int> g_tune_persistent{0};     // lean / fixed-point kernels: 1 = one resident grid looping over chunks
 static std::atomic<int> g_tune_dsfft{1};          // FP32C inverse transforms: 1 = double-single FFT, 0 = cuFFT FP64
+static std::atomic<int> g_tune_small_rows{2};     // rows per warp in the FP32C gridder when S <= 8
+static std::atomic<int> g_tune_small_rows_dg{4};  // rows per warp in the packed degridder when S <= 8
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 bool tune_dsfft() { return g_tune_dsfft.load() != 0; }
 
@@ -1838,18 +1840,17 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
   void (*kern)(Geom, const RowMap *, const uint32_t *, const uint32_t *, uint32_t, const float2 *, const float *,
                const float2 *, float2 *, double *);
-  // Supports up to 8 (64 taps): two rows per warp, 16 lanes each.
-  const bool two = g.S <= 8;
-  if (resid)
-    kern = two ? (g.npol == 1 ? k_grid_fx<1, kWarps, true, 16> : g.npol == 2 ? k_grid_fx<2, kWarps, true, 16>
-                                                                            : k_grid_fx<4, kWarps, true, 16>)
-               : (g.npol == 1 ? k_grid_fx<1, kWarps, true> : g.npol == 2 ? k_grid_fx<2, kWarps, true>
-                                                                        : k_grid_fx<4, kWarps, true>);
-  else
-    kern = two ? (g.npol == 1 ? k_grid_fx<1, kWarps, false, 16> : g.npol == 2 ? k_grid_fx<2, kWarps, false, 16>
-                                                                             : k_grid_fx<4, kWarps, false, 16>)
-               : (g.npol == 1 ? k_grid_fx<1, kWarps, false> : g.npol == 2 ? k_grid_fx<2, kWarps, false>
-                                                                         : k_grid_fx<4, kWarps, false>);
+  // Supports up to 8 (64 taps): several rows per warp (tuning small_rows).
+  const int rpw = g.S <= 8 ? g_tune_small_rows.load() : 1;
+  auto pick = [&](auto resid_c) {
+    constexpr bool RS = decltype(resid_c)::value;
+    if (rpw == 4) return g.npol == 1 ? k_grid_fx<1, kWarps, RS, 8> : g.npol == 2 ? k_grid_fx<2, kWarps, RS, 8>
+                                                                                 : k_grid_fx<4, kWarps, RS, 8>;
+    if (rpw == 2) return g.npol == 1 ? k_grid_fx<1, kWarps, RS, 16> : g.npol == 2 ? k_grid_fx<2, kWarps, RS, 16>
+                                                                                  : k_grid_fx<4, kWarps, RS, 16>;
+    return g.npol == 1 ? k_grid_fx<1, kWarps, RS> : g.npol == 2 ? k_grid_fx<2, kWarps, RS> : k_grid_fx<4, kWarps, RS>;
+  };
+  kern = resid ? pick(BoolC<true>()) : pick(BoolC<false>());
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint32_t chunk = chunk_rows();
   const unsigned blocks = chunk_grid(kern, smem, nvis, chunk);
@@ -1920,8 +1921,13 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
     smem += tap_table_bytes(g.S);
   } else if (g_tune_degrid_kernel.load() == 3) {  // FP32: packed multiply-adds
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
-    // Supports up to 8 (64 taps): two rows per warp, 16 lanes each.
-    if (g.S <= 8)
+    // Supports up to 8 (64 taps): several rows per warp (tuning small_rows_degrid).
+    const int rpw = g.S <= 8 ? g_tune_small_rows_dg.load() : 1;
+    if (rpw == 4)
+      kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps, sizeof(R) == 4, 8>
+                         : g.npol == 2 ? k_degrid_lean<R, 2, kWarps, sizeof(R) == 4, 8>
+                                       : k_degrid_lean<R, 4, kWarps, sizeof(R) == 4, 8>;
+    else if (rpw == 2)
       kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps, sizeof(R) == 4, 16>
                          : g.npol == 2 ? k_degrid_lean<R, 2, kWarps, sizeof(R) == 4, 16>
                                        : k_degrid_lean<R, 4, kWarps, sizeof(R) == 4, 16>;
@@ -2081,6 +2087,8 @@ extern "C" int arlgpu_set_tuning(const char *key, int value) {
   else if (k == "chunk" && value >= 32 && value <= (1 << 20)) g_tune_chunk = value;
   else if (k == "persistent" && (value == 0 || value == 1)) g_tune_persistent = value;
   else if (k == "dsfft" && (value == 0 || value == 1)) g_tune_dsfft = value;
+  else if (k == "small_rows" && (value == 1 || value == 2 || value == 4)) g_tune_small_rows = value;
+  else if (k == "small_rows_degrid" && (value == 1 || value == 2 || value == 4)) g_tune_small_rows_dg = value;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key or value: %s = %d", key, value);
   return ARLGPU_OK;
 }
@@ -2094,6 +2102,8 @@ extern "C" int arlgpu_get_tuning(const char *key, int *value) {
   else if (k == "chunk") *value = g_tune_chunk;
   else if (k == "persistent") *value = g_tune_persistent;
   else if (k == "dsfft") *value = g_tune_dsfft;
+  else if (k == "small_rows") *value = g_tune_small_rows;
+  else if (k == "small_rows_degrid") *value = g_tune_small_rows_dg;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key: %s", key);
   return ARLGPU_OK;
 }

@@ -29,7 +29,7 @@ def set_tuning(**kw):
 def get_tuning():
     lib = nat.load()
     out = {}
-    for k in ('grid_kernel', 'degrid_kernel', 'subgrid', 'chunk', 'persistent', 'dsfft'):
+    for k in ('grid_kernel', 'degrid_kernel', 'subgrid', 'chunk', 'persistent', 'dsfft', 'small_rows', 'small_rows_degrid'):
         v = ctypes.c_int()
         nat.check(lib.arlgpu_get_tuning(k.encode(), ctypes.byref(v)))
         out[k] = v.value

@@ -107,6 +107,9 @@ unsigned long long arlgpu_kernel_launches(void);
  *   "dsfft"         FP32C inverse transforms (invert_2d and w-stacking): 1 = double-single
  *                   FFT on the FP32 pipes for power-of-two sizes 64..8192 (default),
  *                   0 = cuFFT complex128
+ *   "small_rows"    rows per warp (1, 2 or 4; default 2) in the FP32C fixed-point gridder when the
+ *                   largest support is at most 8 (64 taps)
+ *   "small_rows_degrid"  the same for the packed degridder (default 4)
  * No reference counterpart (ARL has one Python loop per function). */
 int arlgpu_set_tuning(const char *key, int value);
 int arlgpu_get_tuning(const char *key, int *value);

@@ -377,3 +377,27 @@ def test_kernel_variants_vs_oracle(arl, oracle, grid_kernel, degrid_kernel, subg
             assert rel(out.vis, oracle.degrid_vec(g_ref, maps, cf.data)) < TOL[precision]
     finally:
         arl.tune.set_tuning(**before)
+
+
+@pytest.mark.parametrize('small_rows,small_rows_degrid', [(1, 1), (2, 2), (4, 4), (2, 4)])
+@pytest.mark.parametrize('npol', [1, 2, 4])
+def test_small_support_rows_per_warp_vs_oracle(arl, oracle, small_rows, small_rows_degrid, npol):
+    """Supports up to 8 run several rows per warp (16 or 8 lanes each); w-kernel
+    planes of supports 8, 6 and 4 put rows of different supports side by side
+    in one warp.  Against the oracle, default kernels otherwise."""
+    before = arl.tune.get_tuning()
+    try:
+        arl.tune.set_tuning(small_rows=small_rows, small_rows_degrid=small_rows_degrid)
+        for precision in ('fp64', 'fp32c'):
+            rng = numpy.random.default_rng(17 + npol)
+            im, cf, vis, maps, gax = _random_case(arl, oracle, rng, 128, 4e-3, 8, 8, 5000, 2, npol, 3, 20.0, True)
+            arl.set_plane_support(cf, [8, 6, 4])
+            gd, sumwt = arl.grid_visibility_to_griddata(vis, arl.create_griddata_from_image(im), cf,
+                                                        precision=precision)
+            g_ref, sw_ref = oracle.grid_vec(vis.vis, vis.imaging_weight, maps, cf.data, gax['shape'])
+            assert rel(gd.data, g_ref) < TOL[precision]
+            assert rel(sumwt, sw_ref) < TOLW[precision]
+            out = arl.degrid_visibility_from_griddata(vis, gd, cf, precision=precision)
+            assert rel(out.vis, oracle.degrid_vec(g_ref, maps, cf.data)) < TOL[precision]
+    finally:
+        arl.tune.set_tuning(**before)
