@@ -216,7 +216,7 @@ __device__ __forceinline__ int brev(int k, int log2L) { return (int)(__brev((uns
 // touch eight different 16-byte bank groups per quarter warp.
 // ---------------------------------------------------------------------------
 constexpr int kColT = 512, kColPts = 4096, kColNPT = kColPts / kColT, kColSmem = (kColPts + 256) * 16,
-              kColSmem2 = (2 * kColPts + 128) * 16;
+              kColSmem2 = (2 * kColPts + 128) * 16 + kColPts * 8;
 
 template <int PTS, int T>
 __global__ void __launch_bounds__(T, 1024 / T)
@@ -487,6 +487,7 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
   // transformed.
   float4 *stw = sm + 2 * kColPts;
   stage_twiddles(stw, cg.log2N2);  // ordered before first use by the barrier after the first load
+  float2 *snt = reinterpret_cast<float2 *>(stw + 128);  // kColPts per-pixel w-screen terms
   auto issue = [&](int64_t pp, float4 *dst) {
     const float4 *p = buf + ((pp - p0) << (log2ny + log2nx));
     for (int t = threadIdx.x; t < kColPts; t += kColT) {
@@ -514,8 +515,18 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
       const int t = threadIdx.x + m * kColT;
       const int k2 = t >> log2S, q = t & S1;
       const float4 v = cur[pos(brev(k2, cg.log2N2), q)];
-      const int k = k1_0 + (q >> cg.log2WC2) + (k2 << cg.log2N1), x = x0 + (q & WC2);
-      const float2 wb = ds_wbeam(ds_wpix(k, x, n, c2), w);
+      // w-screen term of this thread's pixel t, formed at the first slice and
+      // kept in the thread's own shared slot: nterm, or hi = -1 where r^2 >= 1
+      if (pp == p0) {
+        const int k = k1_0 + (q >> cg.log2WC2) + (k2 << cg.log2N1), x = x0 + (q & WC2);
+        const DsPix px = ds_wpix(k, x, n, c2);
+        snt[t] = px.state == 2 ? make_float2(-1.f, 0.f) : make_float2(px.nterm.hi, px.nterm.lo);
+      }
+      const float2 nt = snt[t];
+      DsPix px;
+      px.state = nt.x < 0.f ? 2 : 1;
+      px.nterm = {nt.x, nt.y};
+      const float2 wb = ds_wbeam(px, w);
       // Re(wb v) = wb.re v.re - wb.im v.im
       acc[m] = ds_add(acc[m], ds_sub(ds_mul_f({v.x, v.y}, wb.x), ds_mul_f({v.z, v.w}, wb.y)));
     }

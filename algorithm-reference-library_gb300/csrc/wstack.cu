@@ -195,10 +195,10 @@ static int exec(cufftHandle h, CT *d, int dir) {
   return r == CUFFT_SUCCESS ? ARLGPU_OK : fail(ARLGPU_ERR_CUFFT, "cuFFT exec failed (%d)", (int)r);
 }
 
-// Planes per cuFFT call: batches of at most kGroupBytes of complex128, so the
-// FFT scratch (fftbuf) and cuFFT's own work area stay bounded for large grids
-// (an 8192^2 plane is 1 GiB in complex128).
-constexpr int64_t kGroupBytes = (int64_t)2 << 30;
+// Planes per transform group: at most kGroupBytes of 16-byte cells (complex128
+// or double-single complex), so the FFT scratch (fftbuf) and cuFFT's own work
+// area stay bounded for large grids (an 8192^2 plane is 1 GiB).
+constexpr int64_t kGroupBytes = (int64_t)4 << 30;
 
 int64_t group_planes(int64_t nplanes, int ny, int nx) {
   int64_t g = kGroupBytes / ((int64_t)ny * nx * (int64_t)sizeof(double2));
