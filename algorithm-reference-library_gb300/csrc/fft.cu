@@ -8,9 +8,12 @@
 //
 // The centred transform fftshift(F(ifftshift(a))) for even N equals
 // s * chk * F(chk * a) with chk[y, x] = (-1)^(x + y) and s = (-1)^(nx/2 + ny/2),
-// so the shifts cost nothing: the sign flips are fused into the pre- and
-// post-passes that also sum the w-planes, apply the grid correction and the
-// sumwt normalisation.  The transform itself is cuFFT (batched over chan, pol).
+// and also F(z) with z[y, x] = chk(y, x) a[y + ny/2, x + nx/2] (indices mod N),
+// so the shifts cost nothing: the sign flips are fused into the passes that
+// also sum the w-planes, apply the grid correction and the sumwt
+// normalisation (the forward direction needs no pass after the transform).
+// The transforms are cuFFT (batched over chan, pol) or, for the FP32C
+// inverse, the double-single transform of dsfft.cu.
 #include <cufft.h>
 
 #include <map>
@@ -114,7 +117,9 @@ __global__ void k_post_g2i(const double2 *__restrict__ buf, int nb, int ny, int 
   }
 }
 
-// grid plane 0 of each (chan, pol): chk * image * gcf
+// grid plane 0 of each (chan, pol), ready for a plain forward transform: the
+// centred transform of an even-sized a equals F(z) with
+// z[y, x] = chk(y, x) a[(y + ny/2) mod ny, (x + nx/2) mod nx], a = image * gcf.
 template <typename CT>
 __global__ void k_pre_i2g(const double *__restrict__ image, const double *__restrict__ gcf, int nb, int nw, int ny,
                           int nx, CT *__restrict__ grid) {
@@ -123,24 +128,23 @@ __global__ void k_pre_i2g(const double *__restrict__ image, const double *__rest
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / plane, yx = i - b * plane;
     const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
-    grid[b * nw * plane + yx] = cmk<CT>(image[i] * gcf[i] * (double)chk_sign(y, x), 0.0);
+    const int ys = y + ny / 2 - (y >= ny - ny / 2 ? ny : 0), xs = x + nx / 2 - (x >= nx - nx / 2 ? nx : 0);
+    const int64_t src = b * plane + (int64_t)ys * nx + xs;
+    grid[b * nw * plane + yx] = cmk<CT>(image[src] * gcf[src] * (double)chk_sign(y, x), 0.0);
   }
 }
 
-// grid[b, z] = grid[b, 0] * chk * s for every z
+// grid[b, z] = grid[b, 0] for z = 1 .. nw - 1 (every w-plane holds the same
+// transform, as ARL's fft_image_to_griddata writes it)
 template <typename CT>
-__global__ void k_post_i2g(CT *__restrict__ grid, int nb, int nw, int ny, int nx, float s) {
+__global__ void k_post_i2g(CT *__restrict__ grid, int nb, int nw, int ny, int nx) {
   const int64_t plane = (int64_t)ny * nx;
   const int64_t total = (int64_t)nb * plane;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / plane, yx = i - b * plane;
-    const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
     CT *p = grid + b * nw * plane + yx;
-    CT v = p[0];
-    const float sg = chk_sign(y, x) * s;
-    v.x *= sg;
-    v.y *= sg;
-    for (int z = 0; z < nw; ++z) p[z * plane] = v;
+    const CT v = p[0];
+    for (int z = 1; z < nw; ++z) p[z * plane] = v;
   }
 }
 
@@ -203,10 +207,11 @@ static int i2g(const double *image, const double *gcf, const arlgpu_grid_desc *g
   cufftResult r = cufftSetStream(h, st);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
   ARL_TRY(exec_c2c<CT>(h, grid, CUFFT_FORWARD));
-  const float s = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
-  k_post_i2g<CT><<<grid_blocks(total), 256, 0, st>>>(grid, nb, nw, ny, nx, s);
-  count_launch(1);
-  ARL_LAUNCH_CHECK();
+  if (nw > 1) {
+    k_post_i2g<CT><<<grid_blocks(total), 256, 0, st>>>(grid, nb, nw, ny, nx);
+    count_launch(1);
+    ARL_LAUNCH_CHECK();
+  }
   return ARLGPU_OK;
 }
 

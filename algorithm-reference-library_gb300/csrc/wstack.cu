@@ -127,7 +127,11 @@ __global__ void k_wstack_combine(const double2 *__restrict__ buf, int64_t p0, in
   }
 }
 
-// grid[b, s] = chk * conj(wb_s) * image * gcf  (complex), for every slice s.
+// Plane s of image b, ready for a plain forward transform: the centred
+// transform fftshift(F(ifftshift(a))) of an even-sized a equals F(z) with
+// z[y, x] = chk(y, x) a[(y + ny/2) mod ny, (x + nx/2) mod nx], so
+//   grid[b, s, y, x] = chk(y, x) conj(wb_s) image gcf   at the shifted pixel
+// and no pass after the transform is needed.
 // FP64 path: FP64 w-screen.  FP32C path: double-single w-screen (no FP64
 // square root or per-slice FP64 phase), FP32 sincospi.
 __global__ void k_wstack_pre_predict64(const double *__restrict__ image, const double *__restrict__ gcf, int nb, int K,
@@ -137,8 +141,10 @@ __global__ void k_wstack_pre_predict64(const double *__restrict__ image, const d
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / plane, yx = i - b * plane;
     const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
-    const double m = image[i] * gcf[i] * (((x + y) & 1) ? -1.0 : 1.0);
-    const Pix px = wpix(y, x, nx, fov);
+    const int ys = y + ny / 2 - (y >= ny - ny / 2 ? ny : 0), xs = x + nx / 2 - (x >= nx - nx / 2 ? nx : 0);
+    const int64_t src = b * plane + (int64_t)ys * nx + xs;
+    const double m = image[src] * gcf[src] * (((x + y) & 1) ? -1.0 : 1.0);
+    const Pix px = wpix(ys, xs, nx, fov);
     for (int s = 0; s < K; ++s) {
       const double2 wb = wb64(px, wmean[s]);
       grid[(b * K + s) * plane + yx] = make_double2(wb.x * m, -wb.y * m);
@@ -157,27 +163,14 @@ __global__ void k_wstack_pre_predict32(const double *__restrict__ image, const d
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = i / plane, yx = i - b * plane;
     const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
-    const float m = (float)(image[i] * gcf[i]) * (((x + y) & 1) ? -1.f : 1.f);
-    const DsPix px = ds_wpix(y, x, nx, c2);
+    const int ys = y + ny / 2 - (y >= ny - ny / 2 ? ny : 0), xs = x + nx / 2 - (x >= nx - nx / 2 ? nx : 0);
+    const int64_t src = b * plane + (int64_t)ys * nx + xs;
+    const float m = (float)(image[src] * gcf[src]) * (((x + y) & 1) ? -1.f : 1.f);
+    const DsPix px = ds_wpix(ys, xs, nx, c2);
     for (int s = 0; s < K; ++s) {
       const float2 wb = ds_wbeam(px, s_w[s]);
       grid[(b * K + s) * plane + yx] = make_float2(wb.x * m, -wb.y * m);
     }
-  }
-}
-
-// post-predict: chk * s0 on every plane
-template <typename CT>
-__global__ void k_chk_scale(CT *grid, int64_t nplanes, int ny, int nx, float s0) {
-  const int64_t plane = (int64_t)ny * nx, tot = nplanes * plane;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t yx = i % plane;
-    const int y = (int)(yx / nx), x = (int)(yx - (int64_t)y * nx);
-    const float sg = (((x + y) & 1) ? -1.f : 1.f) * s0;
-    CT v = grid[i];
-    v.x *= sg;
-    v.y *= sg;
-    grid[i] = v;
   }
 }
 
@@ -257,7 +250,6 @@ static int i2g(const double *image, const double *gcf, const double *wmean, doub
   ARL_LAUNCH_CHECK();
   count_launch(1);
   const int64_t G = group_planes(nplanes, ny, nx);
-  const float s0 = (((nx / 2) + (ny / 2)) & 1) ? -1.f : 1.f;
   for (int64_t p0 = 0; p0 < nplanes; p0 += G) {
     const int64_t np = std::min(G, nplanes - p0);
     cufftHandle h;
@@ -265,9 +257,6 @@ static int i2g(const double *image, const double *gcf, const double *wmean, doub
     cufftResult r = cufftSetStream(h, st);
     if (r != CUFFT_SUCCESS) return fail(ARLGPU_ERR_CUFFT, "cufftSetStream failed (%d)", (int)r);
     ARL_TRY(exec<CT>(h, grid + p0 * plane, CUFFT_FORWARD));
-    k_chk_scale<CT><<<nblk(np * plane), 256, 0, st>>>(grid + p0 * plane, np, ny, nx, s0);
-    ARL_LAUNCH_CHECK();
-    count_launch(1);
   }
   return ARLGPU_OK;
 }
