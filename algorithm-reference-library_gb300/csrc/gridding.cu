@@ -1176,10 +1176,6 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   // (one chunk per CTA, or a persistent grid of resident CTAs).
   if ((uint64_t)blockIdx.x * chunk >= nvalid) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // LPR lanes per row: 32, or 16 (two rows per warp) for supports <= 8,
-  // where the per-row scalar work would otherwise dominate the taps.
-  constexpr int RPW = 32 / LPR;
-  const int hl = lane & (LPR - 1), half = lane / LPR;
   const int S = g.S, O = g.O;
   const int ps = (int)g.cf_pol_stride;
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
@@ -1193,7 +1189,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   uint32_t pos = c0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
-    if (threadIdx.x == 0) s_next[parity] = pos + NW * RPW;  // published by the barrier in seg_box
+    if (threadIdx.x == 0) s_next[parity] = pos;  // published by the barrier in seg_box
     uint32_t *next_row = &s_next[parity];
     const SegBox box = seg_box<NW, NPOL, true>(sg, pos, smap, sidx, vis, wt, g, s_red[parity]);
     parity ^= 1;
@@ -1223,113 +1219,130 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
     float wsum[NPOL], wcomp[NPOL];
 #pragma unroll
     for (int p = 0; p < NPOL; ++p) wsum[p] = wcomp[p] = 0.f;
-    // Rows after each warp's first come from a shared counter, one at a
-    // time, which balances rows of different support across the warps; each
-    // warp holds the next row's index and metadata while it computes the
-    // current one.
-    // rbase is the warp's first row (warp-uniform); this lane's row is
-    // rbase + half.
-    uint32_t rbase = pos + warp * RPW;
-    RowMap mnext;
-    uint32_t inext = 0;
-    if (rbase + half < sg.end) {
-      mnext = smap[rbase + half];
-      inext = sidx[rbase + half];
-    }
-    while (rbase < sg.end) {
-      const RowMap m = mnext;
-      const uint32_t idx = inext;
-      const bool act = rbase + half < sg.end;
-      uint32_t rn = 0;
-      if (lane == 0) rn = atomicAdd(next_row, (uint32_t)RPW);
-      rn = __shfl_sync(0xffffffffu, rn, 0);
-      if (rn + half < sg.end) {
-        mnext = smap[rn + half];
-        inext = sidx[rn + half];
+    // Rows per warp: LP lanes per row; the default one-row-per-warp
+    // variant runs a segment two rows per warp when its largest support is
+    // at most 16 (256 taps), sharing the per-row set-up between two rows.
+    auto row_loop = [&](auto lpr_c) {
+      constexpr int LP = decltype(lpr_c)::value;
+      constexpr int RP = 32 / LP;
+      const int hl = lane & (LP - 1), half = lane / LP;
+      // Rows come from a shared counter, RP at a time (one per row slot of
+      // the warp), which balances rows of different support across the warps;
+      // each warp holds its next rows' indices and metadata while it computes
+      // the current ones.  rbase is warp-uniform; this lane's row is
+      // rbase + half.
+      uint32_t rbase = 0;
+      if (lane == 0) rbase = atomicAdd(next_row, (uint32_t)RP);
+      rbase = __shfl_sync(0xffffffffu, rbase, 0);
+      RowMap mnext;
+      uint32_t inext = 0;
+      if (rbase + half < sg.end) {
+        mnext = smap[rbase + half];
+        inext = sidx[rbase + half];
       }
-      rbase = rn;
-      if (!act) continue;
-      const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = plane_sz(g, zc);
-      const int toff = (S - sz) >> 1;
-      const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
-      float2 vw[NPOL];
-#pragma unroll
-      for (int p = 0; p < NPOL; ++p) {
-        const float2 v = vis[(size_t)idx * NPOL + p];
-        const float w = wt[(size_t)idx * NPOL + p];
-        vw[p].x = v.x * w;
-        vw[p].y = v.y * w;
-        if (hl == 0) {
-          const float s2 = wsum[p] + w, bp = s2 - wsum[p];
-          wcomp[p] += (wsum[p] - (s2 - bp)) + (w - bp);
-          wsum[p] = s2;
+      while (rbase < sg.end) {
+        const RowMap m = mnext;
+        const uint32_t idx = inext;
+        const bool act = rbase + half < sg.end;
+        uint32_t rn = 0;
+        if (lane == 0) rn = atomicAdd(next_row, (uint32_t)RP);
+        rn = __shfl_sync(0xffffffffu, rn, 0);
+        if (rn + half < sg.end) {
+          mnext = smap[rn + half];
+          inext = sidx[rn + half];
         }
-      }
-      const float2 *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
-                         ((int64_t)(vf * O + uf) * S + toff) * S + toff;
-      const int n = sz * sz, dk = S - sz;
-      const unsigned char *tj = tab + tap_base(sz) + hl;
-      const float2 *kl = kb + hl;
-      if (direct) {
-        float2 *gl = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
-                     (int64_t)wv * g.nx + wu + hl;
-        const int dg = (int)g.nx - sz;
-        for (int t = 0; t + hl < n; t += LPR) {
-          const int j = tj[t];
-#pragma unroll
-          for (int p = 0; p < NPOL; ++p) {
-            const float2 tp = kl[p * ps + t + j * dk];
-            float2 c;
-            c.x = tp.x * vw[p].x + tp.y * vw[p].y;
-            c.y = tp.x * vw[p].y - tp.y * vw[p].x;
-            red_global<float2>(gl + (int64_t)p * g.nw * plane_elems + t + j * dg, c);
+        rbase = rn;
+        if (!act) continue;
+        const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+        const int sz = plane_sz(g, zc);
+        const int toff = (S - sz) >> 1;
+        const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
+        float2 vw[NPOL];
+  #pragma unroll
+        for (int p = 0; p < NPOL; ++p) {
+          const float2 v = vis[(size_t)idx * NPOL + p];
+          const float w = wt[(size_t)idx * NPOL + p];
+          vw[p].x = v.x * w;
+          vw[p].y = v.y * w;
+          if (hl == 0) {
+            const float s2 = wsum[p] + w, bp = s2 - wsum[p];
+            wcomp[p] += (wsum[p] - (s2 - bp)) + (w - bp);
+            wsum[p] = s2;
           }
         }
-        continue;
-      }
-      const int wofs = (wv - sg.v0) * SG + (wu - sg.u0) + hl, dg = SG - sz;
-      // Groups of K warp steps: all tap loads of a group are in flight before
-      // its first atomic.  Full groups of four run unmasked; the last 1 to 4
-      // steps run as one group of exactly that many, masked per lane only in
-      // its partial last step.
-      auto group = [&](int t, auto kk, auto masked) {
-        constexpr int K = decltype(kk)::value;
-        int j[K];
-        bool on[K];
-        float2 tp[NPOL][K];
-#pragma unroll
-        for (int u = 0; u < K; ++u) {
-          on[u] = !decltype(masked)::value || t + LPR * u + hl < n;
-          j[u] = on[u] ? tj[t + LPR * u] : 0;
-#pragma unroll
-          for (int p = 0; p < NPOL; ++p)
-            tp[p][u] = on[u] ? kl[p * ps + t + LPR * u + j[u] * dk] : make_float2(0.f, 0.f);
-        }
-#pragma unroll
-        for (int u = 0; u < K; ++u) {
-          if (!on[u]) break;
-          const int so = wofs + t + LPR * u + j[u] * dg;
-#pragma unroll
-          for (int p = 0; p < NPOL; ++p) {
-            const float cx = tp[p][u].x * vw[p].x + tp[p][u].y * vw[p].y;  // conj(tap) * vw
-            const float cy = tp[p][u].x * vw[p].y - tp[p][u].y * vw[p].x;
-            fx_add<RESID>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
-            fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
+        const float2 *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                           ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+        const int n = sz * sz, dk = S - sz;
+        const unsigned char *tj = tab + tap_base(sz) + hl;
+        const float2 *kl = kb + hl;
+        if (direct) {
+          float2 *gl = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems +
+                       (int64_t)wv * g.nx + wu + hl;
+          const int dg = (int)g.nx - sz;
+          for (int t = 0; t + hl < n; t += LP) {
+            const int j = tj[t];
+  #pragma unroll
+            for (int p = 0; p < NPOL; ++p) {
+              const float2 tp = kl[p * ps + t + j * dk];
+              float2 c;
+              c.x = tp.x * vw[p].x + tp.y * vw[p].y;
+              c.y = tp.x * vw[p].y - tp.y * vw[p].x;
+              red_global<float2>(gl + (int64_t)p * g.nw * plane_elems + t + j * dg, c);
+            }
           }
+          continue;
         }
-      };
-      int t = 0;
-      for (; t + 4 * LPR <= n; t += 4 * LPR) group(t, IntC<4>(), BoolC<false>());
-      switch ((n - t + LPR - 1) / LPR) {
-        case 1: group(t, IntC<1>(), BoolC<true>()); break;
-        case 2: group(t, IntC<2>(), BoolC<true>()); break;
-        case 3: group(t, IntC<3>(), BoolC<true>()); break;
-        case 4: group(t, IntC<4>(), BoolC<true>()); break;
-        default: break;
+        const int wofs = (wv - sg.v0) * SG + (wu - sg.u0) + hl, dg = SG - sz;
+        // Groups of K warp steps: all tap loads of a group are in flight before
+        // its first atomic.  Full groups of four run unmasked; the last 1 to 4
+        // steps run as one group of exactly that many, masked per lane only in
+        // its partial last step.
+        auto group = [&](int t, auto kk, auto masked) {
+          constexpr int K = decltype(kk)::value;
+          int j[K];
+          bool on[K];
+          float2 tp[NPOL][K];
+  #pragma unroll
+          for (int u = 0; u < K; ++u) {
+            on[u] = !decltype(masked)::value || t + LP * u + hl < n;
+            j[u] = on[u] ? tj[t + LP * u] : 0;
+  #pragma unroll
+            for (int p = 0; p < NPOL; ++p)
+              tp[p][u] = on[u] ? kl[p * ps + t + LP * u + j[u] * dk] : make_float2(0.f, 0.f);
+          }
+  #pragma unroll
+          for (int u = 0; u < K; ++u) {
+            if (!on[u]) break;
+            const int so = wofs + t + LP * u + j[u] * dg;
+  #pragma unroll
+            for (int p = 0; p < NPOL; ++p) {
+              const float cx = tp[p][u].x * vw[p].x + tp[p][u].y * vw[p].y;  // conj(tap) * vw
+              const float cy = tp[p][u].x * vw[p].y - tp[p][u].y * vw[p].x;
+              fx_add<RESID>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
+              fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
+            }
+          }
+        };
+        int t = 0;
+        for (; t + 4 * LP <= n; t += 4 * LP) group(t, IntC<4>(), BoolC<false>());
+        switch ((n - t + LP - 1) / LP) {
+          case 1: group(t, IntC<1>(), BoolC<true>()); break;
+          case 2: group(t, IntC<2>(), BoolC<true>()); break;
+          case 3: group(t, IntC<3>(), BoolC<true>()); break;
+          case 4: group(t, IntC<4>(), BoolC<true>()); break;
+          default: break;
+        }
       }
+    };
+    if constexpr (LPR == 32) {
+      if (box.sz <= 16)
+        row_loop(IntC<16>());
+      else
+        row_loop(IntC<32>());
+    } else {
+      row_loop(IntC<LPR>());
     }
-    if (hl == 0) {  // one weight sum per row slot of the warp
+    {  // the lanes that hold a row slot's weight sums
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) {
         const double s = (double)wsum[p] + (double)wcomp[p];
@@ -1406,9 +1419,6 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   const uint64_t nchunks = ((uint64_t)nvis + chunk - 1) / chunk;
   if (blockIdx.x >= nchunks) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // LPR lanes per row: 32, or 16 (two rows per warp) for supports <= 8.
-  constexpr int RPW = 32 / LPR;
-  const int hl = lane & (LPR - 1), half = lane / LPR;
   const int S = g.S, O = g.O;
   const int ps = (int)g.cf_pol_stride;
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
@@ -1429,7 +1439,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   uint32_t pos = c0;
   while (pos < c1) {
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
-    if (threadIdx.x == 0) s_next[parity] = pos + NW * RPW;  // published by the barrier in seg_box
+    if (threadIdx.x == 0) s_next[parity] = pos;  // published by the barrier in seg_box
     uint32_t *next_row = &s_next[parity];
     // The footprint pass ends in a barrier, which also orders the previous
     // segment's reads of the subgrid before this segment's staging.
@@ -1456,162 +1466,180 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       }
       __syncthreads();
     }
-    // Rows of this warp: r = pos + warp, pos + warp + NW, ...; the metadata of
-    // the next row is loaded while the current one is computed.
-    // Rows after each warp's first come from a shared counter, one at a
-    // time, which balances rows of different support across the warps; each
-    // warp holds the next row's index and metadata while it computes the
-    // current one.
-    // rbase is the warp's first row (warp-uniform); this lane's row is
-    // rbase + half.
-    uint32_t rbase = pos + warp * RPW;
-    RowMap mnext;
-    uint32_t inext = 0;
-    if (rbase + half < sg.end) {
-      mnext = smap[rbase + half];
-      inext = sidx[rbase + half];
-    }
-    while (rbase < sg.end) {
-      const RowMap m = mnext;
-      const uint32_t idx = inext;
-      const bool act = rbase + half < sg.end;
-      uint32_t rn = 0;
-      if (lane == 0) rn = atomicAdd(next_row, (uint32_t)RPW);
-      rn = __shfl_sync(0xffffffffu, rn, 0);
-      if (rn + half < sg.end) {
-        mnext = smap[rn + half];
-        inext = sidx[rn + half];
+    // Rows per warp: LP lanes per row; the default one-row-per-warp
+    // variant runs a segment four rows per warp when its largest support is
+    // at most 8 and two when at most 16 (256 taps), sharing the per-row
+    // set-up between the rows.
+    auto row_loop = [&](auto lpr_c) {
+      constexpr int LP = decltype(lpr_c)::value;
+      constexpr int RP = 32 / LP;
+      const int hl = lane & (LP - 1), half = lane / LP;
+      // Rows come from a shared counter, RP at a time (one per row slot of
+      // the warp), which balances rows of different support across the warps;
+      // each warp holds its next rows' indices and metadata while it computes
+      // the current ones.  rbase is warp-uniform; this lane's row is
+      // rbase + half.
+      uint32_t rbase = 0;
+      if (lane == 0) rbase = atomicAdd(next_row, (uint32_t)RP);
+      rbase = __shfl_sync(0xffffffffu, rbase, 0);
+      RowMap mnext;
+      uint32_t inext = 0;
+      if (rbase + half < sg.end) {
+        mnext = smap[rbase + half];
+        inext = sidx[rbase + half];
       }
-      rbase = rn;
-      R ax[NPOL], ay[NPOL];
-#pragma unroll
-      for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = 0;
-      if (act) {
-      const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-      const int sz = plane_sz(g, zc);
-      const int toff = (S - sz) >> 1;
-      const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
-      const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
-                     ((int64_t)(vf * O + uf) * S + toff) * S + toff;
-      const CT *gl;
-      int64_t pstride;
-      int dg;
-      if (direct) {
-        gl = gplane + (int64_t)wv * g.nx + wu + hl;
-        pstride = (int64_t)g.nw * plane_elems;
-        dg = (int)g.nx - sz;
-      } else {
-        gl = sub + (wv - sg.v0) * SG + (wu - sg.u0) + hl;
-        pstride = SG2;
-        dg = SG - sz;
-      }
-      const int n = sz * sz, dk = S - sz;
-      const unsigned char *tj = tab + tap_base(sz) + hl;
-      const CT *kl = kb + hl;
-      // Groups of K warp steps: every load of a group is in flight before the
-      // multiply-adds that use it.  Full groups of four run unmasked; the
-      // last 1 to 4 steps run as one group of exactly that many steps, masked
-      // per lane only in its partial last step.
-      auto group = [&](int t, auto kk, auto masked) {
-        constexpr int K = decltype(kk)::value;
-        int j[K];
-        bool on[K];
-#pragma unroll
-        for (int u = 0; u < K; ++u) {
-          on[u] = !decltype(masked)::value || t + LPR * u + hl < n;
-          j[u] = on[u] ? tj[t + LPR * u] : 0;
+      while (rbase < sg.end) {
+        const RowMap m = mnext;
+        const uint32_t idx = inext;
+        const bool act = rbase + half < sg.end;
+        uint32_t rn = 0;
+        if (lane == 0) rn = atomicAdd(next_row, (uint32_t)RP);
+        rn = __shfl_sync(0xffffffffu, rn, 0);
+        if (rn + half < sg.end) {
+          mnext = smap[rn + half];
+          inext = sidx[rn + half];
         }
-#pragma unroll
+        rbase = rn;
+        R ax[NPOL], ay[NPOL];
+  #pragma unroll
+        for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = 0;
+        if (act) {
+        const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+        const int sz = plane_sz(g, zc);
+        const int toff = (S - sz) >> 1;
+        const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
+        const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                       ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+        const CT *gl;
+        int64_t pstride;
+        int dg;
+        if (direct) {
+          gl = gplane + (int64_t)wv * g.nx + wu + hl;
+          pstride = (int64_t)g.nw * plane_elems;
+          dg = (int)g.nx - sz;
+        } else {
+          gl = sub + (wv - sg.v0) * SG + (wu - sg.u0) + hl;
+          pstride = SG2;
+          dg = SG - sz;
+        }
+        const int n = sz * sz, dk = S - sz;
+        const unsigned char *tj = tab + tap_base(sz) + hl;
+        const CT *kl = kb + hl;
+        // Groups of K warp steps: every load of a group is in flight before the
+        // multiply-adds that use it.  Full groups of four run unmasked; the
+        // last 1 to 4 steps run as one group of exactly that many steps, masked
+        // per lane only in its partial last step.
+        auto group = [&](int t, auto kk, auto masked) {
+          constexpr int K = decltype(kk)::value;
+          int j[K];
+          bool on[K];
+  #pragma unroll
+          for (int u = 0; u < K; ++u) {
+            on[u] = !decltype(masked)::value || t + LP * u + hl < n;
+            j[u] = on[u] ? tj[t + LP * u] : 0;
+          }
+  #pragma unroll
+          for (int p = 0; p < NPOL; ++p) {
+            CT tp[K], gv[K];
+  #pragma unroll
+            for (int u = 0; u < K; ++u) {
+              tp[u] = on[u] ? kl[p * ps + t + LP * u + j[u] * dk] : czero<CT>();
+              gv[u] = on[u] ? gl[p * pstride + t + LP * u + j[u] * dg] : czero<CT>();
+            }
+  #pragma unroll
+            for (int u = 0; u < K; ++u) {
+              ax[p] += gv[u].x * tp[u].x - gv[u].y * tp[u].y;
+              ay[p] += gv[u].x * tp[u].y + gv[u].y * tp[u].x;
+            }
+          }
+        };
+        // The packed variant: accumulators (sum re t.re, sum re t.im) and
+        // (sum im t.re, sum im t.im) per polarisation.
+        unsigned long long pa[NPOL], pb[NPOL];
+  #pragma unroll
+        for (int p = 0; p < NPOL; ++p) pa[p] = pb[p] = 0ull;
+        const int wofs4 = (wv - sg.v0) * SG + (wu - sg.u0) + hl;
+        auto group2 = [&](int t, auto kk, auto masked) {
+          constexpr int K = decltype(kk)::value;
+          int j[K];
+          bool on[K];
+  #pragma unroll
+          for (int u = 0; u < K; ++u) {
+            on[u] = !decltype(masked)::value || t + LP * u + hl < n;
+            j[u] = on[u] ? tj[t + LP * u] : 0;
+          }
+  #pragma unroll
+          for (int p = 0; p < NPOL; ++p) {
+            unsigned long long tp[K];
+            ulonglong2 gv[K];
+  #pragma unroll
+            for (int u = 0; u < K; ++u) {
+              tp[u] = on[u] ? *reinterpret_cast<const unsigned long long *>(kl + p * ps + t + LP * u + j[u] * dk)
+                            : 0ull;
+              gv[u] = on[u] ? *reinterpret_cast<const ulonglong2 *>(sub4 + p * SG2 + wofs4 + t + LP * u + j[u] * dg)
+                            : make_ulonglong2(0ull, 0ull);
+            }
+  #pragma unroll
+            for (int u = 0; u < K; ++u) {
+              pa[p] = ffma2(gv[u].x, tp[u], pa[p]);
+              pb[p] = ffma2(gv[u].y, tp[u], pb[p]);
+            }
+          }
+        };
+        int t = 0;
+        if (DUP && !direct) {
+          for (; t + 4 * LP <= n; t += 4 * LP) group2(t, IntC<4>(), BoolC<false>());
+          switch ((n - t + LP - 1) / LP) {
+            case 1: group2(t, IntC<1>(), BoolC<true>()); break;
+            case 2: group2(t, IntC<2>(), BoolC<true>()); break;
+            case 3: group2(t, IntC<3>(), BoolC<true>()); break;
+            case 4: group2(t, IntC<4>(), BoolC<true>()); break;
+            default: break;
+          }
+  #pragma unroll
+          for (int p = 0; p < NPOL; ++p) {
+            const float2 a2 = *reinterpret_cast<const float2 *>(&pa[p]);
+            const float2 b2 = *reinterpret_cast<const float2 *>(&pb[p]);
+            ax[p] = (R)(a2.x - b2.y);
+            ay[p] = (R)(a2.y + b2.x);
+          }
+        } else {
+          for (; t + 4 * LP <= n; t += 4 * LP) group(t, IntC<4>(), BoolC<false>());
+          switch ((n - t + LP - 1) / LP) {
+            case 1: group(t, IntC<1>(), BoolC<true>()); break;
+            case 2: group(t, IntC<2>(), BoolC<true>()); break;
+            case 3: group(t, IntC<3>(), BoolC<true>()); break;
+            case 4: group(t, IntC<4>(), BoolC<true>()); break;
+            default: break;
+          }
+        }
+        }  // act
+        // Reduce over each row's LP lanes (all lanes take part).
+  #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
-          CT tp[K], gv[K];
-#pragma unroll
-          for (int u = 0; u < K; ++u) {
-            tp[u] = on[u] ? kl[p * ps + t + LPR * u + j[u] * dk] : czero<CT>();
-            gv[u] = on[u] ? gl[p * pstride + t + LPR * u + j[u] * dg] : czero<CT>();
+          R sx = ax[p], sy = ay[p];
+          for (int o = LP / 2; o > 0; o >>= 1) {
+            sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o);
           }
-#pragma unroll
-          for (int u = 0; u < K; ++u) {
-            ax[p] += gv[u].x * tp[u].x - gv[u].y * tp[u].y;
-            ay[p] += gv[u].x * tp[u].y + gv[u].y * tp[u].x;
+          if (act && hl == p) {
+            CT out;
+            out.x = sx;
+            out.y = sy;
+            vis_out[(size_t)idx * NPOL + p] = out;
           }
-        }
-      };
-      // The packed variant: accumulators (sum re t.re, sum re t.im) and
-      // (sum im t.re, sum im t.im) per polarisation.
-      unsigned long long pa[NPOL], pb[NPOL];
-#pragma unroll
-      for (int p = 0; p < NPOL; ++p) pa[p] = pb[p] = 0ull;
-      const int wofs4 = (wv - sg.v0) * SG + (wu - sg.u0) + hl;
-      auto group2 = [&](int t, auto kk, auto masked) {
-        constexpr int K = decltype(kk)::value;
-        int j[K];
-        bool on[K];
-#pragma unroll
-        for (int u = 0; u < K; ++u) {
-          on[u] = !decltype(masked)::value || t + LPR * u + hl < n;
-          j[u] = on[u] ? tj[t + LPR * u] : 0;
-        }
-#pragma unroll
-        for (int p = 0; p < NPOL; ++p) {
-          unsigned long long tp[K];
-          ulonglong2 gv[K];
-#pragma unroll
-          for (int u = 0; u < K; ++u) {
-            tp[u] = on[u] ? *reinterpret_cast<const unsigned long long *>(kl + p * ps + t + LPR * u + j[u] * dk)
-                          : 0ull;
-            gv[u] = on[u] ? *reinterpret_cast<const ulonglong2 *>(sub4 + p * SG2 + wofs4 + t + LPR * u + j[u] * dg)
-                          : make_ulonglong2(0ull, 0ull);
-          }
-#pragma unroll
-          for (int u = 0; u < K; ++u) {
-            pa[p] = ffma2(gv[u].x, tp[u], pa[p]);
-            pb[p] = ffma2(gv[u].y, tp[u], pb[p]);
-          }
-        }
-      };
-      int t = 0;
-      if (DUP && !direct) {
-        for (; t + 4 * LPR <= n; t += 4 * LPR) group2(t, IntC<4>(), BoolC<false>());
-        switch ((n - t + LPR - 1) / LPR) {
-          case 1: group2(t, IntC<1>(), BoolC<true>()); break;
-          case 2: group2(t, IntC<2>(), BoolC<true>()); break;
-          case 3: group2(t, IntC<3>(), BoolC<true>()); break;
-          case 4: group2(t, IntC<4>(), BoolC<true>()); break;
-          default: break;
-        }
-#pragma unroll
-        for (int p = 0; p < NPOL; ++p) {
-          const float2 a2 = *reinterpret_cast<const float2 *>(&pa[p]);
-          const float2 b2 = *reinterpret_cast<const float2 *>(&pb[p]);
-          ax[p] = (R)(a2.x - b2.y);
-          ay[p] = (R)(a2.y + b2.x);
-        }
-      } else {
-        for (; t + 4 * LPR <= n; t += 4 * LPR) group(t, IntC<4>(), BoolC<false>());
-        switch ((n - t + LPR - 1) / LPR) {
-          case 1: group(t, IntC<1>(), BoolC<true>()); break;
-          case 2: group(t, IntC<2>(), BoolC<true>()); break;
-          case 3: group(t, IntC<3>(), BoolC<true>()); break;
-          case 4: group(t, IntC<4>(), BoolC<true>()); break;
-          default: break;
         }
       }
-      }  // act
-      // Reduce over each row's LPR lanes (all lanes take part).
-#pragma unroll
-      for (int p = 0; p < NPOL; ++p) {
-        R sx = ax[p], sy = ay[p];
-        for (int o = LPR / 2; o > 0; o >>= 1) {
-          sx += __shfl_xor_sync(0xffffffffu, sx, o);
-          sy += __shfl_xor_sync(0xffffffffu, sy, o);
-        }
-        if (act && hl == p) {
-          CT out;
-          out.x = sx;
-          out.y = sy;
-          vis_out[(size_t)idx * NPOL + p] = out;
-        }
-      }
+    };
+    if constexpr (LPR == 32) {
+      if (box.sz <= 8)
+        row_loop(IntC<8>());
+      else if (box.sz <= 16)
+        row_loop(IntC<16>());
+      else
+        row_loop(IntC<32>());
+    } else {
+      row_loop(IntC<LPR>());
     }
     pos = sg.end;
   }
