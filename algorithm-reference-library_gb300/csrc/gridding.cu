@@ -132,6 +132,87 @@ __global__ void k_scan(const uint32_t *__restrict__ hist, uint32_t n, uint32_t *
   if (threadIdx.x == 0 && n_bad_dev) *n_bad_dev = (int64_t)hist[nbins];
 }
 
+// Large histograms (more than kScanTile bins): a three-pass scan.  Pass 1:
+// block b scans bins [b kScanTile, (b + 1) kScanTile) into off (exclusive,
+// block-local) and writes its total; pass 2: one CTA scans the totals;
+// pass 3: each block adds its offset.  Integer sums, so the result equals
+// the single-CTA scan's.
+constexpr uint32_t kScanTile = 8192;  // 1024 threads x 8 bins
+
+__device__ __forceinline__ uint32_t block_excl_scan_1024(uint32_t v, uint32_t *s_warp, uint32_t *total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = s_warp[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    s_warp[lane] = w;  // inclusive over warps
+  }
+  __syncthreads();
+  const uint32_t before = warp ? s_warp[warp - 1] : 0u;
+  *total = s_warp[31];
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_tiles(const uint32_t *__restrict__ hist, uint32_t n,
+                                                     uint32_t *__restrict__ off, uint32_t *__restrict__ tile_sum) {
+  __shared__ uint32_t s_warp[32];
+  const uint32_t b0 = blockIdx.x * kScanTile + threadIdx.x * 8;
+  uint32_t v[8], t = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    v[k] = b0 + k < n ? hist[b0 + k] : 0u;
+    t += v[k];
+  }
+  uint32_t total;
+  uint32_t run = block_excl_scan_1024(t, s_warp, &total);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (b0 + k < n) off[b0 + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_totals(uint32_t *__restrict__ tile_sum, uint32_t ntiles,
+                                                      uint32_t *__restrict__ off, uint32_t n,
+                                                      int64_t *n_bad_dev, const uint32_t *__restrict__ hist,
+                                                      uint32_t nbins) {
+  __shared__ uint32_t s_warp[32];
+  // ntiles <= 8192: eight totals per thread
+  const uint32_t b0 = threadIdx.x * 8;
+  uint32_t v[8], t = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    v[k] = b0 + k < ntiles ? tile_sum[b0 + k] : 0u;
+    t += v[k];
+  }
+  uint32_t total;
+  uint32_t run = block_excl_scan_1024(t, s_warp, &total);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (b0 + k < ntiles) tile_sum[b0 + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0) {
+    off[n] = total;
+    if (n_bad_dev) *n_bad_dev = (int64_t)hist[nbins];
+  }
+}
+
+__global__ void k_scan_add(uint32_t *__restrict__ off, uint32_t n, const uint32_t *__restrict__ tile_sum) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) off[i] += tile_sum[i / kScanTile];
+}
+
 // K2b: scatter rows into bin order (hist reused as zeroed per-bin cursors).
 __global__ void k_scatter(const uint32_t *__restrict__ keys, const RowMap *__restrict__ maps, int64_t nvis,
                           const uint32_t *__restrict__ off, uint32_t *__restrict__ cursor,
@@ -1828,9 +1909,22 @@ int plan_build(const double *uvw, const double *freq, int64_t nvis, const Geom &
     ARL_LAUNCH_CHECK();
     count_launch(1);
   }
-  k_scan<<<1, 1024, 0, st>>>(b.hist, nh, b.offsets, n_bad_dev, g.nbins);
-  ARL_LAUNCH_CHECK();
-  count_launch(1);
+  const uint32_t ntiles = (nh + kScanTile - 1) / kScanTile;
+  if (ntiles <= 4 || ntiles > 8192 || (size_t)plan_wpart_items(g) * 2 < ntiles) {
+    k_scan<<<1, 1024, 0, st>>>(b.hist, nh, b.offsets, n_bad_dev, g.nbins);
+    ARL_LAUNCH_CHECK();
+    count_launch(1);
+  } else {
+    // the plane-mean partials' area is free while the plan is built
+    uint32_t *tile_sum = reinterpret_cast<uint32_t *>(b.wpart);
+    k_scan_tiles<<<ntiles, 1024, 0, st>>>(b.hist, nh, b.offsets, tile_sum);
+    ARL_LAUNCH_CHECK();
+    k_scan_totals<<<1, 1024, 0, st>>>(tile_sum, ntiles, b.offsets, nh, n_bad_dev, b.hist, g.nbins);
+    ARL_LAUNCH_CHECK();
+    k_scan_add<<<(nh + 255) / 256, 256, 0, st>>>(b.offsets, nh, tile_sum);
+    ARL_LAUNCH_CHECK();
+    count_launch(3);
+  }
   ARL_CUDA(cudaMemsetAsync(b.hist, 0, (size_t)nh * 4, st));
   if (nvis > 0) {
     int blocks = (int)std::min<int64_t>((nvis + 255) / 256, (int64_t)num_sms() * 16);
