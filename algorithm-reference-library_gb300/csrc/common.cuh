@@ -57,6 +57,11 @@ struct Geom {
   // Fixed-point decisions (pow2O and every limit below 2^29): the tolerances
   // above in units of 2^-20, plus one.
   int32_t fixmap, tq_u, tq_v, tq_w, tq_z, tq_f;
+  // One grid w-plane whose interval contains every cf plane's (w-projection),
+  // or one cf plane whose interval contains every grid plane's (w-stacking,
+  // 2-D): that index is 0 for every row the other axis accepts, so the fast
+  // path does not compute it.
+  int32_t skip_zg, skip_zc;
   // binning
   int32_t T;       // tile edge (grid pixels)
   int32_t SG;      // staged subgrid edge = T + S

@@ -1822,6 +1822,21 @@ int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precisio
     g->tq_z = tq(g->tol_z);
     g->tq_f = tq(g->tol_f);
     const double lim = 536870912.0;  // 2^29
+    // world interval covered by planes [0, n) of a nearest-plane axis
+    auto span = [](const arlgpu_axis &a, int n, double *lo, double *hi) {
+      const double e0 = a.crval + (0.5 - a.crpix) * a.cdelt, e1 = a.crval + ((double)n + 0.5 - a.crpix) * a.cdelt;
+      *lo = std::min(e0, e1);
+      *hi = std::max(e0, e1);
+    };
+    double glo, ghi, zlo, zhi;
+    span(gd->w, gd->nw, &glo, &ghi);
+    span(cd->z, cd->nz, &zlo, &zhi);
+    auto inside = [](double alo, double ahi, double blo, double bhi) {  // [alo, ahi] well inside [blo, bhi]
+      const double m = 1e-9 * ((bhi - blo) + fabs(blo) + fabs(bhi));
+      return std::isfinite(alo) && std::isfinite(ahi) && alo > blo + m && ahi < bhi - m;
+    };
+    g->skip_zg = gd->nw == 1 && inside(zlo, zhi, glo, ghi);
+    g->skip_zc = cd->nz == 1 && inside(glo, ghi, zlo, zhi);
     g->fixmap = g->pow2O && g->Xlim_u < lim && g->Xlim_v < lim && g->Plim_w < lim && g->Plim_z < lim &&
                 g->Plim_f < lim && g->tq_u < (1 << 18) && g->tq_v < (1 << 18) && g->tq_w < (1 << 18) &&
                 g->tq_z < (1 << 18) && g->tq_f < (1 << 18);

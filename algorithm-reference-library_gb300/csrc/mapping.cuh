@@ -190,9 +190,12 @@ __device__ __forceinline__ Mapped map_row(double u, double v, double w, double f
   Mapped m;
   bool ok;
   int pu, pv, uf, vf, zg, zc, ch;
+  zg = 0;
+  zc = 0;
   if (g.fixmap && fix_axis_x(u, g.rOu, g.cOu, g.tq_u, g.O, g.log2O, &pu, &uf) &&
-      fix_axis_x(v, g.rOv, g.cOv, g.tq_v, g.O, g.log2O, &pv, &vf) && fix_round(w, g.gw, g.rcp_gw, g.tq_w, &zg) &&
-      fix_round(w, g.cz, g.rcp_cz, g.tq_z, &zc) && fix_round(f, g.gf, g.rcp_gf, g.tq_f, &ch)) {
+      fix_axis_x(v, g.rOv, g.cOv, g.tq_v, g.O, g.log2O, &pv, &vf) &&
+      (g.skip_zg || fix_round(w, g.gw, g.rcp_gw, g.tq_w, &zg)) &&
+      (g.skip_zc || fix_round(w, g.cz, g.rcp_cz, g.tq_z, &zc)) && fix_round(f, g.gf, g.rcp_gf, g.tq_f, &ch)) {
     // uf, vf lie in [0, O) by construction
     ok = pu >= 0 && pu < g.nx && pv >= 0 && pv < g.ny && zg >= 0 && zg < g.nw && zc >= 0 && zc < g.nz && ch >= 0 &&
          ch < g.nchan && ch < g.cf_nchan;
