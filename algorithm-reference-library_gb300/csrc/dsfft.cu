@@ -281,7 +281,20 @@ k_dsfft_rows(const float2 *__restrict__ grid, int64_t qstride, int nsum, int64_t
     sm[pos(x, q)] = v;
   }
   }
-  __syncthreads();
+  // An all-zero tile (whole empty grid rows, common in w-stack slices)
+  // transforms to zero: write zeros and skip the arithmetic.
+  bool nz = false;
+  for (int t = threadIdx.x; t < PTS && !nz; t += T) {
+    const float4 v = sm[pos(t & ((1 << log2nx) - 1), t >> log2nx)];
+    nz = v.x != 0.f || v.z != 0.f;
+  }
+  if (!__syncthreads_or(nz)) {
+    for (int t = threadIdx.x; t < PTS; t += T) {
+      const int64_t R = row0 + (t >> log2nx);
+      if (R < nrows) buf[(R << log2nx) + (t & ((1 << log2nx) - 1))] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    return;
+  }
   ds_dif_cta<T>(sm, log2nx, log2S, false, pos, TwGlobal());
   for (int t = threadIdx.x; t < PTS; t += T) {
     const int q = t >> log2nx, x = t & ((1 << log2nx) - 1);
@@ -359,9 +372,18 @@ k_dsfft_rows_split(const float2 *__restrict__ grid, int64_t qstride, int nsum, i
     sm[pos(n, 0)] = v;
   }
   }
-  __syncthreads();
-  ds_dif_cta<512>(sm, LH, 0, false, pos, TwGlobal());
+  // An all-zero half (a whole empty grid row) transforms to zero.
+  bool nz = false;
+  for (int n = threadIdx.x; n < H && !nz; n += 512) {
+    const float4 v = sm[pos(n, 0)];
+    nz = v.x != 0.f || v.z != 0.f;
+  }
   float4 *out = buf + (R << LX) + half;
+  if (!__syncthreads_or(nz)) {
+    for (int k = threadIdx.x; k < H; k += 512) out[2 * k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  ds_dif_cta<512>(sm, LH, 0, false, pos, TwGlobal());
   for (int k = threadIdx.x; k < H; k += 512) out[2 * k] = sm[pos(brev(k, LH), 0)];
 }
 
