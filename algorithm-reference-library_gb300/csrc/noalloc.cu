@@ -12,7 +12,7 @@
 // outputs.
 //
 // Costs and limits of that choice:
-//   * every GPU that loads the library holds kScratchBytes (about 21.5 MB) of
+//   * every GPU that loads the library holds kScratchBytes (about 22.0 MB) of
 //     device memory for this array until the process exits;
 //   * one call handles at most kMaxRows rows and a plan of at most kMaxBins
 //     (channel x w-plane x uv-tile) bins; larger calls are rejected with
@@ -41,7 +41,7 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // sorted RowMap, histogram, offsets) at the maximum sizes above.
 constexpr size_t kScratchBytes = align256(kMaxRows * 4) + align256(kMaxRows * 16) + align256(kMaxRows * 4) +
                                  align256(kMaxRows * 16) + align256((kMaxBins + 1) * 4) +
-                                 align256((kMaxBins + 2) * 4);
+                                 align256((kMaxBins + 2) * 4) + align256(kMaxBins * 8);  // + plane-mean partials
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 

@@ -165,7 +165,7 @@ int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const arlgpu_grid_
  * For callers that cannot allocate device memory when they grid (recording a
  * CUDA graph, a device pool owned by another framework, real-time code that
  * allocates only at start-up).  Same arguments and results as arlgpu_grid, minus
- * the workspace: the row plan lives in a fixed device array of ~21.5 MB that the
+ * the workspace: the row plan lives in a fixed device array of ~22.0 MB that the
  * library holds on every GPU it runs on until the process exits.  At most 524,288
  * rows and 65,536 plan bins (channel x w-plane x uv-tile) per call; larger calls
  * fail with ARLGPU_ERR_WORKSPACE before any GPU work.  All calls share the array:

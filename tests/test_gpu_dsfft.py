@@ -36,15 +36,22 @@ def _rel(a, b):
     return float((a - b).abs().max() / b.abs().max())
 
 
-@pytest.mark.parametrize('ny,nx,nchan,npol,nw', [(64, 64, 1, 1, 1), (128, 256, 1, 2, 3), (256, 64, 2, 1, 1),
-                                                 (1024, 1024, 1, 1, 1), (4096, 4096, 1, 1, 1), (64, 8192, 1, 1, 1),
-                                                 (16384, 64, 1, 1, 1), (512, 2048, 2, 2, 1)])
-def test_dsfft_matches_complex128_transform(arl, dsfft_switch, ny, nx, nchan, npol, nw):
+@pytest.mark.parametrize('ny,nx,nchan,npol,nw,sparse', [
+    (64, 64, 1, 1, 1, False), (128, 256, 1, 2, 3, False), (256, 64, 2, 1, 1, False), (1024, 1024, 1, 1, 1, False),
+    (4096, 4096, 1, 1, 1, False), (64, 8192, 1, 1, 1, False), (16384, 64, 1, 1, 1, False),
+    (512, 2048, 2, 2, 1, False), (256, 512, 1, 1, 1, True), (64, 8192, 1, 2, 1, True)])
+def test_dsfft_matches_complex128_transform(arl, dsfft_switch, ny, nx, nchan, npol, nw, sparse):
+    """sparse: whole grid rows zero (the row pass skips their arithmetic), as in
+    the w-stack slices of C3 / C5."""
     dv = arl.device
     dev = torch.device('cuda')
     g = torch.Generator(device='cpu').manual_seed(ny * 7 + nx)
     shape = (nchan, npol, nw, ny, nx)
-    grid = torch.complex(torch.randn(shape, generator=g), torch.randn(shape, generator=g)).to(torch.complex64).to(dev)
+    grid = torch.complex(torch.randn(shape, generator=g), torch.randn(shape, generator=g)).to(torch.complex64)
+    if sparse:
+        keep = torch.rand((nchan, npol, nw, ny, 1), generator=g) < 0.4
+        grid = grid * keep
+    grid = grid.to(dev)
     gcf = (1.0 + 99.0 * torch.rand((nchan, npol, ny, nx), generator=g, dtype=torch.float64)).to(dev)
     sw = 1.0 + torch.rand((nchan, npol), generator=g, dtype=torch.float64)
     if nchan * npol > 1:
