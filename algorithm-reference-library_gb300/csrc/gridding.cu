@@ -1236,7 +1236,7 @@ __device__ __forceinline__ void fx_add(int *q, int *r, float x, float scale, flo
   }
 }
 
-template <int NPOL, int NW, bool RESID, int LPR = 32>
+template <int NPOL, int NW, bool RESID, int LPR = 32, int SGC = 0>
 __global__ void __launch_bounds__(NW * 32)
 k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
           const uint32_t *__restrict__ off, uint32_t chunk, const float2 *__restrict__ vis,
@@ -1244,7 +1244,9 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
           double *__restrict__ sumwt) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_red[2][NW * 6];
-  const int SG = g.SG, SG2 = SG * SG;
+  // SGC != 0: the subgrid edge as a compile-time constant, so that plane
+  // offsets in shared memory fold into the instructions' immediates.
+  const int SG = SGC ? SGC : g.SG, SG2 = SG * SG;
   // Planar subgrid: integer plane (p, c) at subq + (2 p + c) SG2 (c = 0 real,
   // 1 imaginary); with RESID the residual-limb planes follow all of them.
   // The planes are zero between segments: the flush clears what it reads.
@@ -1481,7 +1483,7 @@ __device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsign
 // DUP (FP32 only, degrid_kernel 3): the staged subgrid holds each cell as
 // (re, re, im, im), so a tap is two packed multiply-adds,
 // (sum re t.re, sum re t.im) and (sum im t.re, sum im t.im), instead of four.
-template <typename R, int NPOL, int NW, bool DUP = false, int LPR = 32>
+template <typename R, int NPOL, int NW, bool DUP = false, int LPR = 32, int SGC = 0>
 __global__ void __launch_bounds__(NW * 32)
 k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
               const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
@@ -1489,7 +1491,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
               typename VisT<R>::C *__restrict__ vis_out) {
   using CT = typename Cplx<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int SG = g.SG, SG2 = SG * SG;
+  const int SG = SGC ? SGC : g.SG, SG2 = SG * SG;  // SGC != 0: compile-time edge
   static_assert(!DUP || sizeof(R) == 4, "the packed variant is FP32 only");
   CT *sub = reinterpret_cast<CT *>(smraw);
   float4 *sub4 = reinterpret_cast<float4 *>(smraw);  // DUP layout
@@ -1979,12 +1981,23 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
                const float2 *, float2 *, double *);
   // Supports up to 8 (64 taps): several rows per warp (tuning small_rows).
   const int rpw = g.S <= 8 ? g_tune_small_rows.load() : 1;
+  // The default subgrid edge (48, or 32 with four polarisations) runs a
+  // compile-time-edge instantiation; other edges (autotuner trials) the
+  // runtime-edge one.
+  const bool csg = g.SG == (g.npol == 4 ? 32 : 48);
   auto pick = [&](auto resid_c) {
     constexpr bool RS = decltype(resid_c)::value;
-    if (rpw == 4) return g.npol == 1 ? k_grid_fx<1, kWarps, RS, 8> : g.npol == 2 ? k_grid_fx<2, kWarps, RS, 8>
-                                                                                 : k_grid_fx<4, kWarps, RS, 8>;
-    if (rpw == 2) return g.npol == 1 ? k_grid_fx<1, kWarps, RS, 16> : g.npol == 2 ? k_grid_fx<2, kWarps, RS, 16>
-                                                                                  : k_grid_fx<4, kWarps, RS, 16>;
+    if (csg) {
+      if (g.npol == 4)
+        return rpw == 4 ? k_grid_fx<4, kWarps, RS, 8, 32>
+                        : rpw == 2 ? k_grid_fx<4, kWarps, RS, 16, 32> : k_grid_fx<4, kWarps, RS, 32, 32>;
+      if (g.npol == 2)
+        return rpw == 4 ? k_grid_fx<2, kWarps, RS, 8, 48>
+                        : rpw == 2 ? k_grid_fx<2, kWarps, RS, 16, 48> : k_grid_fx<2, kWarps, RS, 32, 48>;
+      return rpw == 4 ? k_grid_fx<1, kWarps, RS, 8, 48>
+                      : rpw == 2 ? k_grid_fx<1, kWarps, RS, 16, 48> : k_grid_fx<1, kWarps, RS, 32, 48>;
+    }
+    // runtime edge: rows per warp chosen per segment only
     return g.npol == 1 ? k_grid_fx<1, kWarps, RS> : g.npol == 2 ? k_grid_fx<2, kWarps, RS> : k_grid_fx<4, kWarps, RS>;
   };
   kern = resid ? pick(BoolC<true>()) : pick(BoolC<false>());
@@ -2060,15 +2073,26 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
     // Supports up to 8 (64 taps): several rows per warp (tuning small_rows_degrid).
     const int rpw = g.S <= 8 ? g_tune_small_rows_dg.load() : 1;
-    if (rpw == 4)
-      kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps, sizeof(R) == 4, 8>
-                         : g.npol == 2 ? k_degrid_lean<R, 2, kWarps, sizeof(R) == 4, 8>
-                                       : k_degrid_lean<R, 4, kWarps, sizeof(R) == 4, 8>;
-    else if (rpw == 2)
-      kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps, sizeof(R) == 4, 16>
-                         : g.npol == 2 ? k_degrid_lean<R, 2, kWarps, sizeof(R) == 4, 16>
-                                       : k_degrid_lean<R, 4, kWarps, sizeof(R) == 4, 16>;
-    else
+    bool done = false;
+    if constexpr (sizeof(R) == 4) {
+      // the default subgrid edge as a compile-time constant (see the gridder)
+      if (g.SG == (g.npol == 4 ? 32 : 48)) {
+        done = true;
+        if (g.npol == 4)
+          kern = rpw == 4 ? k_degrid_lean<R, 4, kWarps, true, 8, 32>
+                          : rpw == 2 ? k_degrid_lean<R, 4, kWarps, true, 16, 32>
+                                     : k_degrid_lean<R, 4, kWarps, true, 32, 32>;
+        else if (g.npol == 2)
+          kern = rpw == 4 ? k_degrid_lean<R, 2, kWarps, true, 8, 48>
+                          : rpw == 2 ? k_degrid_lean<R, 2, kWarps, true, 16, 48>
+                                     : k_degrid_lean<R, 2, kWarps, true, 32, 48>;
+        else
+          kern = rpw == 4 ? k_degrid_lean<R, 1, kWarps, true, 8, 48>
+                          : rpw == 2 ? k_degrid_lean<R, 1, kWarps, true, 16, 48>
+                                     : k_degrid_lean<R, 1, kWarps, true, 32, 48>;
+      }
+    }
+    if (!done)  // runtime edge: rows per warp chosen per segment only
       kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps, sizeof(R) == 4>
                          : g.npol == 2 ? k_degrid_lean<R, 2, kWarps, sizeof(R) == 4>
                                        : k_degrid_lean<R, 4, kWarps, sizeof(R) == 4>;

@@ -108,8 +108,10 @@ unsigned long long arlgpu_kernel_launches(void);
  *                   FFT on the FP32 pipes for power-of-two sizes 64..8192 (default),
  *                   0 = cuFFT complex128
  *   "small_rows"    rows per warp (1, 2 or 4; default 2) in the FP32C fixed-point gridder when the
- *                   largest support is at most 8 (64 taps)
+ *                   largest support is at most 8 (64 taps) and the subgrid edge is the default
  *   "small_rows_degrid"  the same for the packed degridder (default 4)
+ *                   Otherwise both kernels choose per segment: two rows per warp when the
+ *                   segment's largest support is at most 16, four (degridder) at most 8.
  * No reference counterpart (ARL has one Python loop per function). */
 int arlgpu_set_tuning(const char *key, int value);
 int arlgpu_get_tuning(const char *key, int *value);
