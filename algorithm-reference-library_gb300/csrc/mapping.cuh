@@ -186,19 +186,29 @@ __device__ __forceinline__ bool fix_round(double x, const arlgpu_axis &a, double
   return true;
 }
 
+// Nearest-plane index of one axis in [0, n), or -1 outside: the fixed-point
+// decision, and NumPy's exact sequence for that axis alone where the value
+// lies within the tolerance of a half-integer.  Whole sets of rows can sit on
+// such a tie: with an even number of w slices centred on w = 0, every row of
+// a coplanar array at transit (w = 0 up to rounding) does.
+__device__ __forceinline__ int plane_index(double x, const arlgpu_axis &a, double rcp, int tq, int n) {
+  int idx;
+  if (fix_round(x, a, rcp, tq, &idx)) return idx >= 0 && idx < n ? idx : -1;
+  const double p = rint(w2p_exact(x, a));  // range test in double: no wrap when narrowed
+  return p >= 0.0 && p < (double)n ? (int)p : -1;
+}
+
 __device__ __forceinline__ Mapped map_row(double u, double v, double w, double f, const Geom &g) {
   Mapped m;
   bool ok;
   int pu, pv, uf, vf, zg, zc, ch;
-  zg = 0;
-  zc = 0;
   if (g.fixmap && fix_axis_x(u, g.rOu, g.cOu, g.tq_u, g.O, g.log2O, &pu, &uf) &&
-      fix_axis_x(v, g.rOv, g.cOv, g.tq_v, g.O, g.log2O, &pv, &vf) &&
-      (g.skip_zg || fix_round(w, g.gw, g.rcp_gw, g.tq_w, &zg)) &&
-      (g.skip_zc || fix_round(w, g.cz, g.rcp_cz, g.tq_z, &zc)) && fix_round(f, g.gf, g.rcp_gf, g.tq_f, &ch)) {
+      fix_axis_x(v, g.rOv, g.cOv, g.tq_v, g.O, g.log2O, &pv, &vf)) {
     // uf, vf lie in [0, O) by construction
-    ok = pu >= 0 && pu < g.nx && pv >= 0 && pv < g.ny && zg >= 0 && zg < g.nw && zc >= 0 && zc < g.nz && ch >= 0 &&
-         ch < g.nchan && ch < g.cf_nchan;
+    zg = g.skip_zg ? 0 : plane_index(w, g.gw, g.rcp_gw, g.tq_w, g.nw);
+    zc = g.skip_zc ? 0 : plane_index(w, g.cz, g.rcp_cz, g.tq_z, g.nz);
+    ch = plane_index(f, g.gf, g.rcp_gf, g.tq_f, min(g.nchan, g.cf_nchan));
+    ok = pu >= 0 && pu < g.nx && pv >= 0 && pv < g.ny && zg >= 0 && zc >= 0 && ch >= 0;
   } else {
     const RawMap r = map_raw(u, v, w, f, g);
     // Range checks in double so huge values cannot wrap when narrowed.

@@ -94,3 +94,47 @@ def test_wstack_many_slices_vs_oracle(arl, oracle, N):
         got, sw = arl.imaging.invert_wstack(vis, im, K, gcfcf=(gcf, cf), precision=p)
         assert_image(got.data, want, oracle.pswf_gcf(N), p)
         assert numpy.allclose(sw, wsw, rtol=1e-12 if p == 'fp64' else 1e-6)
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
+def test_wstack_plan_at_slice_ties_vs_oracle(arl, oracle, precision):
+    """Rows on the half-way points between w slices, and one ulp either side:
+    w = 0 with an even slice count (every row of a coplanar array at transit
+    sits there) and the other slice boundaries.  The planned gridder must put
+    each row in the slice NumPy's round-half-even of world2pix0 picks; the grid
+    is compared cell by cell with the oracle's."""
+    rng = numpy.random.default_rng(21)
+    N, cell, O, S, K, wmax = 128, 4.5e-3, 8, 8, 8, 250.0
+    im = arl.create_image(npixel=N, cellsize=cell, frequency=numpy.array([1e8]), channel_bandwidth=numpy.array([1e6]),
+                          phasecentre=arl.PhaseCentre(0.0, -45.0))
+    gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    step = 2.0 * wmax / (K - 1)
+    ties = numpy.concatenate([[0.0, 1e-13, -1e-13, 5e-324, -5e-324], -wmax + (numpy.arange(K - 1) + 0.5) * step])
+    ties = numpy.concatenate([ties, numpy.nextafter(ties, numpy.inf), numpy.nextafter(ties, -numpy.inf)])
+    w = numpy.concatenate([[wmax, -wmax], numpy.repeat(ties, 60), rng.uniform(-wmax, wmax, 1000)])
+    n = w.size
+    lim = (N // 2 - S // 2 - 2) / (N * cell)
+    uvw = numpy.stack([rng.uniform(-lim, lim, n), rng.uniform(-lim, lim, n), w], axis=1)
+    freq = numpy.full(n, 1e8)
+    v = rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1))
+    wt = numpy.ones((n, 1))
+    dev = torch.device('cuda')
+    dvis = arl.DeviceVisibility(torch.as_tensor(uvw, device=dev), torch.as_tensor(freq, device=dev),
+                                torch.as_tensor(v, device=dev).to(arl.device.CDTYPE[precision]),
+                                torch.ones((n, 1), dtype=arl.device.RDTYPE[precision], device=dev))
+    imager = arl.WStackImager(dvis, im, K, gcfcf=(gcf, cf), precision=precision)
+    assert imager.w_axis == (-wmax, 1.0, step)
+    imager.grid()
+    img = oracle.image_geometry(N, cell)
+    gax = oracle.grid_axes(img, nw=K)
+    gax['w'] = imager.w_axis
+    cax = oracle.cf_axes(img, O, S)
+    _, ocf = oracle.create_pswf_cf(1, 1, 8, 8, O, S)
+    maps = oracle.convolution_mapping(uvw, freq, gax, cax)
+    assert numpy.all((maps[4] >= 0) & (maps[4] < K))
+    cells, vals, sw = oracle.grid_sparse(v, wt, maps, ocf, gax['shape'])
+    flat = imager.grid_t.reshape(-1)
+    got = flat[torch.as_tensor(cells, device=dev)].to(torch.complex128).cpu().numpy()
+    assert rel(got, vals) < TOL[precision]
+    total = float((flat.to(torch.complex128).abs() ** 2).sum())
+    assert abs(total - float(numpy.sum(numpy.abs(got) ** 2))) <= 1e-9 * total
