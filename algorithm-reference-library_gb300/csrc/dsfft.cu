@@ -606,15 +606,19 @@ bool dsfft_supported(int ny, int nx) {
   return col_geom(ly, lx, &cg);
 }
 
+// Function attributes belong to each device's context: set once per device.
 static int set_smem() {
-  static std::atomic<int> done{0};
-  if (done.load()) return ARLGPU_OK;
+  static std::atomic<unsigned> done{0};
+  int dev = 0;
+  ARL_CUDA(cudaGetDevice(&dev));
+  const unsigned bit = 1u << (dev & 31);
+  if (done.load() & bit) return ARLGPU_OK;
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows_split, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_rows<4096, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols1, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_image, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem));
   ARL_CUDA(cudaFuncSetAttribute(k_dsfft_cols2_wstack, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem2));
-  done.store(1);
+  done.fetch_or(bit);
   return ARLGPU_OK;
 }
 

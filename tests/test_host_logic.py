@@ -95,6 +95,26 @@ def test_wslice_iterator_matches_oracle(arl, oracle):
     assert len(got) == len(want) and all(numpy.array_equal(a, b) for a, b in zip(got, want))
 
 
+def test_slice_axis_matches_wslice_iter(arl, oracle):
+    """The w-stack grid axis gives every row the slice ARL's vis_wslice_iter
+    does.  Rows within rounding of a half-way point (where ARL's strict
+    |w - box| < step / 2 may count a row in neither or both neighbours, e.g.
+    w = 0 with an even slice count) go to exactly one, by round-half-even."""
+    import importlib
+    import torch
+    slice_axis = importlib.import_module(arl.__name__ + '.wstack').slice_axis
+    rng = numpy.random.default_rng(10)
+    for K in (2, 7, 8, 32):
+        w = numpy.concatenate([rng.uniform(-300, 300, 5000), [300.0, 0.0, -0.0, 1e-13]])
+        crval, crpix, cdelt = slice_axis(torch.as_tensor(w), K)
+        p = ((w - crval) / cdelt + crpix) - 1.0
+        idx = numpy.round(p).astype(int)
+        assert numpy.all((idx >= 0) & (idx < K))
+        near = numpy.abs(p - numpy.floor(p) - 0.5) < 1e-9
+        for k, m in enumerate(oracle.wslice_rows(w, K)):
+            assert numpy.array_equal(m[~near], (idx == k)[~near])
+
+
 def test_phasecentre_lmn(arl):
     a = arl.PhaseCentre(10.0, -45.0)
     assert a.separation_rad(a) == 0.0
