@@ -156,6 +156,22 @@ def measured_hbm():
         return FALLBACK_HBM_GBS, 'fallback'
 
 
+def launch_insts(kernel, nrows):
+    """Warp instructions of one `kernel` launch over nrows rows from the
+    committed one-pass ncu capture (profiles/ncu_inst.txt), scaled by rows when
+    the capture ran on a different row count; None when absent."""
+    path = os.path.join(ROOT, 'profiles', 'ncu_inst.txt')
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) == 3 and parts[0] == kernel:
+                rows, k = float(parts[1]), float(parts[2])
+                return {'inst': k * nrows / rows, 'captured_rows': int(rows), 'scaled': rows != nrows}
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def launch_traffic(kernel, nrows):
     """DRAM bytes of one `kernel` launch over nrows rows from the committed ncu
     summary (profiles/ncu_dram.txt: kernel, rows captured, bytes), scaled by
@@ -171,6 +187,25 @@ def launch_traffic(kernel, nrows):
     except (OSError, ValueError):
         pass
     return None
+
+
+def issue_roofline(torch, kernel, nrows, kms, clk):
+    """The dominant kernel against the instruction-issue ceiling (one warp
+    instruction per cycle per scheduler, 4 per SM, at the SM clock sampled
+    during the timed region): its ncu instruction count per launch over the
+    CUDA-event launch time measured here."""
+    ins = launch_insts(kernel, nrows)
+    if ins is None or not torch.cuda.is_available():
+        return None
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = (clk or {}).get('sm_mhz') or 2070.0
+    peak = sms * 4 * mhz * 1e6
+    achieved = ins['inst'] / (kms / 1e3)
+    return {'bound': 'issue', 'kernel': kernel, 'achieved': achieved, 'peak': peak, 'unit': 'warp-inst/s',
+            'frac': achieved / peak, 'inst_per_launch': ins['inst'],
+            'inst_source': 'ncu smsp__inst_executed.sum (one pass), %d-row capture%s' %
+                           (ins['captured_rows'], ', scaled by rows' if ins['scaled'] else ''),
+            'peak_source': '%d SMs x 4 schedulers x %.0f MHz' % (sms, mhz)}
 
 
 # ---------------------------------------------------------------------------
@@ -626,6 +661,7 @@ def arm_gb300(args, torch, world, rank, local):
                      'traffic_source': None if tr is None else
                      ('ncu dram__bytes_read.sum + dram__bytes_write.sum, %d-row capture%s' %
                       (tr['captured_rows'], ', scaled by rows' if tr['scaled'] else ''))},
+        'roofline_issue': issue_roofline(torch, 'k_' + kern, n, kms, clk),
         'roofline_step': {'algorithmic_bytes': step_alg, 'achieved_gbs': step_alg / (ms / 1e3) / 1e9,
                           'frac': step_alg / (ms / 1e3) / 1e9 / peak},
         'e2e': {'value': world * n / (e2e_ms / 1e3), 'unit': 'vis/s', 'h2d_bytes_per_step': h2d,
