@@ -216,7 +216,7 @@ __device__ __forceinline__ int brev(int k, int log2L) { return (int)(__brev((uns
 // touch eight different 16-byte bank groups per quarter warp.
 // ---------------------------------------------------------------------------
 constexpr int kColT = 512, kColPts = 4096, kColNPT = kColPts / kColT, kColSmem = (kColPts + 256) * 16,
-              kColSmem2 = (kColPts + 128) * 16 + kColPts * 8;
+              kColSmem2 = (2 * kColPts + 128) * 16 + kColPts * 8;
 
 template <int PTS, int T>
 __global__ void __launch_bounds__(T, 1024 / T)
@@ -494,9 +494,8 @@ k_dsfft_cols2_image(const float4 *__restrict__ buf, int log2ny, int log2nx, ColG
 // order, buf holding them from p0.  Each CTA sums Re(wb_s v) over the slices
 // of its tile into double-single accumulators and adds them to the image's DS
 // slots (image memory viewed as float2; the group holding slice 0 of image b
-// writes them).  One tile buffer and 64 registers a thread: two CTAs per SM,
-// each loading its next slice while the other computes.
-__global__ void __launch_bounds__(kColT, 2)
+// writes them).
+__global__ void __launch_bounds__(kColT)
 k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, ColGeom cg, int64_t p0, int64_t p1,
                      int K, double fov, const double *__restrict__ wmean, float2 *__restrict__ slots) {
   extern __shared__ float4 sm[];
@@ -506,26 +505,31 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
   const int n = 1 << log2nx;
   const dsf c2 = ds_from_double(fov * fov / ((double)n * n));
   auto pos = [&](int k, int q) { return (k << log2S) + q; };
-  float4 *stw = sm + kColPts;
+  // Two tiles: the next slice's tile is copied in while this one is
+  // transformed.
+  float4 *stw = sm + 2 * kColPts;
   stage_twiddles(stw, cg.log2N2);  // ordered before first use by the barrier after the first load
   float2 *snt = reinterpret_cast<float2 *>(stw + 128);  // kColPts per-pixel w-screen terms
+  auto issue = [&](int64_t pp, float4 *dst) {
+    const float4 *p = buf + ((pp - p0) << (log2ny + log2nx));
+    for (int t = threadIdx.x; t < kColPts; t += kColT) {
+      const int n2 = t >> log2S, q = t & S1;
+      const int k1 = k1_0 + (q >> cg.log2WC2);
+      cp_async16(dst + t, p + ((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2));
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
   dsf acc[kColNPT];
 #pragma unroll
   for (int m = 0; m < kColNPT; ++m) acc[m] = {0.f, 0.f};
-  float4 *cur = sm;
+  issue(p0, sm);
   for (int64_t pp = p0; pp < p1; ++pp) {
     const int64_t b = pp / K;
     const int s = (int)(pp - b * K);
-    {
-      const float4 *p = buf + ((pp - p0) << (log2ny + log2nx));
-      for (int t = threadIdx.x; t < kColPts; t += kColT) {
-        const int n2 = t >> log2S, q = t & S1;
-        const int k1 = k1_0 + (q >> cg.log2WC2);
-        cp_async16(cur + t, p + ((int64_t)((k1 << cg.log2N2) + n2) << log2nx) + x0 + (q & WC2));
-      }
-      cp_async_wait_all();
-    }
-    __syncthreads();  // this tile has landed
+    float4 *cur = ((pp - p0) & 1) ? sm + kColPts : sm;
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();  // this tile has landed, and every thread is done with the other one
+    if (pp + 1 < p1) issue(pp + 1, ((pp - p0) & 1) ? sm : sm + kColPts);
     ds_dif_cta<kColT>(cur, cg.log2N2, log2S, true, pos, TwShared{stw, cg.log2N2});
     const dsf w = ds_from_double(wmean[s]);
 #pragma unroll
@@ -548,7 +552,6 @@ k_dsfft_cols2_wstack(const float4 *__restrict__ buf, int log2ny, int log2nx, Col
       // Re(wb v) = wb.re v.re - wb.im v.im
       acc[m] = ds_add(acc[m], ds_sub(ds_mul_f({v.x, v.y}, wb.x), ds_mul_f({v.z, v.w}, wb.y)));
     }
-    __syncthreads();  // every thread is done with the tile before the next slice's copy
     if (pp + 1 == p1 || (pp + 1) / K != b) {
       const bool first = p0 <= b * K;
       float2 *out = slots + (b << (log2ny + log2nx));

@@ -56,6 +56,9 @@ def parse():
     ap.add_argument('--profile-rows', type=int, default=0,
                     help='profiling case for ncu: the workload subsampled to this many rows, --warmup + --steps '
                          'untimed steps with the library defaults, no other arms')
+    ap.add_argument('--wstack-profile', action='store_true',
+                    help='profiling case for ncu: a 2,000,000-row PSWF w-stack invert onto 4 slices of 4096^2 '
+                         '(FP32C, 2.3 GB on the device), run --warmup + --steps times, no other arms')
     ap.add_argument('--transform', type=int, default=0, metavar='N',
                     help='time the FP32C inverse 2-D transform with grid correction alone on two random N^2 '
                          'planes: the double-single FFT against cuFFT complex128 (also a small ncu case)')
@@ -778,6 +781,33 @@ def wstack_stages(torch, imager, stream):
     return {k: round(e[i].elapsed_time(e[i + 1]), 3) for i, k in enumerate(names)}
 
 
+def wstack_profile_case(args, torch):
+    """A w-stack invert small enough for a multi-pass ncu capture of its
+    transform passes: 2,000,000 seeded rows (uv uniform over the disk the grid
+    holds, w uniform in +/-2000 wavelengths) onto 4 slices of 4096^2, PSWF
+    S = 8, O = 16, FP32C."""
+    arl = importlib.import_module('algorithm-reference-library_gb300')
+    dev = torch.device('cuda', 0)
+    rng = numpy.random.default_rng(3)
+    N, cell, O, S, K, n = 4096, 5e-5, 16, 8, 4, 2_000_000
+    im = arl.create_image(npixel=N, cellsize=cell, frequency=numpy.array([1e8]), channel_bandwidth=numpy.array([1e6]),
+                          phasecentre=arl.PhaseCentre(0.0, -45.0))
+    gcfcf = arl.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    lim = (N // 2 - S // 2 - 2) / (N * cell)
+    r = lim * numpy.sqrt(rng.uniform(size=n))
+    th = rng.uniform(0, 2 * numpy.pi, n)
+    uvw = numpy.stack([r * numpy.cos(th), r * numpy.sin(th), rng.uniform(-2000, 2000, n)], axis=1)
+    dvis = arl.DeviceVisibility(torch.as_tensor(uvw, device=dev), torch.full((n,), 1e8, dtype=torch.float64, device=dev),
+                                torch.ones((n, 1), dtype=torch.complex64, device=dev),
+                                torch.ones((n, 1), dtype=torch.float32, device=dev))
+    imager = arl.WStackImager(dvis, im, K, gcfcf=gcfcf, precision='fp32c')
+    for _ in range(args.warmup + args.steps):
+        img, _ = imager.invert()
+    torch.cuda.synchronize()
+    return {'case': 'w-stack invert, %d rows, %d slices of %d^2, FP32C' % (n, K, N), 'calls': args.warmup + args.steps,
+            'image_max': float(img.abs().max()), 'device_gb': torch.cuda.max_memory_allocated() / 1e9}
+
+
 def arm_transform(args, torch):
     """ms per call of the FP32C inverse transform (grid correction and sumwt
     normalisation fused) on two random N^2 planes: the double-single FFT
@@ -893,6 +923,9 @@ def main():
         return
     if args.transform:
         print(json.dumps(arm_transform(args, torch)), flush=True)
+        return
+    if args.wstack_profile:
+        print(json.dumps(wstack_profile_case(args, torch)), flush=True)
         return
     world, rank, local = dist_setup(torch)
     if args.impl == 'reference':
