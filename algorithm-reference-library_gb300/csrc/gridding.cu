@@ -1379,41 +1379,53 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         // Groups of K warp steps: all tap loads of a group are in flight before
         // its first atomic.  Full groups of four run unmasked; the last 1 to 4
         // steps run as one group of exactly that many, masked per lane only in
-        // its partial last step.
-        auto group = [&](int t, auto kk, auto masked) {
-          constexpr int K = decltype(kk)::value;
-          int j[K];
-          bool on[K];
-          float2 tp[NPOL][K];
+        // its partial last step.  With one kernel for every polarisation
+        // (pol stride 0, as ARL's PSWF and w-kernels are) a tap is loaded once.
+        auto taps = [&](auto same) {
+          auto group = [&](int t, auto kk, auto masked) {
+            constexpr int K = decltype(kk)::value;
+            int j[K];
+            bool on[K];
+            float2 tp[NPOL][K];
   #pragma unroll
-          for (int u = 0; u < K; ++u) {
-            on[u] = !decltype(masked)::value || t + LP * u + hl < n;
-            j[u] = on[u] ? tj[t + LP * u] : 0;
+            for (int u = 0; u < K; ++u) {
+              on[u] = !decltype(masked)::value || t + LP * u + hl < n;
+              j[u] = on[u] ? tj[t + LP * u] : 0;
   #pragma unroll
-            for (int p = 0; p < NPOL; ++p)
-              tp[p][u] = on[u] ? kl[p * ps + t + LP * u + j[u] * dk] : make_float2(0.f, 0.f);
-          }
-  #pragma unroll
-          for (int u = 0; u < K; ++u) {
-            if (!on[u]) break;
-            const int so = wofs + t + LP * u + j[u] * dg;
-  #pragma unroll
-            for (int p = 0; p < NPOL; ++p) {
-              const float cx = tp[p][u].x * vw[p].x + tp[p][u].y * vw[p].y;  // conj(tap) * vw
-              const float cy = tp[p][u].x * vw[p].y - tp[p][u].y * vw[p].x;
-              fx_add<RESID>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
-              fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
+              for (int p = 0; p < NPOL; ++p)
+                tp[p][u] = decltype(same)::value && p > 0 ? tp[0][u]
+                           : on[u] ? kl[p * ps + t + LP * u + j[u] * dk] : make_float2(0.f, 0.f);
             }
+  #pragma unroll
+            for (int u = 0; u < K; ++u) {
+              if (!on[u]) break;
+              const int so = wofs + t + LP * u + j[u] * dg;
+  #pragma unroll
+              for (int p = 0; p < NPOL; ++p) {
+                const float cx = tp[p][u].x * vw[p].x + tp[p][u].y * vw[p].y;  // conj(tap) * vw
+                const float cy = tp[p][u].x * vw[p].y - tp[p][u].y * vw[p].x;
+                fx_add<RESID>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
+                fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
+              }
+            }
+          };
+          int t = 0;
+          for (; t + 4 * LP <= n; t += 4 * LP) group(t, IntC<4>(), BoolC<false>());
+          switch ((n - t + LP - 1) / LP) {
+            case 1: group(t, IntC<1>(), BoolC<true>()); break;
+            case 2: group(t, IntC<2>(), BoolC<true>()); break;
+            case 3: group(t, IntC<3>(), BoolC<true>()); break;
+            case 4: group(t, IntC<4>(), BoolC<true>()); break;
+            default: break;
           }
         };
-        int t = 0;
-        for (; t + 4 * LP <= n; t += 4 * LP) group(t, IntC<4>(), BoolC<false>());
-        switch ((n - t + LP - 1) / LP) {
-          case 1: group(t, IntC<1>(), BoolC<true>()); break;
-          case 2: group(t, IntC<2>(), BoolC<true>()); break;
-          case 3: group(t, IntC<3>(), BoolC<true>()); break;
-          case 4: group(t, IntC<4>(), BoolC<true>()); break;
-          default: break;
+        if constexpr (NPOL == 4) {  // two polarisations: the second path spills
+          if (ps == 0)
+            taps(BoolC<true>());
+          else
+            taps(BoolC<false>());
+        } else {
+          taps(BoolC<false>());
         }
       }
     };
@@ -1642,14 +1654,19 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   #pragma unroll
         for (int p = 0; p < NPOL; ++p) pa[p] = pb[p] = 0ull;
         const int wofs4 = (wv - sg.v0) * SG + (wu - sg.u0) + hl;
-        auto group2 = [&](int t, auto kk, auto masked) {
+        // With one kernel for every polarisation (pol stride 0) a tap is
+        // loaded once for all of them.
+        auto group2 = [&](int t, auto kk, auto masked, auto same) {
           constexpr int K = decltype(kk)::value;
           int j[K];
           bool on[K];
+          unsigned long long tp0[K];
   #pragma unroll
           for (int u = 0; u < K; ++u) {
             on[u] = !decltype(masked)::value || t + LP * u + hl < n;
             j[u] = on[u] ? tj[t + LP * u] : 0;
+            if (decltype(same)::value)
+              tp0[u] = on[u] ? *reinterpret_cast<const unsigned long long *>(kl + t + LP * u + j[u] * dk) : 0ull;
           }
   #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
@@ -1657,8 +1674,9 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
             ulonglong2 gv[K];
   #pragma unroll
             for (int u = 0; u < K; ++u) {
-              tp[u] = on[u] ? *reinterpret_cast<const unsigned long long *>(kl + p * ps + t + LP * u + j[u] * dk)
-                            : 0ull;
+              tp[u] = decltype(same)::value ? tp0[u]
+                      : on[u] ? *reinterpret_cast<const unsigned long long *>(kl + p * ps + t + LP * u + j[u] * dk)
+                              : 0ull;
               gv[u] = on[u] ? *reinterpret_cast<const ulonglong2 *>(sub4 + p * SG2 + wofs4 + t + LP * u + j[u] * dg)
                             : make_ulonglong2(0ull, 0ull);
             }
@@ -1669,15 +1687,26 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
             }
           }
         };
+        auto taps2 = [&](auto same) {
+          int t = 0;
+          for (; t + 4 * LP <= n; t += 4 * LP) group2(t, IntC<4>(), BoolC<false>(), same);
+          switch ((n - t + LP - 1) / LP) {
+            case 1: group2(t, IntC<1>(), BoolC<true>(), same); break;
+            case 2: group2(t, IntC<2>(), BoolC<true>(), same); break;
+            case 3: group2(t, IntC<3>(), BoolC<true>(), same); break;
+            case 4: group2(t, IntC<4>(), BoolC<true>(), same); break;
+            default: break;
+          }
+        };
         int t = 0;
         if (DUP && !direct) {
-          for (; t + 4 * LP <= n; t += 4 * LP) group2(t, IntC<4>(), BoolC<false>());
-          switch ((n - t + LP - 1) / LP) {
-            case 1: group2(t, IntC<1>(), BoolC<true>()); break;
-            case 2: group2(t, IntC<2>(), BoolC<true>()); break;
-            case 3: group2(t, IntC<3>(), BoolC<true>()); break;
-            case 4: group2(t, IntC<4>(), BoolC<true>()); break;
-            default: break;
+          if constexpr (NPOL > 1) {
+            if (ps == 0)
+              taps2(BoolC<true>());
+            else
+              taps2(BoolC<false>());
+          } else {
+            taps2(BoolC<false>());
           }
   #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
