@@ -38,6 +38,13 @@ struct RowMap {
 };
 
 // Geometry handed to the device kernels by value.
+// Row pitch of the fixed-point gridder's shared-memory subgrid.  An edge that
+// is a multiple of 32 four-byte words puts every row of a kernel window on the
+// same 32 banks, so the integer atomics of the rows a warp covers collide;
+// 8 words of padding shift consecutive rows by 8 banks, which lays four rows
+// of an 8-wide window (PSWF support 8) on distinct banks.
+__host__ __device__ constexpr int fx_pitch(int sg) { return sg % 32 == 0 ? sg + 8 : sg; }
+
 struct Geom {
   int32_t nchan, npol, nw, ny, nx;     // grid
   int32_t cf_nchan, cf_npol, nz, O, S; // cf

@@ -1246,7 +1246,9 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   __shared__ int s_red[2][NW * 6];
   // SGC != 0: the subgrid edge as a compile-time constant, so that plane
   // offsets in shared memory fold into the instructions' immediates.
-  const int SG = SGC ? SGC : g.SG, SG2 = SG * SG;
+  // Planes of SG rows of SP words (fx_pitch).
+  constexpr int SPC = SGC ? fx_pitch(SGC) : 0;
+  const int SG = SGC ? SGC : g.SG, SP = SPC ? SPC : fx_pitch(SG), SG2 = SG * SP;
   // Planar subgrid: integer plane (p, c) at subq + (2 p + c) SG2 (c = 0 real,
   // 1 imaginary); with RESID the residual-limb planes follow all of them.
   // The planes are zero between segments: the flush clears what it reads.
@@ -1375,7 +1377,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
           }
           continue;
         }
-        const int wofs = (wv - sg.v0) * SG + (wu - sg.u0) + hl, dg = SG - sz;
+        const int wofs = (wv - sg.v0) * SP + (wu - sg.u0) + hl, dg = SP - sz;
         // Groups of K warp steps: all tap loads of a group are in flight before
         // its first atomic.  Full groups of four run unmasked; the last 1 to 4
         // steps run as one group of exactly that many, masked per lane only in
@@ -1451,7 +1453,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       for (int y = box.y0 + warp; y < box.y1; y += NW) {
         const int gy = sg.v0 + y;
         for (int x = box.x0 + lane; x < box.x1; x += 32) {
-          const int gx = sg.u0 + x, cell = y * SG + x;
+          const int gx = sg.u0 + x, cell = y * SP + x;
 #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
             const int qx = subq[2 * p * SG2 + cell], qy = subq[(2 * p + 1) * SG2 + cell];
@@ -1882,7 +1884,7 @@ int make_geom(const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, int precisio
   }
   if (SG - g->S < 8) SG = ((g->S + 8 + 7) / 8) * 8;
   SG = (SG + 7) & ~7;  // a multiple of the band-owner warp count
-  if ((size_t)g->npol * SG * SG * cell > 200 * 1024)
+  if ((size_t)g->npol * SG * fx_pitch(SG) * cell > 200 * 1024)
     return fail(ARLGPU_ERR_UNSUPPORTED, "support %d with %d polarisations needs more shared memory than a CTA has",
                 g->S, g->npol);
   g->SG = SG;
@@ -2004,7 +2006,7 @@ static unsigned chunk_grid(K kern, size_t smem, int64_t nvis, uint32_t chunk) {
 
 static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const void *vis, const void *wt,
                           const void *cf, void *grid, double *sumwt, bool resid, cudaStream_t st) {
-  const size_t smem = (size_t)(resid ? 4 : 2) * g.npol * g.SG * g.SG * 4 + tap_table_bytes(g.S);
+  const size_t smem = (size_t)(resid ? 4 : 2) * g.npol * g.SG * fx_pitch(g.SG) * 4 + tap_table_bytes(g.S);
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
   void (*kern)(Geom, const RowMap *, const uint32_t *, const uint32_t *, uint32_t, const float2 *, const float *,
                const float2 *, float2 *, double *);
