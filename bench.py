@@ -855,8 +855,8 @@ def arm_transform(args, torch):
 
 def arm_reference(args, torch, world, rank):
     """The reference's CPU algorithm (the oracle's faithful per-row loops; the
-    reference itself is Python needing astropy, absent on the box) on all host
-    cores: one process per core, each on its own seeded row sample."""
+    reference itself is Python that needs astropy, which is not installed) on
+    all host cores: one process per core, each on its own seeded row sample."""
     if rank != 0:
         return None
     sim = importlib.import_module('algorithm-reference-library_gb300.simulation')
