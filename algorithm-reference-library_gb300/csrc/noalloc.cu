@@ -2,14 +2,14 @@
 // memory.
 //
 // Some callers of this library have no way to obtain scratch memory at the
-// moment they want to grid: code that is recording a CUDA graph (cudaMalloc is
-// not allowed while a stream is being captured), hosts whose device memory is
-// entirely owned by another framework's pool, and real-time pipelines that
-// allocate everything once at start-up and forbid allocation afterwards.  For
-// them this file keeps the gridder's scratch (the row plan: mapping, bin keys,
-// sorted row ids, bin histogram and offsets) in a fixed file-scope device
-// array, so the entry point needs nothing beyond the caller's inputs and
-// outputs.
+// moment they want to grid: hosts whose device memory is entirely owned by
+// another framework's pool (the pool hands out only the buffers it was asked
+// for at start-up), and real-time pipelines that allocate everything once
+// when they start and forbid allocation, with its possible implicit
+// synchronisation, afterwards.  For them this file keeps the gridder's
+// scratch (the row plan: mapping, bin keys, sorted row ids, bin histogram and
+// offsets) in a fixed file-scope device array, so the entry point needs
+// nothing beyond the caller's inputs and outputs.
 //
 // Costs and limits of that choice:
 //   * every GPU that loads the library holds kScratchBytes (about 22.0 MB) of
@@ -26,6 +26,9 @@
 //   * the device address of the array is looked up once per device (with
 //     cudaGetSymbolAddress), the first time the entry point runs with that
 //     device current.  Make that first call before any stream capture begins.
+//     The cached address belongs to the device's context at that time: after
+//     cudaDeviceReset the module is loaded again at another address, so this
+//     entry point must not be used across a device reset.
 #include <mutex>
 
 #include "common.cuh"
@@ -77,6 +80,13 @@ extern "C" int arlgpu_grid_noalloc(const double *uvw, const double *frequency, c
     return fail(ARLGPU_ERR_WORKSPACE,
                 "arlgpu_grid_noalloc takes at most %lld rows per call (got %lld); use arlgpu_grid with a workspace",
                 (long long)kMaxRows, (long long)nvis);
+  Geom g;
+  ARL_TRY(make_geom(gd, cd, precision, &g));
+  if ((int64_t)g.nbins > kMaxBins)
+    return fail(ARLGPU_ERR_WORKSPACE,
+                "arlgpu_grid_noalloc takes a plan of at most %lld bins per call (this grid has %u channel x "
+                "w-plane x uv-tile bins); use arlgpu_grid with a workspace",
+                (long long)kMaxBins, g.nbins);
   size_t need = 0;
   ARL_TRY(arlgpu_plan_workspace_bytes(nvis, gd, cd, &need));
   if (need > kScratchBytes)

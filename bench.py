@@ -51,6 +51,8 @@ def parse():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline')
     ap.add_argument('--cpu-seconds', type=float, default=12.0, help='CPU-baseline time budget')
     ap.add_argument('--no-tune', action='store_true', help='keep the library\'s default kernel variants')
+    ap.add_argument('--no-c5', action='store_true',
+                    help='skip the sub-record of the largest single-GPU workload (C5 w-stacking)')
     ap.add_argument('--no-stages', action='store_true',
                     help='skip the invert_2d / predict_2d / gradient-step rates')
     ap.add_argument('--profile-rows', type=int, default=0,
@@ -537,9 +539,31 @@ def cpu_model():
     return 'unknown'
 
 
-def oracle_errors(arl, torch, w, cf, ctx, nsub=20000):
-    """Max-norm and RMS error of the GPU grid and degrid (this context's
-    precision) against the complex128 oracle on a seeded row subsample."""
+def _err(a, b):
+    """Max-norm and RMS error of a against the oracle result b, each relative
+    to b's own max-norm / RMS."""
+    return {'max_rel': float(numpy.max(numpy.abs(a - b)) / numpy.max(numpy.abs(b))),
+            'rms_rel': float(numpy.sqrt(numpy.mean(numpy.abs(a - b) ** 2)) / numpy.sqrt(numpy.mean(numpy.abs(b) ** 2)))}
+
+
+def _img_err(a, b, gcf):
+    """Image error over the whole image and over the inner region where the
+    grid correction is <= 100 (the PSWF correction grows to ~6e4 at the field
+    edge and multiplies the FP32 rounding there)."""
+    e = _err(a, b)
+    inner = numpy.broadcast_to(gcf, b.shape) <= 100.0
+    d = numpy.abs(a - b)
+    e['inner_max_rel'] = float(d[inner].max() / numpy.max(numpy.abs(b)))
+    e['inner_fraction'] = float(inner.mean())
+    return e
+
+
+def oracle_errors(arl, torch, w, ctx, nsub=20000):
+    """Max-norm and RMS error against the complex128 oracle, on a seeded row
+    subsample of the workload, of every result the bench times on it: the
+    grid and the degridded rows (this context's precision, the oracle's own
+    w-kernels), the invert_2d image (plan + grid + inverse transform + grid
+    correction + sumwt normalisation) and the predict_2d rows of a model image."""
     from oracle import arl_oracle as orc
     dv = arl.device
     rng = numpy.random.default_rng(11)
@@ -547,14 +571,23 @@ def oracle_errors(arl, torch, w, cf, ctx, nsub=20000):
     sel = numpy.sort(rng.choice(n, min(nsub, n), replace=False))
     uvw, f = w['uvw'][sel], w['frequency'][sel]
     vis = w['vis'].cpu().numpy()[sel]
-    wt = w['weight'][sel]
+    wt = numpy.ones(vis.shape)
     img = orc.image_geometry(w['npixel'], w['cellsize'], len(w['freqs']), w['npol'], w['freqs'][0],
                              w['channel_bandwidth'])
+    nz = int(w.get('nwplanes', 1))
+    wstep = float(w.get('wstep', 1e15))
+    if w['kernel'] == 'wproj':
+        ogcf, ocf = orc.create_awterm_cf(img, nw=nz, wstep=wstep, oversampling=w['oversampling'],
+                                         support=w['support'])
+        ocf = orc.crop_cf_planes(ocf, w['plane_support'])
+    else:
+        ogcf, ocf = orc.create_pswf_cf(img['nchan'], img['npol'], img['ny'], img['nx'], w['oversampling'],
+                                       w['support'])
     gax = orc.grid_axes(img)
-    cax = orc.cf_axes(img, w['oversampling'], w['support'], nz=cf.shape[2], zstep=float(w.get('wstep', 1e15)))
+    cax = orc.cf_axes(img, w['oversampling'], w['support'], nz=nz, zstep=wstep)
     maps = orc.convolution_mapping(uvw, f, gax, cax)
-    g_ref, _ = orc.grid_vec(vis, wt, maps, cf, gax['shape'])
-    d_ref = orc.degrid_vec(g_ref, maps, cf)
+    g_ref, _ = orc.grid_vec(vis, wt, maps, ocf, gax['shape'])
+    d_ref = orc.degrid_vec(g_ref, maps, ocf)
     p = ctx['precision']
     dev = ctx['uvw'].device
     t_uvw = torch.as_tensor(uvw, device=dev)
@@ -566,11 +599,22 @@ def oracle_errors(arl, torch, w, cf, ctx, nsub=20000):
     d, _ = dv.degrid(t_uvw, t_f, gr, ctx['cf_t'], ctx['cd'], ctx['gd'], p)
     g = g.to(torch.complex128).cpu().numpy()
     d = d.to(torch.complex128).cpu().numpy()
-
-    def err(a, b):
-        return {'max_rel': float(numpy.max(numpy.abs(a - b)) / numpy.max(numpy.abs(b))),
-                'rms_rel': float(numpy.sqrt(numpy.mean(numpy.abs(a - b) ** 2)) / numpy.sqrt(numpy.mean(numpy.abs(b) ** 2)))}
-    return {'rows': int(sel.size), 'grid': err(g, g_ref), 'degrid': err(d, d_ref)}
+    out = {'rows': int(sel.size), 'precision': p, 'grid': _err(g, g_ref), 'degrid': _err(d, d_ref)}
+    # invert_2d and predict_2d through the package's public functions on the
+    # same rows (device-resident), against the oracle's invert_2d / predict_2d
+    dvis = arl.DeviceVisibility(t_uvw, t_f, t_v, t_w)
+    gcfcf = (ctx['gcf'], ctx['cf'])
+    dirty, _ = arl.invert_2d(dvis, ctx['im'], gcfcf=gcfcf, precision=p)
+    im_ref, _ = orc.invert_2d(uvw, f, vis, wt, img, ogcf, ocf, cax)
+    out['invert_2d'] = _img_err(dirty.data.cpu().numpy(), im_ref.real, ogcf)
+    model = numpy.zeros((img['nchan'], img['npol'], img['ny'], img['nx']))
+    c = img['ny'] // 2
+    model[..., c - 40:c + 40:7, c - 40:c + 40:5] = 1.0
+    mim = arl.Image(model, ctx['im'].wcs.deepcopy(), ctx['im'].polarisation_frame)
+    pv = arl.predict_2d(dvis, mim, gcfcf=gcfcf, precision=p)
+    p_ref = orc.predict_2d(uvw, f, model, img, ogcf, ocf, cax)
+    out['predict_2d'] = _err(pv.vis.to(torch.complex128).cpu().numpy(), p_ref)
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -637,11 +681,15 @@ def arm_gb300(args, torch, world, rank, local):
         stages['gradient_step'] = gradient_step_rate(arl, torch, device, 3, 2, flush)
     e2e_ms = max_over_ranks(torch, world, e2e_ms)
 
-    # Roofline of the dominant kernel (grid or degrid launch), HBM-bound.
+    # Roofline of the dominant kernel (grid or degrid launch), HBM-bound, with
+    # the algorithmic bytes of the gridding / degridding stage: each row's uvw
+    # (3 x f64), vis (c64 per pol), weight (f32 per pol, gridder only) and
+    # channel id (i32) read once, and every cell of the grid written (gridder)
+    # or read (degridder) once.
     npol = w['npol']
     gd = ctx['gd']
     grid_bytes = 8 * gd.ny * gd.nx * gd.npol * gd.nchan * gd.nw
-    alg = {'grid': n * (20 + 12 * npol) + grid_bytes, 'degrid': n * (20 + 8 * npol) + grid_bytes}
+    alg = {'grid': n * (24 + 8 * npol + 4 * npol + 4) + grid_bytes, 'degrid': n * (24 + 4 + 8 * npol) + grid_bytes}
     kern = 'grid' if r['grid_ms'] >= r['degrid_ms'] else 'degrid'
     kms = r[kern + '_ms']
     peak, peak_kind = measured_hbm()
@@ -677,7 +725,7 @@ def arm_gb300(args, torch, world, rank, local):
     }
     line.update(out)
     if rank == 0:
-        line['err_vs_oracle_fp32c'] = oracle_errors(arl, torch, w, ctx['cf'].data, ctx)
+        line['err_vs_oracle_fp32c'] = oracle_errors(arl, torch, w, ctx)
         if not args.no_cpu:
             cb = CpuBaseline(w, ctx['cf'].data, 1)
             rate, rows = cb.rate(args.cpu_seconds, 200000)
@@ -685,6 +733,10 @@ def arm_gb300(args, torch, world, rank, local):
                                     'sample': '%d rows of the workload through the oracle\'s per-row complex128 '
                                               'grid and degrid loops (%.0f s budget), %s' %
                                               (rows, args.cpu_seconds, cpu_model())}
+        if not args.no_c5:
+            del ctx
+            torch.cuda.empty_cache()
+            line['c5'] = wstack_record(torch, device)
     return line
 
 
@@ -754,6 +806,94 @@ def arm_wstack(args, torch, world, rank, local):
         line['fp64'] = res['fp64']
         line['fp32c_speedup'] = (res['fp64']['invert_ms'] + res['fp64']['predict_ms']) / ms
     return line
+
+
+def wstack_record(torch, device, name='C5', steps=2, warmup=1, nsub=20000):
+    """Sub-record of the default bench for the largest single-GPU workload
+    (C5: 100,466,688 rows onto 32 w-stack slices of 8192^2, PSWF 8 x 16),
+    FP32C: invert / predict rates, one staged pass with each stage's HBM
+    roofline (algorithmic bytes: grid nvis (24 + 12 npol + 4) + 8 N^2 npol P;
+    degrid nvis (24 + 4 + 8 npol) + 8 N^2 npol P; each of the P inverse / forward
+    transforms 2 x 8 N^2 npol), and the grid and degrid against the oracle on a
+    seeded row subsample (the cells the rows touch, and the rows' windows)."""
+    from oracle import arl_oracle as orc
+    arl = importlib.import_module('algorithm-reference-library_gb300')
+    sim = arl.simulation
+    w = sim.make_workload(name, device=device)
+    n = w['uvw'].shape[0]
+    im = sim.workload_image(arl, w)
+    gcfcf = arl.create_pswf_convolutionfunction(im, oversampling=w['oversampling'], support=w['support'])
+    model = torch.zeros((1, w['npol'], w['npixel'], w['npixel']), dtype=torch.float64, device=device)
+    c = w['npixel'] // 2
+    model[..., c - 200:c + 200:37, c - 200:c + 200:41] = 1.0
+    stream = torch.cuda.current_stream()
+    dvis = arl.DeviceVisibility(torch.as_tensor(w['uvw'], device=device),
+                                torch.as_tensor(w['frequency'], device=device), w['vis'].to(torch.complex64),
+                                torch.ones((n, w['npol']), dtype=torch.float32, device=device))
+    imager = arl.WStackImager(dvis, im, w['vis_slices'], gcfcf=gcfcf, precision='fp32c')
+    imager.set_model(model)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e = _events(torch, 2)
+        e[0].record(stream)
+        for _ in range(steps):
+            fn()
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]) / steps
+
+    t_inv = timed(lambda: imager.invert(replan=True))
+    t_pred = timed(lambda: imager.predict(replan=True))
+    st = wstack_stages(torch, imager, stream)
+    peak, peak_kind = measured_hbm()
+    npol, N, P = w['npol'], w['npixel'], w['vis_slices']
+    cells = 8 * N * N * npol * P
+    alg = {'grid': n * (24 + 12 * npol + 4) + cells, 'degrid': n * (28 + 8 * npol) + cells,
+           'g2i': 2 * cells, 'i2g': 2 * cells}
+    roof = {k: {'ms': st[k], 'algorithmic_bytes': b, 'achieved_gbs': b / (st[k] / 1e3) / 1e9,
+                'frac': b / (st[k] / 1e3) / 1e9 / peak} for k, b in alg.items()}
+    # oracle check on a seeded subsample, through the same imager geometry
+    rng = numpy.random.default_rng(55)
+    sel = numpy.sort(rng.choice(n, min(nsub, n), replace=False))
+    img = orc.image_geometry(N, w['cellsize'], len(w['image_frequency']), npol, w['image_frequency'][0],
+                             w['image_bandwidth'])
+    _, ocf = orc.create_pswf_cf(1, npol, 8, 8, w['oversampling'], w['support'])
+    vis64 = w['vis'][torch.as_tensor(sel, device=w['vis'].device)].cpu().numpy()
+    wt = numpy.ones(vis64.shape)
+    sub = arl.DeviceVisibility(torch.as_tensor(w['uvw'][sel], device=device),
+                               torch.as_tensor(w['frequency'][sel], device=device),
+                               torch.as_tensor(vis64, device=device).to(torch.complex64),
+                               torch.ones(vis64.shape, dtype=torch.float32, device=device))
+    del imager
+    torch.cuda.empty_cache()
+    simg = arl.WStackImager(sub, im, w['vis_slices'], gcfcf=gcfcf, precision='fp32c')
+    simg.grid()
+    gax = orc.grid_axes(img, nw=simg.vis_slices)
+    gax['w'] = simg.w_axis
+    cax = orc.cf_axes(img, w['oversampling'], w['support'])
+    maps = orc.convolution_mapping(w['uvw'][sel], w['frequency'][sel], gax, cax)
+    cells_i, vals, _ = orc.grid_sparse(vis64, wt, maps, ocf, gax['shape'])
+    flat = simg.grid_t.reshape(-1)
+    got = flat[torch.as_tensor(cells_i, device=device)].to(torch.complex128).cpu().numpy()
+    out = simg.predict(model)
+    idx = torch.as_tensor(orc.window_index(maps, gax['shape'], w['support']), device=device)
+    win = simg.grid_t.reshape(-1)[idx].to(torch.complex128).cpu().numpy()
+    d_ref = orc.degrid_windows(win, maps, ocf)
+    err = {'rows': int(sel.size), 'grid': _err(got, vals),
+           'degrid': _err(out.to(torch.complex128).cpu().numpy(), d_ref)}
+    del simg, sub, dvis, idx, flat, out
+    torch.cuda.empty_cache()
+    return {'workload': '%s: %d rows x %d pol, %d w-stack slices of %d^2, PSWF S=%d O=%d, FP32C' %
+                        (name, n, npol, P, N, w['support'], w['oversampling']),
+            'nvis': n, 'invert_ms': t_inv, 'predict_ms': t_pred, 'value': n / ((t_inv + t_pred) / 1e3),
+            'unit': 'vis/s (invert + predict)', 'invert_vis_s': n / (t_inv / 1e3),
+            'predict_vis_s': n / (t_pred / 1e3), 'stages_ms': st, 'roofline_stages': roof,
+            'peak_gbs': peak, 'peak_source': peak_kind + ' (MEASURED_PEAKS.json hbm_gbs)',
+            'err_vs_oracle_fp32c': err, 'steps': steps, 'warmup': warmup,
+            'l2': 'rows and grids exceed L2 (no flush needed)'}
 
 
 def wstack_stages(torch, imager, stream):

@@ -164,16 +164,18 @@ int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const arlgpu_grid_
 
 /* ---- Gridding without any device allocation (no counterpart in the reference,
  * whose gridder is a NumPy loop) ----
- * For callers that cannot allocate device memory when they grid (recording a
- * CUDA graph, a device pool owned by another framework, real-time code that
- * allocates only at start-up).  Same arguments and results as arlgpu_grid, minus
- * the workspace: the row plan lives in a fixed device array of ~22.0 MB that the
- * library holds on every GPU it runs on until the process exits.  At most 524,288
- * rows and 65,536 plan bins (channel x w-plane x uv-tile) per call; larger calls
- * fail with ARLGPU_ERR_WORKSPACE before any GPU work.  All calls share the array:
- * calls whose GPU work overlaps (other streams or threads) race on it.  The first
- * call on each device looks up the array's address; make it before any stream
- * capture begins.  No cudaMalloc / cudaFree is called. */
+ * For callers that cannot allocate device memory when they grid: hosts whose
+ * device memory is all owned by another framework's pool, and real-time code
+ * that allocates only at start-up.  Same arguments and results as arlgpu_grid,
+ * minus the workspace: the row plan lives in a fixed device array of ~22.0 MB
+ * that the library holds on every GPU it runs on until the process exits.  At
+ * most 524,288 rows and 65,536 plan bins (channel x w-plane x uv-tile) per call;
+ * larger calls fail with ARLGPU_ERR_WORKSPACE before any GPU work.  All calls
+ * share the array, which keeps the last call's contents: calls whose GPU work
+ * overlaps (other streams or threads) race on it.  The first call on each device
+ * looks up the array's address; make it before any stream capture begins, and
+ * do not use this entry point across a cudaDeviceReset.  No cudaMalloc /
+ * cudaFree is called. */
 int arlgpu_grid_noalloc(const double *uvw, const double *frequency, const void *vis, const void *weight,
                         int64_t nvis, int precision, const void *cf, const arlgpu_cf_desc *cd, void *grid,
                         const arlgpu_grid_desc *gd, double *sumwt, int64_t *n_bad_dev, void *stream);

@@ -118,3 +118,30 @@ def test_tuning_keys(nat):
     assert lib.arlgpu_set_tuning(b'no_such_key', 1) == INVALID
     assert lib.arlgpu_set_tuning(b'small_rows', 3) == INVALID
     assert lib.arlgpu_get_tuning(b'no_such_key', ctypes.byref(v)) != OK
+
+
+def test_noalloc_rejects_too_many_rows_or_bins(nat, descs):
+    """arlgpu_grid_noalloc checks its row limit and its bin limit on their own,
+    on the host, before any device access: a call with few rows but more than
+    65,536 plan bins fails like a call with too many rows."""
+    g, c = descs
+    lib = nat.load()
+    buf = ctypes.create_string_buffer(16)
+    ptr = ctypes.cast(buf, ctypes.c_void_p)
+
+    def call(nvis, gd):
+        return lib.arlgpu_grid_noalloc(ptr, ptr, ptr, ptr, nvis, FP32C, ptr, ctypes.byref(c), ptr, ctypes.byref(gd),
+                                       ptr, None, None)
+
+    assert call((1 << 19) + 1, g) == WORKSPACE
+    assert 'rows' in last_error(nat)
+    # 1024^2 grid: 26 x 26 uv-tiles of 40 pixels per (channel, w-plane); 100
+    # channels make 67,600 bins
+    big = type(g).from_buffer_copy(g)
+    big.nx = big.ny = 1024
+    big.nchan = 100
+    assert call(10, big) == WORKSPACE
+    assert 'bins' in last_error(nat)
+    big.nchan = 90  # 60,840 bins: accepted by both checks, fails only later
+    st = call(-1, big)
+    assert st == INVALID and 'nvis' in last_error(nat)

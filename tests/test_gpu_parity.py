@@ -353,6 +353,86 @@ def test_c2_full_size_properties(arl):
     assert numpy.max(numpy.abs(g2.data.to(torch.complex128).cpu().numpy() - 2 * g1)) <= 1e-6 * numpy.abs(g1).max()
 
 
+def _oracle_by_support(oracle, vis, wt, maps, ocf, gshape, supports, grid=None):
+    """The oracle's grid_vec / degrid_vec with each row's window cropped to its
+    plane's support: rows are grouped by the support of their cf plane and
+    each group runs on the centrally cropped table (the same taps and window
+    positions as the full S x S window, whose outer taps are zero).  Returns
+    (grid, sumwt) when grid is None, else the degridded rows of grid."""
+    pwc = maps[5]
+    S = ocf.shape[-1]
+    out = None
+    if grid is None:
+        out = numpy.zeros(gshape, dtype=numpy.complex128)
+        sumwt = numpy.zeros(gshape[:2])
+    else:
+        res = numpy.zeros((pwc.size, gshape[1]), dtype=numpy.complex128)
+    for sz in numpy.unique(supports):
+        rows = numpy.nonzero(supports[pwc] == sz)[0]
+        if rows.size == 0:
+            continue
+        lo = S // 2 - sz // 2
+        cfz = ocf[..., lo:lo + sz, lo:lo + sz]
+        m = tuple(a[rows] for a in maps)
+        if grid is None:
+            g, sw = oracle.grid_vec(vis[rows], wt[rows], m, cfz, gshape)
+            out += g
+            sumwt += sw
+        else:
+            res[rows] = oracle.degrid_vec(grid, m, cfz)
+    return (out, sumwt) if grid is None else res
+
+
+def test_c2_subsample_vs_oracle(arl, oracle):
+    """The bench workload's own geometry (C2: 4 channels onto 4 x 1024^2, 64
+    w-kernel planes with support 8 -> 32, O = 8) on a seeded 1,000,000-row
+    subsample: GPU grid and degrid, both precisions, against the oracle's
+    complex128 gridder and degridder with the oracle's own w-kernels."""
+    sim = __import__('importlib').import_module('algorithm-reference-library_gb300.simulation')
+    w = sim.make_workload('C2')
+    rng = numpy.random.default_rng(22)
+    n = w['uvw'].shape[0]
+    sel = numpy.sort(rng.choice(n, 1_000_000, replace=False))
+    img = oracle.image_geometry(w['npixel'], w['cellsize'], len(w['freqs']), w['npol'], w['freqs'][0],
+                                w['channel_bandwidth'])
+    _, ocf = oracle.create_awterm_cf(img, nw=w['nwplanes'], wstep=w['wstep'], oversampling=w['oversampling'],
+                                     support=w['support'])
+    ocf = oracle.crop_cf_planes(ocf, w['plane_support'])
+    gax = oracle.grid_axes(img)
+    cax = oracle.cf_axes(img, w['oversampling'], w['support'], nz=w['nwplanes'], zstep=w['wstep'])
+    uvw, f = w['uvw'][sel], w['frequency'][sel]
+    maps = oracle.convolution_mapping(uvw, f, gax, cax)
+    assert numpy.all(oracle.rows_in_grid(maps, gax['shape'], ocf.shape))
+    vis = w['vis'].numpy()[sel]
+    wt = numpy.ones(vis.shape)
+    supports = numpy.asarray(w['plane_support'])
+    g_ref, sw_ref = _oracle_by_support(oracle, vis, wt, maps, ocf, gax['shape'], supports)
+    d_ref = _oracle_by_support(oracle, vis, wt, maps, ocf, gax['shape'], supports, grid=g_ref)
+
+    im = make_image(arl, w['npixel'], w['cellsize'], w['freqs'], w['channel_bandwidth'])
+    _, cf = arl.create_awterm_convolutionfunction(im, nw=w['nwplanes'], wstep=w['wstep'],
+                                                  oversampling=w['oversampling'], support=w['support'],
+                                                  plane_support=w['plane_support'])
+    assert rel(cf.data, ocf) < 1e-12
+    dv = arl.device
+    dev = torch.device('cuda')
+    gd = dv.grid_desc(arl.kernels._grid_wcs(im, 1, 1e15), gax['shape'])
+    for p in ('fp64', 'fp32c'):
+        cf_t, cs, ps, psup = dv.device_cf(cf, p, dev)
+        cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
+        t_uvw = torch.as_tensor(uvw, device=dev)
+        t_f = torch.as_tensor(f, device=dev)
+        g, sw, nbad = dv.grid(t_uvw, t_f, torch.as_tensor(vis, device=dev).to(dv.CDTYPE[p]),
+                              torch.as_tensor(wt, device=dev).to(dv.RDTYPE[p]), cf_t, cd, gd, p)
+        assert int(nbad.item()) == 0
+        assert rel(g.to(torch.complex128).cpu().numpy(), g_ref) < TOL[p], p
+        assert numpy.allclose(sw.cpu().numpy(), sw_ref, rtol=1e-12)
+        d, _ = dv.degrid(t_uvw, t_f, torch.as_tensor(g_ref, device=dev).to(dv.CDTYPE[p]), cf_t, cd, gd, p)
+        assert rel(d.to(torch.complex128).cpu().numpy(), d_ref) < TOL[p], p
+        del g, d, cf_t
+        torch.cuda.empty_cache()
+
+
 @pytest.mark.parametrize('grid_kernel,degrid_kernel,subgrid,chunk', [
     (0, 0, 48, 512), (1, 1, 0, 512), (2, 2, 32, 2048), (2, 2, 0, 512), (3, 0, 0, 512), (4, 2, 0, 512),
     (4, 2, 32, 2048), (5, 2, 0, 512), (4, 3, 0, 512), (2, 3, 0, 2048)])

@@ -1,8 +1,10 @@
 """arlgpu_grid_noalloc: the gridder for callers that cannot allocate device
-memory (graph capture, externally owned device pools, real-time code).  Called
-through the C ABI and checked against arlgpu_grid, which grids the same rows
-with a caller-provided workspace, on two calls in a row (the second call finds
-the first call's plan still in the shared scratch array).
+memory when they grid (device memory owned by another framework's pool,
+real-time code that allocates only at start-up).  Called through the C ABI
+and checked against arlgpu_grid, which grids the same rows with a
+caller-provided workspace.  The shared scratch array keeps the previous
+call's plan, so the check runs after a call on a different case (more rows,
+other uv values, a larger grid with more bins), and twice in a row.
 
 Kept in a file that pytest collects last, so a failure here cannot stop the
 rest of the suite from running first."""
@@ -40,6 +42,31 @@ def case(arl):
     return arl, t, gd, cd, cf_t, n
 
 
+@pytest.fixture(scope='module')
+def other_case(arl):
+    """A different call for the shared scratch: 400,000 rows with other uv
+    values on a 512^2 grid (a larger plan with more bins than `case`)."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    rng = numpy.random.default_rng(7)
+    N, cell, O, S, n = 512, 1e-3, 8, 8, 400000
+    im = arl.create_image(npixel=N, cellsize=cell, frequency=numpy.array([1e8, 1.1e8]),
+                          channel_bandwidth=numpy.array([1e7]), phasecentre=arl.PhaseCentre(0.0, -45.0))
+    _, cf = arl.create_pswf_convolutionfunction(im, oversampling=O, support=S)
+    dev = torch.device('cuda')
+    lim = (N // 2 - S // 2 - 2) / (N * cell)
+    uvw = numpy.stack([rng.uniform(-lim, lim, n), rng.uniform(-lim, lim, n), rng.uniform(-50, 50, n)], axis=1)
+    freq = rng.choice([1e8, 1.1e8], n)
+    t = dict(uvw=torch.as_tensor(uvw, device=dev), freq=torch.as_tensor(freq, device=dev),
+             vis=torch.as_tensor(rng.normal(size=(n, 1)) + 1j * rng.normal(size=(n, 1)), device=dev).to(
+                 torch.complex64),
+             wt=torch.as_tensor(rng.uniform(0.5, 2, (n, 1)), device=dev).to(torch.float32))
+    gd = arl.device.grid_desc(arl.kernels._grid_wcs(im, 1, 1e15), (2, 1, 1, N, N))
+    cf_t, cs, ps, psup = arl.device.device_cf(cf, 'fp32c', dev)
+    cd = arl.device.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
+    return arl, t, gd, cd, cf_t, n
+
+
 def _grid(arl, t, gd, cd, cf_t, n, noalloc):
     nat = arl._native
     lib = nat.load()
@@ -59,10 +86,18 @@ def _grid(arl, t, gd, cd, cf_t, n, noalloc):
     return grid.to(torch.complex128).cpu().numpy(), sumwt.cpu().numpy(), int(nbad.item())
 
 
-def test_noalloc_matches_workspace_gridder_twice(case):
+def test_noalloc_matches_workspace_gridder_twice(case, other_case):
     arl, t, gd, cd, cf_t, n = case
     ref, ref_sw, ref_bad = _grid(arl, t, gd, cd, cf_t, n, noalloc=False)
     assert ref_bad == 0
+    # Leave a different, larger plan in the shared scratch first (and check
+    # that call too): a part of the plan the next call failed to rewrite would
+    # then hold wrong values.
+    o_ref, o_sw, _ = _grid(*other_case, noalloc=False)
+    o_got, o_sw2, o_bad = _grid(*other_case, noalloc=True)
+    assert o_bad == 0
+    assert numpy.max(numpy.abs(o_got - o_ref)) / numpy.max(numpy.abs(o_ref)) < 1e-5
+    assert numpy.allclose(o_sw2, o_sw, rtol=1e-12)
     for _ in range(2):
         got, sw, bad = _grid(arl, t, gd, cd, cf_t, n, noalloc=True)
         assert bad == 0
