@@ -18,7 +18,8 @@ from .gridding import (DeviceVisibility, convolution_mapping, degrid_visibility_
                        fft_griddata_to_image, fft_image_to_griddata, grid_visibility_to_griddata)
 from .imaging import (imaging_context, imaging_contexts, invert_2d, invert_list_serial_workflow,  # noqa: F401
                       invert_wstack, invert_wstack_single, normalize_sumwt, predict_2d, predict_list_serial_workflow,
-                      predict_wstack, predict_wstack_single, shift_vis_to_image, vis_null_iter, vis_wslice_iter)
+                      predict_wstack, predict_wstack_single, phaserotate_visibility, shift_vis_to_image,
+                      vis_null_iter, vis_wslice_iter)
 from . import autograd, simulation, tune  # noqa: F401
 from .kernels import (apply_bounding_box_convolutionfunction, calculate_bounding_box_convolutionfunction,  # noqa: F401
                       copy_convolutionfunction, copy_griddata, create_awterm_convolutionfunction,
@@ -31,7 +32,8 @@ from .weighting import (grid_weight_to_griddata, griddata_merge_weights, griddat
                         weight_visibility)
 from .coalesce import (convert_blockvisibility_to_visibility, convert_visibility_to_blockvisibility,  # noqa: F401
                        decoalesce_visibility)
-from .data_models import Skycomponent, copy_blockvisibility  # noqa: F401
+from .data_models import GainTable, ReceptorFrame, Skycomponent, copy_blockvisibility  # noqa: F401
+from .calibration import apply_gaintable, vis_timeslice_iter  # noqa: F401
 from .skycomponents import predict_skycomponent_visibility  # noqa: F401
 from .deconvolution import deconvolve_cube, hogbom, msclean  # noqa: F401
 

@@ -65,6 +65,9 @@ SIGNATURES = {
     'arlgpu_dft_adjoint': (ctypes.c_int, [_vp, _i64, _vp, _i32, _i32, ctypes.c_int, _vp, _vp, _vp]),
     'arlgpu_hogbom': (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _f64, _f64, _i32, _f64, _f64, _f64,
                                      _vp, _vp, _P(_i32), _vp]),
+    'arlgpu_msclean_setup_bytes': (ctypes.c_int, [_i32, _i32, _i32, _i32, _i32, _P(_sz)]),
+    'arlgpu_msclean_setup': (ctypes.c_int, [_vp, _i32, _i32, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp,
+                                            _vp, _vp, _vp, _sz, _vp]),
     'arlgpu_msclean': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _f64, _f64, _i32, _vp,
                                       _P(_i32), _vp]),
     'arlgpu_wstack_fftbuf_bytes': (ctypes.c_int, [_P(GridDesc), _P(ctypes.c_size_t)]),
@@ -76,6 +79,8 @@ SIGNATURES = {
     'arlgpu_make_pswf': (ctypes.c_int, [_i32, _i32, _i32, _i32, _vp, _vp, _vp]),
     'arlgpu_make_wkernels': (ctypes.c_int, [_i32, _f64, _i32, _i32, _i32, _i32, _f64, _vp, _vp]),
     'arlgpu_apply_gains': (ctypes.c_int, [_vp, _i64, _i32, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, _vp]),
+    'arlgpu_apply_gaintable': (ctypes.c_int, [_vp, _i32, _i32, _i32, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int,
+                                              _vp]),
     'arlgpu_gain_chi2': (ctypes.c_int, [_vp, _vp, _vp, _i64, _i32, ctypes.c_int, _vp, _vp, _vp, _i32, _vp, _vp,
                                         _vp, _vp]),
     'arlgpu_phaserotate': (ctypes.c_int, [_vp, _vp, _i64, _i32, ctypes.c_int, _f64, _f64, ctypes.c_int, _vp]),

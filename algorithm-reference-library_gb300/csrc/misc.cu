@@ -116,6 +116,48 @@ __global__ void k_gain_chi2(const CT *__restrict__ vobs, const CT *__restrict__ 
       }
 }
 
+// apply_gaintable with scalar gains on a BlockVisibility (one polarisation):
+// cell [t][i][j][c] of the block, for a time t with a gain-table row
+// k = time_row[t] >= 0, becomes V * g[k][i][c] conj(g[k][j][c]), where g is the
+// gain or, for the inverse, 1/gain where |gain| > 0 and 1 elsewhere
+// (operations.py:124-137); the cell is zeroed where the product of the two
+// antennas' gain weights is 0 (:138-140).  Times with time_row[t] < 0 are
+// left as they are.
+template <typename CT>
+__global__ void k_gaintable(CT *vis, int ntimes, int nant, int nchan, const int32_t *__restrict__ time_row,
+                            const double2 *__restrict__ g, const double *__restrict__ gw, int inverse) {
+  const int64_t ncell = (int64_t)ntimes * nant * nant * nchan;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < ncell; q += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(q % nchan);
+    int64_t r = q / nchan;
+    const int j = (int)(r % nant);
+    r /= nant;
+    const int i = (int)(r % nant);
+    const int t = (int)(r / nant);
+    const int k = time_row[t];
+    if (k < 0) continue;
+    const int64_t gi = ((int64_t)k * nant + i) * nchan + c, gj = ((int64_t)k * nant + j) * nchan + c;
+    double2 ga = g[gi], gb = g[gj];
+    if (inverse) {
+      const double na = ga.x * ga.x + ga.y * ga.y, nb = gb.x * gb.x + gb.y * gb.y;
+      ga = na > 0.0 ? make_double2(ga.x / na, -ga.y / na) : make_double2(1.0, 0.0);
+      gb = nb > 0.0 ? make_double2(gb.x / nb, -gb.y / nb) : make_double2(1.0, 0.0);
+    }
+    CT v = vis[q];
+    if (gw[gi] * gw[gj] == 0.0) {
+      v.x = 0;
+      v.y = 0;
+    } else {
+      // m = ga conj(gb), then V m
+      const double mr = ga.x * gb.x + ga.y * gb.y, mi = ga.y * gb.x - ga.x * gb.y;
+      const double re = (double)v.x * mr - (double)v.y * mi, im = (double)v.x * mi + (double)v.y * mr;
+      v.x = re;
+      v.y = im;
+    }
+    vis[q] = v;
+  }
+}
+
 static int nblk(int64_t n) {
   int64_t b = (n + 255) / 256;
   return (int)(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
@@ -152,6 +194,28 @@ extern "C" int arlgpu_apply_gains(void *vis, int64_t nvis, int32_t npol, int pre
     k_gains<double2><<<nblk(nvis), 256, 0, st>>>(static_cast<double2 *>(vis), nvis, npol, a1, a2, g, inverse);
   else if (precision == ARLGPU_FP32C)
     k_gains<float2><<<nblk(nvis), 256, 0, st>>>(static_cast<float2 *>(vis), nvis, npol, a1, a2, g, inverse);
+  else
+    return fail(ARLGPU_ERR_INVALID, "bad precision");
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  return ARLGPU_OK;
+}
+
+extern "C" int arlgpu_apply_gaintable(void *vis, int32_t ntimes, int32_t nants, int32_t nchan, int precision,
+                                      const int32_t *time_row, const void *gain, const double *gain_weight,
+                                      int inverse, void *stream) {
+  if (ntimes < 0 || nants < 1 || nchan < 1) return fail(ARLGPU_ERR_INVALID, "bad block shape");
+  const int64_t ncell = (int64_t)ntimes * nants * nants * nchan;
+  if (ncell == 0) return ARLGPU_OK;
+  if (!vis || !time_row || !gain || !gain_weight) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const double2 *g = static_cast<const double2 *>(gain);
+  if (precision == ARLGPU_FP64)
+    k_gaintable<double2><<<nblk(ncell), 256, 0, st>>>(static_cast<double2 *>(vis), ntimes, nants, nchan, time_row, g,
+                                                      gain_weight, inverse);
+  else if (precision == ARLGPU_FP32C)
+    k_gaintable<float2><<<nblk(ncell), 256, 0, st>>>(static_cast<float2 *>(vis), ntimes, nants, nchan, time_row, g,
+                                                     gain_weight, inverse);
   else
     return fail(ARLGPU_ERR_INVALID, "bad precision");
   ARL_LAUNCH_CHECK();

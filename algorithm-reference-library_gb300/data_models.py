@@ -289,6 +289,80 @@ class Skycomponent:
         return self.flux.shape[1]
 
 
+class ReceptorFrame:
+    """Receptors of a gain table (``data_models/polarisation.py`` ReceptorFrame):
+    'circular' (R, L), 'linear' (X, Y) or 'stokesI' (I)."""
+    _frames = {'circular': ('R', 'L'), 'linear': ('X', 'Y'), 'stokesI': ('I',)}
+
+    def __init__(self, name):
+        if name not in self._frames:
+            raise ValueError('Unknown receptor frame %s' % str(name))
+        self.type = name
+
+    @property
+    def nrec(self):
+        return len(self._frames[self.type])
+
+
+class GainTable:
+    """Antenna gains over time (``memory_data_models.py`` GainTable): ARL's
+    structured array with one record per solution time: gain [nants, nchan,
+    nrec, nrec] complex, weight [nants, nchan, nrec, nrec], residual [nchan,
+    nrec, nrec], time and interval (seconds).  V_obs = g_i g_j^* V_model."""
+
+    def __init__(self, data=None, gain=None, time=None, interval=None, weight=None, residual=None, frequency=None,
+                 receptor_frame=ReceptorFrame('linear'), phasecentre=None, configuration=None):
+        if data is None and gain is not None:
+            nrec = receptor_frame.nrec
+            nrows, nants, nchan = gain.shape[0], gain.shape[1], gain.shape[2]
+            assert len(frequency) == nchan, 'Discrepancy in frequency channels'
+            desc = [('gain', 'c16', (nants, nchan, nrec, nrec)), ('weight', 'f8', (nants, nchan, nrec, nrec)),
+                    ('residual', 'f8', (nchan, nrec, nrec)), ('time', 'f8'), ('interval', 'f8')]
+            data = numpy.zeros(shape=[nrows], dtype=desc)
+            data['gain'] = gain
+            data['weight'] = weight
+            data['time'] = time
+            data['interval'] = interval
+            data['residual'] = residual
+        self.data = data
+        self.frequency = numpy.asarray(frequency, dtype=numpy.float64)
+        self.receptor_frame = receptor_frame
+        self.phasecentre = phasecentre
+        self.configuration = configuration
+
+    @property
+    def time(self):
+        return self.data['time']
+
+    @property
+    def interval(self):
+        return self.data['interval']
+
+    @property
+    def gain(self):
+        return self.data['gain']
+
+    @property
+    def weight(self):
+        return self.data['weight']
+
+    @property
+    def ntimes(self):
+        return self.data['gain'].shape[0]
+
+    @property
+    def nants(self):
+        return self.data['gain'].shape[1]
+
+    @property
+    def nchan(self):
+        return self.data['gain'].shape[2]
+
+    @property
+    def nrec(self):
+        return self.receptor_frame.nrec
+
+
 class Image:
     """Image [nchan, npol, ny, nx] with its WCS (``memory_data_models.py:349-434``)."""
 

@@ -5,12 +5,14 @@ Reference behaviour:
   msclean and its helpers   processing_library/arrays/cleaners.py:165-440
   deconvolve_cube           processing_components/image/deconvolution.py:43-300 ('hogbom', 'msclean')
 
-The minor cycles run on the device (``csrc/clean.cu``) in FP64 with the
-reference's operation order, so components and residuals equal NumPy's bit
-for bit.  The multiscale set-up (scale images, their FFT convolutions with
-the dirty image and the PSF, the coupling matrix) is NumPy on the host, as
-the reference computes it, so the device loop starts from identical values.
-deconvolve_cube's other algorithms raise NotImplementedError.
+Everything runs on the device.  The Hogbom minor cycle (``csrc/clean.cu``)
+is FP64 in the reference's operation order, so components and residuals
+equal NumPy's bit for bit.  The multiscale set-up (scale images, their
+convolutions with the dirty image and the PSF as complex128 cuFFT transforms,
+the coupling matrix, the window stack) is ``csrc/msclean_setup.cu``; it
+rounds differently from NumPy's FFTs, so msclean agrees with the reference to
+a stated FP64 tolerance rather than bit for bit.  deconvolve_cube's other
+algorithms raise NotImplementedError.
 """
 import ctypes
 
@@ -59,126 +61,48 @@ def hogbom(dirty, psf, window, gain, thresh, niter, fracthresh, prefix=''):
     return comps.cpu().numpy(), res.cpu().numpy()
 
 
-# Schwab's rational approximation (m = 6, alpha = 1) as msclean evaluates it
-# (``cleaners.py:398-440``), one scalar at a time.
-_SPH_P = ((8.203343e-2, -3.644705e-1, 6.278660e-1, -5.335581e-1, 2.312756e-1),
-          (4.028559e-3, -3.697768e-2, 1.021332e-1, -1.201436e-1, 6.412774e-2))
-_SPH_Q = ((1.0000000, 8.212018e-1, 2.078043e-1), (1.0000000, 9.599102e-1, 2.918724e-1))
-
-
-def _spheroidal(vnu):
-    if 0.0 <= vnu < 0.75:
-        part, nuend = 0, 0.75
-    elif 0.75 <= vnu <= 1.0:
-        part, nuend = 1, 1.0
-    else:
-        return 0.0
-    top = _SPH_P[part][0]
-    bot = _SPH_Q[part][0]
-    d = vnu ** 2 - nuend ** 2
-    for k in range(1, 5):
-        top += _SPH_P[part][k] * d ** k
-    for k in range(1, 3):
-        bot += _SPH_Q[part][k] * d ** k
-    value = top / bot if bot != 0.0 else 0.0
-    return value if value >= 0.0 else 0.0
-
-
-def create_scalestack(scaleshape, scales, norm=True):
-    """``cleaners.py:283-316``: [nscales, nx, ny] stack of the scale basis images."""
-    assert scaleshape[0] == len(scales)
-    basis = numpy.zeros(scaleshape)
-    nx, ny = scaleshape[1], scaleshape[2]
-    xcen = int(numpy.ceil(float(nx) / 2.0))
-    ycen = int(numpy.ceil(float(ny) / 2.0))
-    for iscale in numpy.arange(0, len(scales)):
-        halfscale = int(numpy.ceil(scales[iscale] / 2.0))
-        if scales[iscale] > 0.0:
-            rscale2 = 1.0 / (float(scales[iscale]) / 2.0) ** 2
-            for y in range(ycen - halfscale - 1, ycen + halfscale + 1):
-                for x in range(xcen - halfscale - 1, xcen + halfscale + 1):
-                    fx = float(x - xcen)
-                    fy = float(y - ycen)
-                    r2 = rscale2 * (fx * fx + fy * fy)
-                    r = numpy.sqrt(r2)
-                    basis[iscale, x, y] = _spheroidal(r) * (1.0 - r ** 2)
-            basis[basis < 0.0] = 0.0
-            if norm:
-                basis[iscale, :, :] /= numpy.sum(basis[iscale, :, :])
-        else:
-            basis[iscale, xcen, ycen] = 1.0
-    return basis
-
-
-def _fft2c(a):
-    return numpy.fft.fftshift(numpy.fft.fft2(numpy.fft.fftshift(a)))
-
-
-def convolve_scalestack(scalestack, img):
-    """``cleaners.py:319-335``."""
-    convolved = numpy.zeros(scalestack.shape)
-    ximg = _fft2c(img)
-    for iscale in range(scalestack.shape[0]):
-        xmult = ximg * numpy.conjugate(_fft2c(scalestack[iscale, :, :]))
-        convolved[iscale, :, :] = numpy.real(numpy.fft.ifftshift(numpy.fft.ifft2(numpy.fft.ifftshift(xmult))))
-    return convolved
-
-
-def convolve_convolve_scalestack(scalestack, img):
-    """``cleaners.py:338-360``: [nscales, nscales, nx, ny]."""
-    nscales, nx, ny = scalestack.shape
-    convolved = numpy.zeros([nscales, nscales, nx, ny])
-    ximg = _fft2c(img)
-    xscale = numpy.zeros([nscales, nx, ny], dtype='complex')
-    for s in range(nscales):
-        xscale[s] = _fft2c(scalestack[s, ...])
-    for s in range(nscales):
-        for p in range(nscales):
-            xmult = ximg * xscale[p] * numpy.conjugate(xscale[s])
-            convolved[s, p, ...] = numpy.real(numpy.fft.ifftshift(numpy.fft.ifft2(numpy.fft.ifftshift(xmult))))
-    return convolved
-
-
 def msclean(dirty, psf, window, gain, thresh, niter, scales, fracthresh, prefix=''):
-    """``cleaners.py:165-280``: (component array, residual array); the set-up on
-    the host as the reference forms it, the minor cycle on the device."""
+    """``cleaners.py:165-280``: (component array, residual array).  The set-up
+    (``arlgpu_msclean_setup``) and the minor cycle (``arlgpu_msclean``) run on
+    the device; dirty / psf / window are arrays or CUDA tensors."""
     assert 0.0 < gain < 2.0
     assert niter > 0
     assert len(scales) > 0
     device = dv.require_cuda()
-    dirty = numpy.asarray(dirty, dtype=numpy.float64)
-    psf = numpy.asarray(psf, dtype=numpy.float64)
-    pmax = psf.max()
-    assert pmax > 0.0
-    lpsf = psf / pmax
-    ldirty = dirty / pmax
-    scalestack = create_scalestack([len(scales), ldirty.shape[0], ldirty.shape[1]], scales, norm=True)
-    pscalestack = create_scalestack([len(scales), lpsf.shape[0], lpsf.shape[1]], scales, norm=True)
-    res_scalestack = convolve_scalestack(scalestack, numpy.array(ldirty))
-    psf_scalescalestack = convolve_convolve_scalestack(pscalestack, numpy.array(lpsf))
+    d = _plane(dirty, device)
+    p = _plane(psf, device)
+    w = None if window is None else _plane(window, device)
     ns = len(scales)
-    coupling = numpy.zeros([ns, ns])
-    for i in range(ns):
-        for j in range(ns):
-            coupling[i, j] = numpy.max(psf_scalescalestack[i, j, :, :])
-    if window is None:
-        windowstack = None
-    else:
-        windowstack = numpy.zeros_like(scalestack)
-        windowstack[convolve_scalestack(scalestack, window) > 0.9] = 1.0
-        assert numpy.sum(windowstack) > 0
-    absolutethresh = max(thresh, fracthresh * numpy.fabs(res_scalestack[0, :, :]).max())
-    stack_t = torch.as_tensor(res_scalestack).to(device)
-    pss_t = torch.as_tensor(psf_scalescalestack).to(device)
-    ps_t = torch.as_tensor(pscalestack).to(device)
-    ws_t = None if windowstack is None else torch.as_tensor(windowstack).to(device)
-    cm_t = torch.as_tensor(coupling).to(device)
-    comps = torch.empty(dirty.shape, dtype=torch.float64, device=device)
+    nx, ny = d.shape
+    pnx, pny = p.shape
+    sc = (ctypes.c_double * ns)(*[float(x) for x in scales])
+    nb = ctypes.c_size_t(0)
+    nat.call('arlgpu_msclean_setup_bytes', nx, ny, pnx, pny, ns, ctypes.byref(nb))
+    ws = dv.WORKSPACE.get(nb.value, device)
+    f64 = dict(dtype=torch.float64, device=device)
+    stack = torch.empty((ns, nx, ny), **f64)
+    pss = torch.empty((ns, ns, pnx, pny), **f64)
+    pscale = torch.empty((ns, pnx, pny), **f64)
+    wstack = None if w is None else torch.empty((ns, nx, ny), **f64)
+    coupling = torch.empty((ns, ns), **f64)
+    scalars = torch.empty(2, **f64)
+    nat.call('arlgpu_msclean_setup', nat.ptr(d), nx, ny, nat.ptr(p), pnx, pny, nat.ptr(w), sc, ns, nat.ptr(stack),
+             nat.ptr(pss), nat.ptr(pscale), nat.ptr(wstack), nat.ptr(coupling), nat.ptr(scalars), nat.ptr(ws),
+             ws.numel(), nat.stream_ptr())
+    pmax, res0max = (float(x) for x in scalars.cpu())
+    assert pmax > 0.0
+    if wstack is not None:
+        assert float(wstack.sum().item()) > 0
+    absolutethresh = max(thresh, fracthresh * res0max)
+    comps = torch.empty((nx, ny), **f64)
     iters = ctypes.c_int32(0)
-    nat.call('arlgpu_msclean', nat.ptr(stack_t), nat.ptr(pss_t), nat.ptr(ps_t), nat.ptr(ws_t), nat.ptr(cm_t), ns,
-             dirty.shape[0], dirty.shape[1], psf.shape[0], psf.shape[1], float(gain), float(absolutethresh),
-             int(niter), nat.ptr(comps), ctypes.byref(iters), nat.stream_ptr())
-    return comps.cpu().numpy(), pmax * stack_t[0].cpu().numpy()
+    nat.call('arlgpu_msclean', nat.ptr(stack), nat.ptr(pss), nat.ptr(pscale), nat.ptr(wstack), nat.ptr(coupling), ns,
+             nx, ny, pnx, pny, float(gain), float(absolutethresh), int(niter), nat.ptr(comps), ctypes.byref(iters),
+             nat.stream_ptr())
+    res = stack[0] * pmax
+    if isinstance(dirty, torch.Tensor):
+        return comps, res
+    return comps.cpu().numpy(), res.cpu().numpy()
 
 
 def deconvolve_cube(dirty, psf, prefix='', **kwargs):

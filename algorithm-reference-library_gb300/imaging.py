@@ -49,37 +49,56 @@ def normalize_sumwt(im, sumwt):
     return im
 
 
-def _image_phasecentre_offset(vis, im):
-    pc = getattr(vis, 'phasecentre', None)
-    if pc is None:
-        return None
-    ipc = im.phasecentre
-    if ipc.separation_rad(pc) > 1e-15:
-        return ipc.lmn(pc)
-    return None
+def phaserotate_visibility(vis, newphasecentre, tangent=True, inverse=False):
+    """``visibility/base.py:295-381`` on the tangent plane: a copy of ``vis``
+    whose rows are multiplied by conj(exp(-2 pi i (u l + v m + w (n - 1)))) (by
+    the phasor itself with ``inverse``), (l, m, n - 1) the direction cosines of
+    ``newphasecentre`` relative to ``vis.phasecentre``; ``vis`` itself when
+    |n - 1| < 1e-15.  Visibility, DeviceVisibility or BlockVisibility (per
+    channel uvw = metres x f / c).  The rotation runs on the GPU in FP64
+    phase.  ``tangent=False`` (re-projected uvw) raises NotImplementedError."""
+    if not tangent:
+        raise NotImplementedError('phaserotate_visibility: only tangent-plane rotation runs on the GB300 path')
+    l, m, n1 = newphasecentre.lmn(vis.phasecentre)
+    if numpy.abs(n1) < 1e-15:
+        return vis
+    device = dv.require_cuda()
+    if isinstance(vis, DeviceVisibility):
+        out = vis.vis.clone()
+        nat.call('arlgpu_phaserotate', nat.ptr(out), nat.ptr(vis.uvw), vis.nvis, vis.npol,
+                 nat.PRECISIONS[vis.precision], float(l), float(m), int(inverse), nat.stream_ptr())
+        return DeviceVisibility(vis.uvw, vis.frequency, out, vis.imaging_weight, vis.polarisation_frame,
+                                vis.phasecentre)
+    if isinstance(vis, Visibility):
+        newvis = copy_visibility(vis)
+        v = dv.to_device(vis.vis, torch.complex128, device)
+        uvw = dv.to_device(vis.uvw, torch.float64, device)
+        nat.call('arlgpu_phaserotate', nat.ptr(v), nat.ptr(uvw), vis.nvis, vis.npol, nat.FP64, float(l), float(m),
+                 int(inverse), nat.stream_ptr())
+        newvis.data['vis'][...] = v.cpu().numpy()
+        return newvis
+    from .data_models import BlockVisibility, copy_blockvisibility
+    from .skycomponents import C_M_S
+    assert isinstance(vis, BlockVisibility), 'vis argument neither Visibility or BlockVisibility'
+    newvis = copy_blockvisibility(vis)
+    ntimes, nant, _, nchan, npol = vis.vis.shape
+    k = torch.as_tensor(vis.frequency / C_M_S, device=device)
+    buvw = dv.to_device(vis.uvw, torch.float64, device)                      # [t, i, j, 3], metres
+    uvw = (buvw[..., None, :] * k[:, None]).reshape(-1, 3).contiguous()     # [t, i, j, c, 3], wavelengths
+    v = dv.to_device(vis.vis, torch.complex128, device).reshape(-1, npol).contiguous()
+    nat.call('arlgpu_phaserotate', nat.ptr(v), nat.ptr(uvw), uvw.shape[0], npol, nat.FP64, float(l), float(m),
+             int(inverse), nat.stream_ptr())
+    newvis.data['vis'][...] = v.cpu().numpy().reshape(vis.vis.shape)
+    return newvis
 
 
 def shift_vis_to_image(vis, im, tangent=True, inverse=False):
     """``imaging/base.py:50-81``: phase-rotate rows to the image's FFT phase
     centre (a no-op when the phase centres coincide).  Rotation runs on the GPU."""
-    lmn = _image_phasecentre_offset(vis, im)
-    if lmn is None:
+    pc = getattr(vis, 'phasecentre', None)
+    if pc is None or im.phasecentre.separation_rad(pc) <= 1e-15:
         return vis
-    l, m, _ = lmn
-    device = dv.require_cuda()
-    if isinstance(vis, DeviceVisibility):
-        prec = vis.precision
-        out = vis.vis.clone()
-        nat.call('arlgpu_phaserotate', nat.ptr(out), nat.ptr(vis.uvw), vis.nvis, vis.npol,
-                 nat.PRECISIONS[prec], float(l), float(m), int(inverse), nat.stream_ptr())
-        return DeviceVisibility(vis.uvw, vis.frequency, out, vis.imaging_weight, vis.polarisation_frame,
-                                im.phasecentre)
-    newvis = copy_visibility(vis)
-    v = dv.to_device(vis.vis, torch.complex128, device)
-    uvw = dv.to_device(vis.uvw, torch.float64, device)
-    nat.call('arlgpu_phaserotate', nat.ptr(v), nat.ptr(uvw), vis.nvis, vis.npol, nat.FP64, float(l), float(m),
-             int(inverse), nat.stream_ptr())
-    newvis.data['vis'][...] = v.cpu().numpy()
+    newvis = phaserotate_visibility(vis, im.phasecentre, tangent=tangent, inverse=inverse)
     newvis.phasecentre = im.phasecentre
     return newvis
 

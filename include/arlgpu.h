@@ -294,11 +294,32 @@ int arlgpu_hogbom(const double *dirty, const double *psf, const double *window, 
  * stack [nscales][nx][ny] is the scale-convolved residual (updated in place), psf_ss
  * [nscales][nscales][psf_nx][psf_ny] the twice-convolved PSF stack, pscale [nscales]
  * [psf_nx][psf_ny] the PSF-sized scale images, windowstack [nscales][nx][ny] or NULL,
- * coupling [nscales][nscales]; comps [nx][ny] is written.  The caller forms these as
- * the reference does (NumPy FFTs) and applies the final pmax scaling. */
+ * coupling [nscales][nscales]; comps [nx][ny] is written.  arlgpu_msclean_setup forms
+ * these; the caller applies the final pmax scaling. */
 int arlgpu_msclean(double *stack, const double *psf_ss, const double *pscale, const double *windowstack,
                    const double *coupling, int32_t nscales, int32_t nx, int32_t ny, int32_t psf_nx, int32_t psf_ny,
                    double gain, double absthresh, int32_t niter, double *comps, int32_t *iterations, void *stream);
+
+/* ---- (f4) msclean set-up (processing_library/arrays/cleaners.py:165-212, with
+ * create_scalestack :283-316, convolve_scalestack :319-335,
+ * convolve_convolve_scalestack :338-360, spheroidal_function :398-440) ----
+ * From dirty [nx][ny], psf [psf_nx][psf_ny] and window [nx][ny] (or NULL), float64
+ * device arrays, and the nscales scale sizes (host array, pixels): pscale
+ * [nscales][psf_nx][psf_ny] (the PSF-sized scale images), stack [nscales][nx][ny]
+ * (dirty / max(psf) convolved with each dirty-sized scale image), psf_ss
+ * [nscales][nscales][psf_nx][psf_ny] (psf / max(psf) convolved with scale p and
+ * correlated with scale s), windowstack [nscales][nx][ny] (1 where the window
+ * convolved with a scale exceeds 0.9; needed only with a window), coupling
+ * [nscales][nscales] (the maximum of each psf_ss plane) and scalars[2] = {max(psf),
+ * max|stack[0]|}, all device arrays.  Convolutions are complex128 cuFFT transforms;
+ * workspace bytes come from arlgpu_msclean_setup_bytes.  A scale whose window
+ * (2 ceil(scale / 2) + 2 pixels) is wider than the image or the PSF is rejected. */
+int arlgpu_msclean_setup_bytes(int32_t nx, int32_t ny, int32_t psf_nx, int32_t psf_ny, int32_t nscales,
+                               size_t *bytes_host);
+int arlgpu_msclean_setup(const double *dirty, int32_t nx, int32_t ny, const double *psf, int32_t psf_nx,
+                         int32_t psf_ny, const double *window, const double *scales_host, int32_t nscales,
+                         double *stack, double *psf_ss, double *pscale, double *windowstack, double *coupling,
+                         double *scalars, void *workspace, size_t workspace_bytes, void *stream);
 
 /* ---- a7/a8: create_pswf_convolutionfunction (griddata/kernels.py:52-97), FP64 ----
  * cf_out: [O][O][S][S] complex128 (one plane; ARL broadcasts it over chan/pol);
@@ -318,6 +339,18 @@ int arlgpu_make_wkernels(int32_t nw, double wstep, int32_t oversampling, int32_t
  * vis[r,p] *= g[a2[r]] * conj(g[a1[r]])  (inverse: 1/g), complex128 gains [nant]. */
 int arlgpu_apply_gains(void *vis, int64_t nvis, int32_t npol, int precision, const int32_t *a1,
                        const int32_t *a2, const void *gains, int inverse, void *stream);
+
+/* ---- a17: apply_gaintable on a BlockVisibility, scalar gains
+ * (calibration/operations.py:79-164, the scalar branch :124-140) ----
+ * vis: the block [ntimes][nants][nants][nchan] (one polarisation; complex64 for
+ * FP32C, complex128 for FP64).  time_row [ntimes] int32: the gain-table row of
+ * each block time, or -1 to leave that time alone.  gain [rows][nants][nchan]
+ * complex128 and gain_weight [rows][nants][nchan] float64.  Cell [t][i][j][c]
+ * becomes V * g[i] conj(g[j]) with g the row's gains (inverse: 1/gain where
+ * |gain| > 0, else 1), and 0 where the two antennas' gain weights multiply to 0. */
+int arlgpu_apply_gaintable(void *vis, int32_t ntimes, int32_t nants, int32_t nchan, int precision,
+                           const int32_t *time_row, const void *gain, const double *gain_weight,
+                           int inverse, void *stream);
 
 /* ---- a13: phaserotate_visibility, tangent plane (visibility/base.py:295-334) ----
  * vis[r,:] *= exp(+/-2 pi i (u l + v m + w (n - 1))), n = sqrt(1 - l^2 - m^2); inverse selects +. */

@@ -807,3 +807,44 @@ def apply_gains(vis, a1, a2, gain):
     """Scalar ``apply_gaintable`` (``processing_components/calibration/operations.py:134-137``)
     for rows of baseline (a1 < a2), stored at [a2, a1]: V *= g[a2] * conj(g[a1])."""
     return vis * (gain[a2] * np.conj(gain[a1]))[:, None]
+
+
+def skycoord_to_lmn(ra_deg, dec_deg, ra0_deg, dec0_deg):
+    """``skycoord_to_lmn`` (``processing_library/util/coordinate_support.py:150-169``)
+    for a direction (ra, dec) relative to the phase centre (ra0, dec0), all in
+    degrees: the direction's unit vector in the sky-offset frame of the phase
+    centre (astropy's frame: axes rotated by lon0 about z, then by -lat0 about
+    y), returned as (y, z, x - 1)."""
+    ra, dec, ra0, dec0 = ra_deg * D2R, dec_deg * D2R, ra0_deg * D2R, dec0_deg * D2R
+    v = np.array([np.cos(dec) * np.cos(ra), np.cos(dec) * np.sin(ra), np.sin(dec)])
+    c, s = np.cos(ra0), np.sin(ra0)
+    rz = np.array([[c, s, 0.0], [-s, c, 0.0], [0.0, 0.0, 1.0]])
+    c, s = np.cos(-dec0), np.sin(-dec0)
+    ry = np.array([[c, 0.0, -s], [0.0, 1.0, 0.0], [s, 0.0, c]])
+    x, y, z = ry @ (rz @ v)
+    return y, z, x - 1.0
+
+
+def apply_gaintable_block(vis, time_row, gain, gain_weight, inverse=False):
+    """Scalar branch of ``apply_gaintable`` (``processing_components/calibration/
+    operations.py:124-140``) on a block [ntimes, nants, nants, nchan] (one
+    polarisation) for block times t with a gain-table row time_row[t] >= 0:
+    V[t, i, j, c] * lg[i, c] conj(lg[j, c]), lg = gain (or 1/gain where
+    |gain| > 0, else 1, for the inverse), zero where the two gain weights
+    multiply to 0.  Returns a new array."""
+    out = vis.copy()
+    for t, k in enumerate(time_row):
+        if k < 0:
+            continue
+        g = gain[k]
+        if inverse:
+            lg = np.ones_like(g)
+            lg[np.abs(g) > 0.0] = 1.0 / g[np.abs(g) > 0.0]
+        else:
+            lg = g
+        for c in range(vis.shape[3]):
+            m = np.outer(lg[:, c], np.conjugate(lg[:, c]))
+            ww = np.outer(gain_weight[k][:, c], gain_weight[k][:, c])
+            out[t, :, :, c] = out[t, :, :, c] * m
+            out[t, :, :, c][ww == 0.0] = 0.0
+    return out

@@ -1,9 +1,12 @@
 """Generate golden fixtures by running the reference's own Python code.
 
-Run in a container that has the ARL sources (default ``/root/reference``, or
-``$ARL_REFERENCE``):
+Run in a container that has the ARL sources; their location is required,
+given with ``--reference`` or the ``ARL_REFERENCE`` environment variable:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference PATH [--out DIR] [case ...]
+
+With no case names every case runs; ``--out`` (default: this folder) is where
+the ``ref_*.npz`` files go.
 
 The reference cannot be imported unchanged here (no astropy; numpy 2 rejects
 the scalar assignment at ``processing_components/griddata/kernels.py:72``;
@@ -11,14 +14,15 @@ Python 3.12 lacks ``collections.Iterable``).  Three environment shims make it
 importable without touching its sources:
 
 * ``astropy_standin.install()`` supplies a linear-axis WCS (all axes on this
-  path are linear) and inert celestial placeholders;
+  path are linear), celestial directions with the sky-offset transform of
+  ``skycoord_to_lmn``, and inert placeholders for the rest;
 * ``kernels.grdsf`` is wrapped so a length-1 input returns scalars (the value
   is the reference's own ``grdsf``);
 * ``collections.Iterable`` is aliased to ``collections.abc.Iterable``.
 
 Everything else -- mapping, gridding and degridding loops, FFT stages, PSWF
-and w-kernel builders, invert_2d / predict_2d, the w-stack workflow -- is the
-reference's code.  Outputs go to ``tests/golden/*.npz``.
+and w-kernel builders, invert_2d / predict_2d, the w-stack workflow, phase
+rotation, component predict, gain application -- is the reference's code.
 """
 import collections
 import collections.abc
@@ -28,7 +32,24 @@ import sys
 import numpy
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get('ARL_REFERENCE', '/root/reference')
+
+
+def _args(argv):
+    ref, out, cases = os.environ.get('ARL_REFERENCE'), HERE, []
+    it = iter(argv)
+    for a in it:
+        if a == '--reference':
+            ref = next(it)
+        elif a == '--out':
+            out = next(it)
+        else:
+            cases.append(a)
+    if not ref or not os.path.isdir(ref):
+        sys.exit('make_golden.py: give the ARL source tree with --reference PATH or ARL_REFERENCE')
+    return ref, out, cases
+
+
+REF, OUT, CASES = _args(sys.argv[1:]) if __name__ == '__main__' else (os.environ.get('ARL_REFERENCE'), HERE, [])
 
 sys.path.insert(0, HERE)
 import astropy_standin  # noqa: E402
@@ -293,7 +314,7 @@ def case_msclean(out):
     ``deconvolve_cube(algorithm='msclean')`` on the Hogbom case's dirty image."""
     from processing_library.arrays.cleaners import msclean
     from processing_components.image.deconvolution import deconvolve_cube
-    d = numpy.load(os.path.join(HERE, 'ref_hogbom.npz'))
+    d = numpy.load(os.path.join(OUT, 'ref_hogbom.npz'))
     dirty, psf, window = d['dirty'], d['psf'], d['window']
     c1, r1 = msclean(dirty, psf, None, 0.3, 0.0, 150, [0, 3, 10], 0.01)
     c2, r2 = msclean(dirty, psf[32:96, 32:96], window, 0.7, 0.02, 100, [0, 3], 0.001)
@@ -305,15 +326,137 @@ def case_msclean(out):
     numpy.savez_compressed(out, c1=c1, r1=r1, c2=c2, r2=r2, cube_comp=comp.data, cube_resid=resid.data)
 
 
+def case_rowops(out):
+    """Row operations on the path's edges, from the reference's own code:
+
+    * ``skycoord_to_lmn`` (``processing_library/util/coordinate_support.py:150-169``)
+      on the stand-in's directions, first checked against every expectation of
+      the reference's ``test_skycoord_to_lmn``, then on offsets of the kind
+      the imaging path meets;
+    * ``shift_vis_to_image`` / ``phaserotate_visibility`` (tangent, both
+      directions; ``processing_components/imaging/base.py:50-81``,
+      ``processing_components/visibility/base.py:295-334``) on a Visibility
+      whose phase centre differs from the image's;
+    * ``predict_skycomponent_visibility`` (``imaging/base.py:192-244``) on a
+      Visibility (3 channels, 2 polarisations) and a BlockVisibility;
+    * ``apply_gaintable`` with scalar gains, forward and inverse
+      (``processing_components/calibration/operations.py:79-164``), with
+      zero gain weights and one zero gain."""
+    from numpy.testing import assert_allclose
+    from data_models.memory_data_models import BlockVisibility, GainTable, Skycomponent
+    from data_models.polarisation import ReceptorFrame
+    from processing_library.util.coordinate_support import skycoord_to_lmn
+    from processing_components.imaging.base import shift_vis_to_image, predict_skycomponent_visibility
+    from processing_components.visibility.base import phaserotate_visibility
+    from processing_components.calibration.operations import apply_gaintable
+    res = {}
+    # (1) the stand-in against the reference's own skycoord_to_lmn test
+    center, north, south = SkyCoord(0, 0), SkyCoord(0, 90), SkyCoord(0, -90)
+    east, west = SkyCoord(90, 0), SkyCoord(-90, 0)
+    kat = [(center, center, (0, 0, 0), 0), (north, center, (0, 1, -1), 0), (south, center, (0, -1, -1), 0),
+           (south, north, (0, 0, -2), 1e-14), (east, center, (1, 0, -1), 0), (west, center, (-1, 0, -1), 0),
+           (center, west, (1, 0, -1), 0), (north, west, (0, 1, -1), 1e-14), (south, west, (0, -1, -1), 1e-14),
+           (north, east, (0, 1, -1), 1e-14), (south, east, (0, -1, -1), 1e-14)]
+    for a, b, want, atol in kat:
+        assert_allclose(skycoord_to_lmn(a, b), want, atol=atol)
+    rng = numpy.random.default_rng(4848)
+    pcs = numpy.column_stack([rng.uniform(-180, 180, 16), rng.uniform(-85, 85, 16)])
+    offs = numpy.column_stack([pcs[:, 0] + rng.uniform(-6, 6, 16), numpy.clip(pcs[:, 1] + rng.uniform(-6, 6, 16),
+                                                                                -89, 89)])
+    res['lmn_pc'] = pcs
+    res['lmn_dir'] = offs
+    res['lmn'] = numpy.array([skycoord_to_lmn(SkyCoord(*o), SkyCoord(*p)) for o, p in zip(offs, pcs)])
+
+    # (2) phase rotation to the image's phase centre
+    n = 3000
+    uvw = rng.normal(size=(n, 3)) * numpy.array([800.0, 800.0, 80.0])
+    z = numpy.zeros(n)
+    vis = rng.normal(size=(n, 2)) + 1j * rng.normal(size=(n, 2))
+    v = Visibility(uvw=uvw, time=z, frequency=z + 1e8, channel_bandwidth=z + 1e6, vis=vis, weight=z[:, None] + 1.0,
+                   imaging_weight=z[:, None] + 1.0, integration_time=z + 1.0, antenna1=z.astype(int),
+                   antenna2=z.astype(int), polarisation_frame=PolarisationFrame('stokesIQ'))
+    v.phasecentre = SkyCoord(10.0, -45.0)
+    im = make_image(64, 1e-3, numpy.array([1e8]), 1e6, 'stokesIQ')
+    im.wcs.wcs.crval[0], im.wcs.wcs.crval[1] = 10.3, -44.8
+    fwd = shift_vis_to_image(v, im, tangent=True, inverse=False)
+    inv = shift_vis_to_image(v, im, tangent=True, inverse=True)
+    far = phaserotate_visibility(v, SkyCoord(25.0, -30.0), tangent=True, inverse=False)
+    res.update(rot_uvw=uvw, rot_vis=vis, rot_vis_pc=numpy.array([10.0, -45.0]), rot_im_pc=numpy.array([10.3, -44.8]),
+               rot_fwd=fwd.vis.copy(), rot_inv=inv.vis.copy(), rot_far_pc=numpy.array([25.0, -30.0]),
+               rot_far=far.vis.copy(),
+               rot_lmn=numpy.array(skycoord_to_lmn(im.phasecentre, v.phasecentre)))
+
+    # (3) point components onto rows (3 channels, 2 pols) and onto blocks
+    freqs = numpy.array([1.0e8, 1.1e8, 1.2e8])
+    n = 4000
+    f = rng.choice(freqs, n)
+    uvw = rng.uniform(-3000, 3000, (n, 3)) * numpy.array([1.0, 1.0, 0.1])
+    z = numpy.zeros(n)
+    base = rng.normal(size=(n, 2)) + 1j * rng.normal(size=(n, 2))
+    v = Visibility(uvw=uvw, time=z, frequency=f, channel_bandwidth=z + 1e7, vis=base.copy(), weight=z[:, None] + 1.0,
+                   imaging_weight=z[:, None] + 1.0, integration_time=z + 1.0, antenna1=z.astype(int),
+                   antenna2=z.astype(int), polarisation_frame=PolarisationFrame('linearnp'))
+    v.phasecentre = SkyCoord(0.0, -45.0)
+    cdir = numpy.column_stack([rng.uniform(-4, 4, 10), -45.0 + rng.uniform(-4, 4, 10)])
+    cflux = rng.uniform(0.1, 5.0, (10, 3, 2))
+    comps = [Skycomponent(direction=SkyCoord(*d), frequency=freqs, flux=fl,
+                          polarisation_frame=PolarisationFrame('linearnp')) for d, fl in zip(cdir, cflux)]
+    predict_skycomponent_visibility(v, comps)
+    res.update(dft_uvw=uvw, dft_freq=f, dft_base=base, dft_dir=cdir, dft_flux=cflux, dft_pc=numpy.array([0.0, -45.0]),
+               dft_vis=v.vis.copy())
+    ntimes, nant = 3, 6
+    buvw = rng.uniform(-2000.0, 2000.0, (ntimes, nant, nant, 3))
+    bbase = rng.normal(size=(ntimes, nant, nant, 3, 2)) + 1j * rng.normal(size=(ntimes, nant, nant, 3, 2))
+    bv = BlockVisibility(frequency=freqs, channel_bandwidth=numpy.full(3, 1e7), phasecentre=SkyCoord(0.0, -45.0),
+                         configuration=None, uvw=buvw, time=numpy.arange(ntimes) * 30.0, vis=bbase.copy(),
+                         weight=numpy.ones(bbase.shape), integration_time=numpy.full(ntimes, 30.0),
+                         polarisation_frame=PolarisationFrame('linearnp'), imaging_weight=numpy.ones(bbase.shape))
+    predict_skycomponent_visibility(bv, comps)
+    res.update(dftb_uvw=buvw, dftb_base=bbase, dftb_vis=bv.vis.copy())
+
+    # (4) scalar gains on a BlockVisibility, forward and inverse
+    ntimes, nant, nchan = 4, 7, 3
+    times = 4.5e9 + numpy.arange(ntimes) * 30.0
+    gshape = (ntimes, nant, nant, nchan, 1)
+    gvis = rng.normal(size=gshape) + 1j * rng.normal(size=gshape)
+    gain = (rng.normal(1.0, 0.1, (ntimes, nant, nchan, 1, 1)) *
+            numpy.exp(1j * rng.uniform(-numpy.pi, numpy.pi, (ntimes, nant, nchan, 1, 1))))
+    gain[2, 3, 1] = 0.0
+    gwt = numpy.ones((ntimes, nant, nchan, 1, 1))
+    gwt[1, 2, 0] = 0.0
+    gwt[3, 5, 2] = 0.0
+    gt = GainTable(gain=gain, time=times, interval=numpy.full(ntimes, 30.0), weight=gwt,
+                   residual=numpy.zeros((ntimes, nchan, 1, 1)), frequency=freqs,
+                   receptor_frame=ReceptorFrame('stokesI'))
+
+    def block():
+        return BlockVisibility(frequency=freqs, channel_bandwidth=numpy.full(nchan, 1e7),
+                               phasecentre=SkyCoord(0.0, -45.0), configuration=None,
+                               uvw=numpy.zeros((ntimes, nant, nant, 3)), time=times, vis=gvis.copy(),
+                               weight=numpy.ones(gshape), integration_time=numpy.full(ntimes, 30.0),
+                               polarisation_frame=PolarisationFrame('stokesI'), imaging_weight=numpy.ones(gshape))
+    fwd = apply_gaintable(block(), gt)
+    inv = apply_gaintable(block(), gt, inverse=True)
+    res.update(gt_vis=gvis, gt_time=times, gt_interval=numpy.full(ntimes, 30.0), gt_gain=gain, gt_weight=gwt,
+               gt_freqs=freqs, gt_fwd=fwd.vis.copy(), gt_inv=inv.vis.copy())
+    numpy.savez_compressed(out, **res)
+
+
+ALL_CASES = {
+    'ref_2d_pswf': case_2d_pswf,
+    'ref_wproj_2chan_2pol': case_wproj_2chan_2pol,
+    'ref_wstack': case_wstack,
+    'ref_kernels': case_kernels,
+    'ref_weighting': case_weighting,
+    'ref_blocks': case_blocks,
+    'ref_hogbom': case_hogbom,
+    'ref_msclean': case_msclean,
+    'ref_rowops': case_rowops,
+}
+
 if __name__ == '__main__':
-    case_2d_pswf(os.path.join(HERE, 'ref_2d_pswf.npz'))
-    case_wproj_2chan_2pol(os.path.join(HERE, 'ref_wproj_2chan_2pol.npz'))
-    case_wstack(os.path.join(HERE, 'ref_wstack.npz'))
-    case_kernels(os.path.join(HERE, 'ref_kernels.npz'))
-    case_weighting(os.path.join(HERE, 'ref_weighting.npz'))
-    case_blocks(os.path.join(HERE, 'ref_blocks.npz'))
-    case_hogbom(os.path.join(HERE, 'ref_hogbom.npz'))
-    case_msclean(os.path.join(HERE, 'ref_msclean.npz'))
-    for f in sorted(os.listdir(HERE)):
-        if f.endswith('.npz'):
-            print(f, os.path.getsize(os.path.join(HERE, f)))
+    os.makedirs(OUT, exist_ok=True)
+    for name, fn in ALL_CASES.items():
+        if not CASES or name in CASES:
+            fn(os.path.join(OUT, name + '.npz'))
+            print(name, os.path.getsize(os.path.join(OUT, name + '.npz')))

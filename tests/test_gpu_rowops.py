@@ -53,3 +53,81 @@ def test_apply_gains(arl, oracle):
                              arl._native.stream_ptr())
             gg = 1.0 / g if inverse else g
             assert rel(t.cpu().numpy(), oracle.apply_gains(v, a1, a2, gg)) < tol
+
+
+# ---------------------------------------------------------------------------
+# Against the reference's own outputs (tests/golden/ref_rowops.npz)
+# ---------------------------------------------------------------------------
+def test_phase_rotation_matches_reference(arl, golden):
+    """shift_vis_to_image (both directions) and phaserotate_visibility to a
+    far phase centre, against the reference's results with its own
+    skycoord_to_lmn.  FP64 1e-10, as the DFT tests: the package forms l and m
+    with the direct spherical-trigonometry formula and the reference through
+    astropy's rotation matrices; both lose ~1e-16 absolute to cancellation,
+    which baselines of ~2e3 wavelengths turn into ~1e-12 of phase.  FP32C 1e-6."""
+    d = golden('ref_rowops.npz')
+    frame = arl.PolarisationFrame('stokesIQ')
+    n = d['rot_uvw'].shape[0]
+    vis = arl.Visibility(uvw=d['rot_uvw'], frequency=numpy.full(n, 1e8), vis=d['rot_vis'].copy(),
+                         weight=numpy.ones((n, 2)), polarisation_frame=frame)
+    vis.phasecentre = arl.PhaseCentre(*d['rot_vis_pc'])
+    im = arl.create_image(npixel=64, cellsize=1e-3, phasecentre=arl.PhaseCentre(*d['rot_im_pc']),
+                          polarisation_frame=frame)
+    fwd = arl.shift_vis_to_image(vis, im, tangent=True, inverse=False)
+    assert rel(fwd.vis, d['rot_fwd']) < 1e-10
+    assert fwd.phasecentre is im.phasecentre and vis.phasecentre.ra_deg == d['rot_vis_pc'][0]
+    inv = arl.shift_vis_to_image(vis, im, tangent=True, inverse=True)
+    assert rel(inv.vis, d['rot_inv']) < 1e-10
+    far = arl.phaserotate_visibility(vis, arl.PhaseCentre(*d['rot_far_pc']), tangent=True)
+    assert rel(far.vis, d['rot_far']) < 1e-10
+    assert numpy.array_equal(vis.vis, d['rot_vis'])  # the input is not modified
+    dvis = arl.DeviceVisibility.from_visibility(vis, 'fp32c')
+    dvis.phasecentre = vis.phasecentre
+    dfwd = arl.shift_vis_to_image(dvis, im)
+    assert rel(dfwd.vis.to(torch.complex128).cpu().numpy(), d['rot_fwd']) < 1e-6
+
+
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-10), ('fp32c', 1e-6)])
+def test_skycomponents_match_reference(arl, golden, precision, tol):
+    """predict_skycomponent_visibility on rows (3 channels, 2 polarisations) and
+    on a BlockVisibility, against the reference's results (tolerances of
+    test_gpu_dft.py)."""
+    d = golden('ref_rowops.npz')
+    frame = arl.PolarisationFrame('linearnp')
+    freqs = numpy.unique(d['dft_freq'])
+    comps = [arl.Skycomponent(direction=arl.PhaseCentre(*dr), frequency=freqs, flux=fl, polarisation_frame=frame)
+             for dr, fl in zip(d['dft_dir'], d['dft_flux'])]
+    n = d['dft_uvw'].shape[0]
+    vis = arl.Visibility(uvw=d['dft_uvw'], frequency=d['dft_freq'], vis=d['dft_base'].copy(),
+                         weight=numpy.ones((n, 2)), polarisation_frame=frame)
+    vis.phasecentre = arl.PhaseCentre(*d['dft_pc'])
+    arl.predict_skycomponent_visibility(vis, comps, precision=precision)
+    assert rel(vis.vis, d['dft_vis']) < tol
+    base = d['dftb_base']
+    ntimes = base.shape[0]
+    bv = arl.BlockVisibility(frequency=freqs, channel_bandwidth=numpy.full(3, 1e7),
+                             phasecentre=arl.PhaseCentre(*d['dft_pc']), uvw=d['dftb_uvw'],
+                             time=numpy.arange(ntimes) * 30.0, vis=base.copy(), weight=numpy.ones(base.shape),
+                             integration_time=numpy.full(ntimes, 30.0), polarisation_frame=frame)
+    arl.predict_skycomponent_visibility(bv, comps, precision=precision)
+    assert rel(bv.vis, d['dftb_vis']) < tol
+
+
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-12), ('fp32c', 1e-6)])
+def test_apply_gaintable_matches_reference(arl, golden, precision, tol):
+    """apply_gaintable with scalar gains on a BlockVisibility, forward and
+    inverse, with zero gain weights and a zero gain, against the reference."""
+    d = golden('ref_rowops.npz')
+    gshape = d['gt_vis'].shape
+    ntimes, nant, _, nchan, _ = gshape
+    gt = arl.GainTable(gain=d['gt_gain'], time=d['gt_time'], interval=d['gt_interval'], weight=d['gt_weight'],
+                       residual=numpy.zeros((ntimes, nchan, 1, 1)), frequency=d['gt_freqs'],
+                       receptor_frame=arl.ReceptorFrame('stokesI'))
+    for inverse, key in ((False, 'gt_fwd'), (True, 'gt_inv')):
+        bv = arl.BlockVisibility(frequency=d['gt_freqs'], channel_bandwidth=numpy.full(nchan, 1e7),
+                                 phasecentre=arl.PhaseCentre(0.0, -45.0), uvw=numpy.zeros((ntimes, nant, nant, 3)),
+                                 time=d['gt_time'], vis=d['gt_vis'].copy(), weight=numpy.ones(gshape),
+                                 integration_time=numpy.full(ntimes, 30.0))
+        out = arl.apply_gaintable(bv, gt, inverse=inverse, precision=precision)
+        assert out is bv
+        assert rel(bv.vis, d[key]) < tol, (inverse, precision)
