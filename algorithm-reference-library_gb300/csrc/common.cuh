@@ -87,6 +87,7 @@ struct PlanBufs {
   uint32_t *hist;     // nbins + 1
   uint32_t *offsets;  // nbins + 2
   double *wpart;      // per-plane partial w sums (plan_wpart_items entries)
+  uint32_t *queue;    // device work-queue words of the gridder [0] and degridder [1]
 };
 uint32_t plan_wpart_items(const Geom &g);
 size_t plan_bytes(int64_t nvis, const Geom &g);

@@ -56,6 +56,7 @@ static std::atomic<int> g_tune_persistent{0};     // lean / fixed-point kernels:
 static std::atomic<int> g_tune_dsfft{1};          // FP32C inverse transforms: 1 = double-single FFT, 0 = cuFFT FP64
 static std::atomic<int> g_tune_small_rows{2};     // rows per warp in the FP32C gridder when S <= 8
 static std::atomic<int> g_tune_small_rows_dg{4};  // rows per warp in the packed degridder when S <= 8
+static std::atomic<int> g_tune_lanes{0};          // lanes per row for every segment (0: by support)
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 bool tune_dsfft() { return g_tune_dsfft.load() != 0; }
 
@@ -458,7 +459,7 @@ k_grid(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sid
        const uint32_t *__restrict__ off, uint32_t chunk,
        const typename VisT<R>::C *__restrict__ vis, const typename VisT<R>::W *__restrict__ wt,
        const typename Cplx<R>::T *__restrict__ cf, typename Cplx<R>::T *__restrict__ grid,
-       double *__restrict__ sumwt) {
+       double *__restrict__ sumwt, uint32_t *) {  // one CTA per chunk: no work queue
   using CT = typename Cplx<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int SG = g.SG, SG2 = SG * SG, npol = g.npol;
@@ -605,7 +606,7 @@ k_grid_band(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
             const uint32_t *__restrict__ off, uint32_t chunk,
             const typename VisT<R>::C *__restrict__ vis, const typename VisT<R>::W *__restrict__ wt,
             const typename Cplx<R>::T *__restrict__ cf, typename Cplx<R>::T *__restrict__ grid,
-            double *__restrict__ sumwt) {
+            double *__restrict__ sumwt, uint32_t *) {  // one CTA per chunk: no work queue
   using CT = typename Cplx<R>::T;
   constexpr int BATCH = NW * 32;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -749,7 +750,7 @@ __global__ void __launch_bounds__(NW * 32)
 k_degrid(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
          const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
          const typename Cplx<R>::T *__restrict__ cf, const typename Cplx<R>::T *__restrict__ grid,
-         typename VisT<R>::C *__restrict__ vis_out) {
+         typename VisT<R>::C *__restrict__ vis_out, uint32_t *) {  // one CTA per chunk: no work queue
   using CT = typename Cplx<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int SG = g.SG, SG2 = SG * SG, npol = g.npol;
@@ -850,7 +851,7 @@ __global__ void __launch_bounds__(NW * 32)
 k_degrid_batch(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
                const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
                const typename Cplx<R>::T *__restrict__ cf, const typename Cplx<R>::T *__restrict__ grid,
-               typename VisT<R>::C *__restrict__ vis_out) {
+               typename VisT<R>::C *__restrict__ vis_out, uint32_t *) {  // one CTA per chunk: no work queue
   using CT = typename Cplx<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int SG = g.SG, SG2 = SG * SG, npol = g.npol;
@@ -969,6 +970,19 @@ k_degrid_batch(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restri
   }
 }
 
+// Next chunk of sorted rows for a chunk-looping kernel: every gridDim.x-th
+// chunk after this one (static), or, with a device work queue, the next
+// unclaimed chunk: thread 0 takes it with one atomic on the queue word (zeroed
+// before the launch; chunks 0 .. gridDim.x - 1 are the CTAs' first) and the
+// barriers broadcast it.  Block-uniform.
+__device__ __forceinline__ uint64_t next_chunk(uint64_t cb, uint32_t *queue, uint32_t *s_slot) {
+  if (!queue) return cb + gridDim.x;
+  __syncthreads();  // every thread has read the previous value
+  if (threadIdx.x == 0) *s_slot = gridDim.x + atomicAdd(queue, 1u);
+  __syncthreads();
+  return *s_slot;
+}
+
 // Per-row set-up shared by the lean kernels: the sub-kernel base pointer and
 // the 32-bit tap / subgrid offsets of this lane's first tap, plus the offset
 // steps for "32 taps further" (q rows and rr columns, with a row wrap).
@@ -1040,7 +1054,7 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
             const uint32_t *__restrict__ off, uint32_t chunk,
             const typename VisT<R>::C *__restrict__ vis, const typename VisT<R>::W *__restrict__ wt,
             const typename Cplx<R>::T *__restrict__ cf, typename Cplx<R>::T *__restrict__ grid,
-            double *__restrict__ sumwt) {
+            double *__restrict__ sumwt, uint32_t *__restrict__ queue) {
   using CT = typename Cplx<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int SG = g.SG, SG2 = SG * SG;
@@ -1062,9 +1076,9 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   for (int k = threadIdx.x; k < 2 * NPOL * SG2 * ACC::kWords; k += blockDim.x) sub[k] = (R)0;
   build_tap_table(tab, S);
   __shared__ int s_red[2][NW * 6];
-  __shared__ uint32_t s_next[2];
+  __shared__ uint32_t s_next[2], s_chunk;
   int parity = 0;
-  for (uint64_t cb = blockIdx.x; cb * chunk < nvalid; cb += gridDim.x) {
+  for (uint64_t cb = blockIdx.x; cb * chunk < nvalid; cb = next_chunk(cb, queue, &s_chunk)) {
   const uint32_t c0 = (uint32_t)(cb * chunk), c1 = min(c0 + chunk, nvalid);
   uint32_t pos = c0;
   while (pos < c1) {
@@ -1236,12 +1250,12 @@ __device__ __forceinline__ void fx_add(int *q, int *r, float x, float scale, flo
   }
 }
 
-template <int NPOL, int NW, bool RESID, int LPR = 32, int SGC = 0>
+template <int NPOL, int NW, bool RESID, int LPR = 0, int SGC = 0>
 __global__ void __launch_bounds__(NW * 32)
 k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
           const uint32_t *__restrict__ off, uint32_t chunk, const float2 *__restrict__ vis,
           const float *__restrict__ wt, const float2 *__restrict__ cf, float2 *__restrict__ grid,
-          double *__restrict__ sumwt) {
+          double *__restrict__ sumwt, uint32_t *__restrict__ queue) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_red[2][NW * 6];
   // SGC != 0: the subgrid edge as a compile-time constant, so that plane
@@ -1267,9 +1281,9 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   for (int k = threadIdx.x; k < kPlanes * SG2; k += blockDim.x) subq[k] = 0;
   build_tap_table(tab, S);
 
-  __shared__ uint32_t s_next[2];
+  __shared__ uint32_t s_next[2], s_chunk;
   int parity = 0;
-  for (uint64_t cb = blockIdx.x; cb * chunk < nvalid; cb += gridDim.x) {
+  for (uint64_t cb = blockIdx.x; cb * chunk < nvalid; cb = next_chunk(cb, queue, &s_chunk)) {
   const uint32_t c0 = (uint32_t)(cb * chunk), c1 = min(c0 + chunk, nvalid);
   uint32_t pos = c0;
   while (pos < c1) {
@@ -1431,7 +1445,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         }
       }
     };
-    if constexpr (LPR == 32) {
+    if constexpr (LPR == 0) {  // lanes per row chosen per segment
       if (box.sz <= 16)
         row_loop(IntC<16>());
       else
@@ -1497,12 +1511,12 @@ __device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsign
 // DUP (FP32 only, degrid_kernel 3): the staged subgrid holds each cell as
 // (re, re, im, im), so a tap is two packed multiply-adds,
 // (sum re t.re, sum re t.im) and (sum im t.re, sum im t.im), instead of four.
-template <typename R, int NPOL, int NW, bool DUP = false, int LPR = 32, int SGC = 0>
+template <typename R, int NPOL, int NW, bool DUP = false, int LPR = 0, int SGC = 0>
 __global__ void __launch_bounds__(NW * 32)
 k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
               const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
               const typename Cplx<R>::T *__restrict__ cf, const typename Cplx<R>::T *__restrict__ grid,
-              typename VisT<R>::C *__restrict__ vis_out) {
+              typename VisT<R>::C *__restrict__ vis_out, uint32_t *__restrict__ queue) {
   using CT = typename Cplx<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int SG = SGC ? SGC : g.SG, SG2 = SG * SG;  // SGC != 0: compile-time edge
@@ -1521,10 +1535,10 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
   const int64_t plane_elems = (int64_t)g.ny * g.nx;
 
   __shared__ int s_red[2][NW * 6];
-  __shared__ uint32_t s_next[2];
+  __shared__ uint32_t s_next[2], s_chunk;
   build_tap_table(tab, S);  // ordered before first use by the barrier in seg_box
   int parity = 0;
-  for (uint64_t cb = blockIdx.x; cb < nchunks; cb += gridDim.x) {
+  for (uint64_t cb = blockIdx.x; cb < nchunks; cb = next_chunk(cb, queue, &s_chunk)) {
   const uint32_t c0 = (uint32_t)(cb * chunk);
   if (c0 + chunk > nvalid) {  // rows the plan rejected: zero output
     const uint32_t b = max(c0, nvalid), e = (uint32_t)min((uint64_t)c0 + chunk, (uint64_t)nvis);
@@ -1745,7 +1759,7 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
         }
       }
     };
-    if constexpr (LPR == 32) {
+    if constexpr (LPR == 0) {  // lanes per row chosen per segment
       if (box.sz <= 8)
         row_loop(IntC<8>());
       else if (box.sz <= 16)
@@ -1911,7 +1925,7 @@ size_t plan_bytes(int64_t nvis, const Geom &g) {
   size_t n = (size_t)nvis;
   return align_up(n * 4) + align_up(n * sizeof(RowMap)) + align_up(n * 4) + align_up(n * sizeof(RowMap)) +
          align_up(((size_t)g.nbins + 1) * 4) + align_up(((size_t)g.nbins + 2) * 4) +
-         align_up((size_t)plan_wpart_items(g) * 8);
+         align_up((size_t)plan_wpart_items(g) * 8) + align_up(16);
 }
 
 int plan_carve(void *ws, size_t bytes, int64_t nvis, const Geom &g, PlanBufs *b) {
@@ -1933,6 +1947,8 @@ int plan_carve(void *ws, size_t bytes, int64_t nvis, const Geom &g, PlanBufs *b)
   b->offsets = reinterpret_cast<uint32_t *>(p);
   p += align_up(((size_t)g.nbins + 2) * 4);
   b->wpart = reinterpret_cast<double *>(p);
+  p += align_up((size_t)plan_wpart_items(g) * 8);
+  b->queue = reinterpret_cast<uint32_t *>(p);
   return ARLGPU_OK;
 }
 
@@ -1994,7 +2010,7 @@ template <typename K>
 static unsigned chunk_grid(K kern, size_t smem, int64_t nvis, uint32_t chunk) {
   const int64_t nchunks = (nvis + chunk - 1) / chunk;
   if (nchunks <= 0) return 0;
-  if (g_tune_persistent.load()) {
+  if (g_tune_persistent.load() != 0) {
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kWarps * 32, smem) == cudaSuccess && occ > 0) {
       const int64_t resident = (int64_t)occ * num_sms();
@@ -2004,31 +2020,51 @@ static unsigned chunk_grid(K kern, size_t smem, int64_t nvis, uint32_t chunk) {
   return (unsigned)nchunks;
 }
 
+// Lanes per row of the FP32C gridder / packed degridder: the tuning key
+// lanes_per_row when set (8, 16 or 32 for every segment); else, for supports
+// up to 8, 32 / small_rows (gridder) or 32 / small_rows_degrid (degridder);
+// else 0, the per-segment choice.
+static int lanes_per_row(const Geom &g, bool degrid = false) {
+  const int fixed = g_tune_lanes.load();
+  if (fixed) return fixed;
+  if (g.S <= 8) return 32 / (degrid ? g_tune_small_rows_dg.load() : g_tune_small_rows.load());
+  return 0;
+}
+
+// The device work-queue word of a chunk-looping launch (0: gridder, 1:
+// degridder) when the persistent grid takes its chunks dynamically
+// (tuning "persistent" = 2), else null (static every-gridDim-th chunk).
+static uint32_t *work_queue(const PlanBufs &b, int which, cudaStream_t) {
+  return g_tune_persistent.load() == 2 ? b.queue + which : nullptr;
+}
+
 static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const void *vis, const void *wt,
                           const void *cf, void *grid, double *sumwt, bool resid, cudaStream_t st) {
   const size_t smem = (size_t)(resid ? 4 : 2) * g.npol * g.SG * fx_pitch(g.SG) * 4 + tap_table_bytes(g.S);
   if (smem > 227 * 1024) return fail(ARLGPU_ERR_UNSUPPORTED, "gridder needs %zu bytes of shared memory", smem);
   void (*kern)(Geom, const RowMap *, const uint32_t *, const uint32_t *, uint32_t, const float2 *, const float *,
-               const float2 *, float2 *, double *);
-  // Supports up to 8 (64 taps): several rows per warp (tuning small_rows).
-  const int rpw = g.S <= 8 ? g_tune_small_rows.load() : 1;
+               const float2 *, float2 *, double *, uint32_t *);
+  // Lanes per row: the tuning key lanes_per_row (8, 16 or 32 for every
+  // segment), else for supports up to 8 (64 taps) 32 / small_rows, else
+  // chosen per segment (0).
+  const int lpr = lanes_per_row(g);
   // The default subgrid edge (48, or 32 with four polarisations) runs a
   // compile-time-edge instantiation; other edges (autotuner trials) the
-  // runtime-edge one.
+  // runtime-edge one, with lanes per row chosen per segment.
   const bool csg = g.SG == (g.npol == 4 ? 32 : 48);
   auto pick = [&](auto resid_c) {
     constexpr bool RS = decltype(resid_c)::value;
+    auto by_lpr = [&](auto npol_c, auto sg_c) {
+      constexpr int NP = decltype(npol_c)::value, SGV = decltype(sg_c)::value;
+      return lpr == 8 ? k_grid_fx<NP, kWarps, RS, 8, SGV>
+                      : lpr == 16 ? k_grid_fx<NP, kWarps, RS, 16, SGV>
+                                  : lpr == 32 ? k_grid_fx<NP, kWarps, RS, 32, SGV> : k_grid_fx<NP, kWarps, RS, 0, SGV>;
+    };
     if (csg) {
-      if (g.npol == 4)
-        return rpw == 4 ? k_grid_fx<4, kWarps, RS, 8, 32>
-                        : rpw == 2 ? k_grid_fx<4, kWarps, RS, 16, 32> : k_grid_fx<4, kWarps, RS, 32, 32>;
-      if (g.npol == 2)
-        return rpw == 4 ? k_grid_fx<2, kWarps, RS, 8, 48>
-                        : rpw == 2 ? k_grid_fx<2, kWarps, RS, 16, 48> : k_grid_fx<2, kWarps, RS, 32, 48>;
-      return rpw == 4 ? k_grid_fx<1, kWarps, RS, 8, 48>
-                      : rpw == 2 ? k_grid_fx<1, kWarps, RS, 16, 48> : k_grid_fx<1, kWarps, RS, 32, 48>;
+      if (g.npol == 4) return by_lpr(IntC<4>(), IntC<32>());
+      if (g.npol == 2) return by_lpr(IntC<2>(), IntC<48>());
+      return by_lpr(IntC<1>(), IntC<48>());
     }
-    // runtime edge: rows per warp chosen per segment only
     return g.npol == 1 ? k_grid_fx<1, kWarps, RS> : g.npol == 2 ? k_grid_fx<2, kWarps, RS> : k_grid_fx<4, kWarps, RS>;
   };
   kern = resid ? pick(BoolC<true>()) : pick(BoolC<false>());
@@ -2036,9 +2072,11 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
   const uint32_t chunk = chunk_rows();
   const unsigned blocks = chunk_grid(kern, smem, nvis, chunk);
   if (blocks == 0) return ARLGPU_OK;
+  uint32_t *queue = work_queue(b, 0, st);
+  if (queue) ARL_CUDA(cudaMemsetAsync(queue, 0, 4, st));
   kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk, static_cast<const float2 *>(vis),
                                           static_cast<const float *>(wt), static_cast<const float2 *>(cf),
-                                          static_cast<float2 *>(grid), sumwt);
+                                          static_cast<float2 *>(grid), sumwt, queue);
   ARL_LAUNCH_CHECK();
   count_launch(1);
   return ARLGPU_OK;
@@ -2078,11 +2116,13 @@ static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const voi
   const bool loops = g_tune_grid_kernel.load() >= 2;  // the lean kernels loop over chunks
   const unsigned blocks = loops ? chunk_grid(kern, smem, nvis, chunk) : (unsigned)((nvis + chunk - 1) / chunk);
   if (blocks == 0) return ARLGPU_OK;
+  uint32_t *queue = loops ? work_queue(b, 0, st) : nullptr;
+  if (queue) ARL_CUDA(cudaMemsetAsync(queue, 0, 4, st));
   kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk,
                                           static_cast<const typename VisT<R>::C *>(vis),
                                           static_cast<const typename VisT<R>::W *>(wt),
                                           static_cast<const typename Cplx<R>::T *>(cf),
-                                          static_cast<typename Cplx<R>::T *>(grid), sumwt);
+                                          static_cast<typename Cplx<R>::T *>(grid), sumwt, queue);
   ARL_LAUNCH_CHECK();
   count_launch(1);
   return ARLGPU_OK;
@@ -2102,25 +2142,26 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
     smem += tap_table_bytes(g.S);
   } else if (g_tune_degrid_kernel.load() == 3) {  // FP32: packed multiply-adds
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
-    // Supports up to 8 (64 taps): several rows per warp (tuning small_rows_degrid).
-    const int rpw = g.S <= 8 ? g_tune_small_rows_dg.load() : 1;
+    // Lanes per row as in the gridder (small_rows_degrid for supports up to 8).
+    const int lpr = lanes_per_row(g, true);
     bool done = false;
     if constexpr (sizeof(R) == 4) {
       // the default subgrid edge as a compile-time constant (see the gridder)
       if (g.SG == (g.npol == 4 ? 32 : 48)) {
         done = true;
+        auto by_lpr = [&](auto npol_c, auto sg_c) {
+          constexpr int NP = decltype(npol_c)::value, SGV = decltype(sg_c)::value;
+          return lpr == 8 ? k_degrid_lean<R, NP, kWarps, true, 8, SGV>
+                          : lpr == 16 ? k_degrid_lean<R, NP, kWarps, true, 16, SGV>
+                                      : lpr == 32 ? k_degrid_lean<R, NP, kWarps, true, 32, SGV>
+                                                  : k_degrid_lean<R, NP, kWarps, true, 0, SGV>;
+        };
         if (g.npol == 4)
-          kern = rpw == 4 ? k_degrid_lean<R, 4, kWarps, true, 8, 32>
-                          : rpw == 2 ? k_degrid_lean<R, 4, kWarps, true, 16, 32>
-                                     : k_degrid_lean<R, 4, kWarps, true, 32, 32>;
+          kern = by_lpr(IntC<4>(), IntC<32>());
         else if (g.npol == 2)
-          kern = rpw == 4 ? k_degrid_lean<R, 2, kWarps, true, 8, 48>
-                          : rpw == 2 ? k_degrid_lean<R, 2, kWarps, true, 16, 48>
-                                     : k_degrid_lean<R, 2, kWarps, true, 32, 48>;
+          kern = by_lpr(IntC<2>(), IntC<48>());
         else
-          kern = rpw == 4 ? k_degrid_lean<R, 1, kWarps, true, 8, 48>
-                          : rpw == 2 ? k_degrid_lean<R, 1, kWarps, true, 16, 48>
-                                     : k_degrid_lean<R, 1, kWarps, true, 32, 48>;
+          kern = by_lpr(IntC<1>(), IntC<48>());
       }
     }
     if (!done)  // runtime edge: rows per warp chosen per segment only
@@ -2135,10 +2176,12 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
   const bool loops = g_tune_degrid_kernel.load() >= 2;  // the lean kernels loop over chunks
   const unsigned blocks = loops ? chunk_grid(kern, smem, nvis, chunk) : (unsigned)((nvis + chunk - 1) / chunk);
   if (blocks == 0) return ARLGPU_OK;
+  uint32_t *queue = loops ? work_queue(b, 1, st) : nullptr;
+  if (queue) ARL_CUDA(cudaMemsetAsync(queue, 0, 4, st));
   kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk, nvis,
                                           static_cast<const typename Cplx<R>::T *>(cf),
                                           static_cast<const typename Cplx<R>::T *>(grid),
-                                          static_cast<typename VisT<R>::C *>(vis_out));
+                                          static_cast<typename VisT<R>::C *>(vis_out), queue);
   ARL_LAUNCH_CHECK();
   count_launch(1);
   return ARLGPU_OK;
@@ -2277,10 +2320,11 @@ extern "C" int arlgpu_set_tuning(const char *key, int value) {
   else if (k == "degrid_kernel" && value >= 0 && value <= 3) g_tune_degrid_kernel = value;
   else if (k == "subgrid" && (value == 0 || (value >= 16 && value <= 128))) g_tune_subgrid = value;
   else if (k == "chunk" && value >= 32 && value <= (1 << 20)) g_tune_chunk = value;
-  else if (k == "persistent" && (value == 0 || value == 1)) g_tune_persistent = value;
+  else if (k == "persistent" && value >= 0 && value <= 2) g_tune_persistent = value;
   else if (k == "dsfft" && (value == 0 || value == 1)) g_tune_dsfft = value;
   else if (k == "small_rows" && (value == 1 || value == 2 || value == 4)) g_tune_small_rows = value;
   else if (k == "small_rows_degrid" && (value == 1 || value == 2 || value == 4)) g_tune_small_rows_dg = value;
+  else if (k == "lanes_per_row" && (value == 0 || value == 8 || value == 16 || value == 32)) g_tune_lanes = value;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key or value: %s = %d", key, value);
   return ARLGPU_OK;
 }
@@ -2296,6 +2340,7 @@ extern "C" int arlgpu_get_tuning(const char *key, int *value) {
   else if (k == "dsfft") *value = g_tune_dsfft;
   else if (k == "small_rows") *value = g_tune_small_rows;
   else if (k == "small_rows_degrid") *value = g_tune_small_rows_dg;
+  else if (k == "lanes_per_row") *value = g_tune_lanes;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key: %s", key);
   return ARLGPU_OK;
 }

@@ -44,7 +44,8 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // sorted RowMap, histogram, offsets) at the maximum sizes above.
 constexpr size_t kScratchBytes = align256(kMaxRows * 4) + align256(kMaxRows * 16) + align256(kMaxRows * 4) +
                                  align256(kMaxRows * 16) + align256((kMaxBins + 1) * 4) +
-                                 align256((kMaxBins + 2) * 4) + align256(kMaxBins * 8);  // + plane-mean partials
+                                 align256((kMaxBins + 2) * 4) + align256(kMaxBins * 8) +  // plane-mean partials
+                                 align256(16);                                            // work-queue words
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 

@@ -18,6 +18,8 @@ GRID_KERNELS = (0, 1, 2, 4)  # shared atomics + TwoSum, band owner + Kahan, lean
 DEGRID_KERNELS = (0, 1, 2, 3)  # warp per row, 32-row batches, lean warp per row, lean packed FMA
 SUBGRIDS = (32, 48, 64)
 CHUNKS = (512, 2048)
+LANES = (0, 8, 16, 32)                          # lanes per row: per segment, or fixed
+SMALL_ROWS = ((1, 1), (2, 2), (4, 4), (2, 4))   # (gridder, degridder) rows per warp, supports <= 8
 
 
 def set_tuning(**kw):
@@ -29,7 +31,8 @@ def set_tuning(**kw):
 def get_tuning():
     lib = nat.load()
     out = {}
-    for k in ('grid_kernel', 'degrid_kernel', 'subgrid', 'chunk', 'persistent', 'dsfft', 'small_rows', 'small_rows_degrid'):
+    for k in ('grid_kernel', 'degrid_kernel', 'subgrid', 'chunk', 'persistent', 'dsfft', 'small_rows', 'small_rows_degrid',
+              'lanes_per_row'):
         v = ctypes.c_int()
         nat.check(lib.arlgpu_get_tuning(k.encode(), ctypes.byref(v)))
         out[k] = v.value
@@ -104,8 +107,11 @@ def stage_times(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps=3):
 def autotune(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps=2, subgrids=SUBGRIDS, chunks=CHUNKS,
              grid_kernels=GRID_KERNELS, degrid_kernels=DEGRID_KERNELS):
     """Pick the fastest (subgrid, chunk) and, for it, the fastest gridder and
-    degridder variants, timing plan, grid and degrid separately on these rows.
-    Returns (best setting, {setting string: (plan, grid, degrid) ms})."""
+    degridder variants, then lanes per row (threads per visibility; rows per
+    warp for supports up to 8) and the chunk assignment (hardware scheduling,
+    a static resident grid, or the device work queue), timing plan, grid and
+    degrid separately on these rows.  Returns (best setting, {setting string:
+    (plan, grid, degrid) ms})."""
     results = {}
     best, best_ms = None, float('inf')
     for sg, ch in itertools.product(subgrids, chunks):
@@ -131,9 +137,37 @@ def autotune(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps=2, subgrids=SUBGR
         if total < best_ms:
             best_ms = total
             best = dict(grid_kernel=gk, degrid_kernel=dk, subgrid=sg, chunk=ch)
-    # persistent grid (resident CTAs looping over chunks) or one CTA per chunk
+    # Lanes per row (threads per visibility): chosen per segment by its
+    # largest support (0), or fixed for every segment; for supports up to 8
+    # also the rows-per-warp keys.  Gridder and degridder are timed apart, so
+    # each keeps its own best.
+    set_tuning(persistent=0, **best)
+    lanes_opts = [dict(lanes_per_row=v) for v in LANES]
+    if cd.support <= 8:
+        lanes_opts += [dict(lanes_per_row=0, small_rows=a, small_rows_degrid=b) for a, b in SMALL_ROWS]
+    g_best, d_best = None, None
+    for opt in lanes_opts:
+        full = dict(dict(lanes_per_row=0, small_rows=2, small_rows_degrid=4), **opt)
+        set_tuning(**full)
+        t = stage_times(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps)
+        results['lanes/' + '/'.join('%s%d' % (k, v) for k, v in sorted(opt.items()))] = tuple(round(x, 4) for x in t)
+        if g_best is None or t[1] < g_best[0]:
+            g_best = (t[1], full)
+        if d_best is None or t[2] < d_best[0]:
+            d_best = (t[2], full)
+    # One lanes_per_row key serves both kernels: keep the one whose grid +
+    # degrid sum is smallest among the two winners.
+    cands = {}
+    for _, full in (g_best, d_best):
+        set_tuning(**full)
+        t = stage_times(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps)
+        cands[tuple(sorted(full.items()))] = t[1] + t[2]
+    best.update(dict(min(cands, key=cands.get)))
+    # Chunk assignment: one CTA per chunk (hardware block scheduling, 0), a
+    # resident grid taking every gridDim-th chunk (1), or a resident grid fed
+    # by the device work queue (2).
     step_ms = {}
-    for pers in (1, 0):
+    for pers in (0, 1, 2):
         set_tuning(persistent=pers, **best)
         t = stage_times(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps)
         results['best/persistent%d' % pers] = tuple(round(x, 4) for x in t)

@@ -102,14 +102,19 @@ unsigned long long arlgpu_kernel_launches(void);
  *   "subgrid"       subgrid edge in cells (16..128), 0 = automatic (48, or 32 when 4 pols)
  *   "chunk"         sorted rows per gridder / degridder CTA (32..2^20, default 512)
  *   "persistent"    1 = the lean and fixed-point kernels run as one grid of resident CTAs,
- *                   each looping over every gridDim-th chunk; 0 = one CTA per chunk, which the
- *                   hardware schedules dynamically (default: measured faster on C2)
+ *                   each looping over every gridDim-th chunk; 2 = the same resident grid fed by
+ *                   a device work queue (each CTA takes the next unclaimed chunk with one
+ *                   atomic); 0 = one CTA per chunk, which the hardware schedules dynamically
+ *                   (default)
  *   "dsfft"         FP32C inverse transforms (invert_2d and w-stacking): 1 = double-single
  *                   FFT on the FP32 pipes for power-of-two sizes 64..8192 (default),
  *                   0 = cuFFT complex128
  *   "small_rows"    rows per warp (1, 2 or 4; default 2) in the FP32C fixed-point gridder when the
  *                   largest support is at most 8 (64 taps) and the subgrid edge is the default
  *   "small_rows_degrid"  the same for the packed degridder (default 4)
+ *   "lanes_per_row" 0 = lanes per row (threads per visibility) chosen per segment and support
+ *                   (default); 8, 16 or 32 = that many lanes per row in every segment of the
+ *                   FP32C fixed-point gridder and packed degridder at the default subgrid edge
  *                   Otherwise both kernels choose per segment: two rows per warp when the
  *                   segment's largest support is at most 16, four (degridder) at most 8.
  * No reference counterpart (ARL has one Python loop per function). */

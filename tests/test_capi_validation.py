@@ -111,12 +111,14 @@ def test_tuning_keys(nat):
     lib = nat.load()
     v = ctypes.c_int(-1)
     for key in ('grid_kernel', 'degrid_kernel', 'subgrid', 'chunk', 'persistent', 'dsfft', 'small_rows',
-                'small_rows_degrid'):
+                'small_rows_degrid', 'lanes_per_row'):
         assert lib.arlgpu_get_tuning(key.encode(), ctypes.byref(v)) == OK
         old = v.value
         assert lib.arlgpu_set_tuning(key.encode(), old) == OK  # current values are valid
     assert lib.arlgpu_set_tuning(b'no_such_key', 1) == INVALID
     assert lib.arlgpu_set_tuning(b'small_rows', 3) == INVALID
+    assert lib.arlgpu_set_tuning(b'lanes_per_row', 4) == INVALID
+    assert lib.arlgpu_set_tuning(b'persistent', 3) == INVALID
     assert lib.arlgpu_get_tuning(b'no_such_key', ctypes.byref(v)) != OK
 
 

@@ -459,6 +459,32 @@ def test_kernel_variants_vs_oracle(arl, oracle, grid_kernel, degrid_kernel, subg
         arl.tune.set_tuning(**before)
 
 
+@pytest.mark.parametrize('persistent,lanes_per_row,chunk', [(1, 0, 256), (2, 0, 256), (2, 8, 64), (2, 16, 512),
+                                                          (2, 32, 128), (0, 8, 512), (0, 32, 512)])
+@pytest.mark.parametrize('npol', [1, 4])
+def test_work_queue_and_lanes_per_row_vs_oracle(arl, oracle, persistent, lanes_per_row, chunk, npol):
+    """The resident grid with static (1) or work-queue (2) chunk assignment,
+    and every fixed lanes-per-row choice, against the oracle.  Small chunks
+    make many more chunks than resident CTAs, so the queue hands out most of
+    them; supports 12, 8 and 4 mix rows of different supports in one bin."""
+    before = arl.tune.get_tuning()
+    try:
+        arl.tune.set_tuning(persistent=persistent, lanes_per_row=lanes_per_row, chunk=chunk)
+        for precision in ('fp64', 'fp32c'):
+            rng = numpy.random.default_rng(27 + npol)
+            im, cf, vis, maps, gax = _random_case(arl, oracle, rng, 128, 4e-3, 8, 12, 30000, 2, npol, 3, 20.0, True)
+            arl.set_plane_support(cf, [12, 8, 4])
+            gd, sumwt = arl.grid_visibility_to_griddata(vis, arl.create_griddata_from_image(im), cf,
+                                                        precision=precision)
+            g_ref, sw_ref = oracle.grid_vec(vis.vis, vis.imaging_weight, maps, cf.data, gax['shape'])
+            assert rel(gd.data, g_ref) < TOL[precision]
+            assert rel(sumwt, sw_ref) < TOLW[precision]
+            out = arl.degrid_visibility_from_griddata(vis, gd, cf, precision=precision)
+            assert rel(out.vis, oracle.degrid_vec(g_ref, maps, cf.data)) < TOL[precision]
+    finally:
+        arl.tune.set_tuning(**before)
+
+
 @pytest.mark.parametrize('small_rows,small_rows_degrid', [(1, 1), (2, 2), (4, 4), (2, 4)])
 @pytest.mark.parametrize('npol', [1, 2, 4])
 def test_small_support_rows_per_warp_vs_oracle(arl, oracle, small_rows, small_rows_degrid, npol):
