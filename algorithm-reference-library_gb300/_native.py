@@ -52,6 +52,7 @@ SIGNATURES = {
                                            _vp, _sz, _vp]),
     'arlgpu_degrid_planned': (ctypes.c_int, [_i64, ctypes.c_int, _vp, _P(CfDesc), _vp, _P(GridDesc), _vp, _vp, _sz,
                                              _vp]),
+    'arlgpu_plan_flags': (ctypes.c_int, [_i64, _P(GridDesc), _P(CfDesc), _vp, _sz, _P(ctypes.c_uint32), _vp]),
     'arlgpu_plan_plane_mean_w': (ctypes.c_int, [_vp, _i64, _P(GridDesc), _P(CfDesc), _vp, _sz, _vp, _vp]),
     'arlgpu_wstack_grid_to_image': (ctypes.c_int, [_vp, _P(GridDesc), ctypes.c_int, _vp, _vp, _f64, _vp, _vp, _vp,
                                                    _vp]),

@@ -15,6 +15,8 @@
 //              one vector atomic per touched cell
 //   k_degrid   same chunking; the bin's subgrid is staged in shared memory and
 //              each row is a warp-wide dot product reduced with shuffles
+#include <cuda.h>  // CUtensorMap and its enums; the encoder is looked up in the driver at run time
+
 #include <cstdarg>
 #include <cstring>
 #include <atomic>
@@ -1775,6 +1777,410 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
 }
 
 // ---------------------------------------------------------------------------
+// K4 (TMA variant, degrid_kernel 4): the packed FP32 degridder with the grid
+// footprint and the kernel taps staged in shared memory by the tensor-memory
+// accelerator.  FP32C, one polarisation, supports up to 32, subgrid edge 48.
+//
+// Grid: after the footprint pass, thread 0 loads the segment's whole
+// (SG + 2) x SG subgrid tile of its grid plane with one 3-D tensor copy
+// (cells outside the grid arrive as zeros), into the tap-ring area, which is
+// idle between segments; the footprint cells are then expanded to the
+// (re, re, im, im) layout of the packed multiply-adds.
+//
+// Taps: each warp streams its rows' sub-kernels through a private ring in
+// shared memory.  A row's window of sz x sz taps is cut into pieces of up to
+// eight kernel rows; piece k of a row is one 2-D tensor copy of a box
+// bw x 8 taps (bw = sz, or sz + 2 when the window's first column is odd, so
+// that the copy starts on a 16-byte boundary) from the cf table viewed as
+// [rows][S].  Lane 0 issues pieces in order into the ring (a byte FIFO with
+// kQ mbarriers, piece q completing on barrier q mod kQ in phase (q / kQ) & 1);
+// the warp consumes them in the same order.  While it computes the current
+// step of rows (one, two or four rows per warp, as the lean kernel), the
+// pieces of its next step (already taken from the segment's row counter) are
+// in flight.  Every wait is bounded: a wait that gives up sets bit 0 of *err
+// and the kernel carries on, draining its copies (also bounded) before it
+// exits, so a fault shows as a flag, never as a hang.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_done(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for the phase of the given parity to complete; gives up after about a
+// second (2^24 polls, backing off with nanosleep) and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 24); ++it) {
+    if (mbar_done(bar, parity)) return true;
+    if (it >= 32) __nanosleep(64);
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+struct TmaDesc {
+  CUtensorMap tap[16];  // cf table as [rows][S] 8-byte taps; map m has a box of (2 m + 2) x 8 taps
+  CUtensorMap grid;     // grid as [planes][ny][nx] 8-byte cells; box (SG + 2) x SG x 1
+};
+
+constexpr int kTmaRing = 6144;  // tap-ring bytes per warp
+constexpr int kTmaQ = 8;        // tap pieces in flight per warp (mbarriers per warp)
+constexpr int kTmaSG = 48;      // subgrid edge of the TMA degridder
+constexpr int kTmaMaxS = 32;    // largest support it takes
+
+// Tap pieces of one step of rows (one to four rows), identical in every lane
+// of the warp.  Pieces are numbered column-major: piece (h, k) -- kernel rows
+// 8k .. 8k + 7 of row h -- comes after every piece of a smaller k.
+struct TmaStep {
+  int n;                 // rows in the step
+  int np[4], bw[4];      // pieces and box width of each row
+  int x[4], y[4];        // copy coordinates of each row's piece 0
+  int total, maxk;       // pieces in the step, largest piece count
+};
+
+__device__ __forceinline__ int tma_piece_index(const TmaStep &s, int h, int k) {
+  int i = 0;
+  for (int kk = 0; kk < k; ++kk)
+    for (int r = 0; r < s.n; ++r) i += kk < s.np[r];
+  for (int r = 0; r < h; ++r) i += k < s.np[r];
+  return i;
+}
+
+template <int NW>
+__global__ void __launch_bounds__(NW * 32, 2)
+k_degrid_tma(const __grid_constant__ TmaDesc tmd, Geom g, const RowMap *__restrict__ smap,
+             const uint32_t *__restrict__ sidx, const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
+             const float2 *__restrict__ cf, const float2 *__restrict__ grid, float2 *__restrict__ vis_out,
+             uint32_t *__restrict__ queue, uint32_t *__restrict__ err) {
+  constexpr int SG = kTmaSG, SG2 = SG * SG, RW = SG + 2;  // RW: row pitch of the copied grid tile
+  extern __shared__ __align__(16) unsigned char smraw[];
+  // Tensor copies land on 128-byte boundaries: the dynamic area starts after
+  // the static one, so round its base up (the launch adds 128 bytes).
+  unsigned char *base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
+  float4 *sub4 = reinterpret_cast<float4 *>(base);                        // [SG][SG] (re, re, im, im)
+  unsigned char *ring_all = base + (size_t)SG2 * sizeof(float4);          // [NW][kTmaRing], 128-byte aligned
+  unsigned char *tab = ring_all + (size_t)NW * kTmaRing;
+  __shared__ __align__(8) uint64_t s_bar[NW][kTmaQ];
+  __shared__ __align__(8) uint64_t s_gbar;
+  __shared__ uint32_t s_poff[NW][kTmaQ], s_pend[NW][kTmaQ];
+  __shared__ int s_red[2][NW * 6];
+  __shared__ uint32_t s_next[2], s_chunk;
+  const uint32_t nvalid = off[g.nbins];
+  const uint64_t nchunks = ((uint64_t)nvis + chunk - 1) / chunk;
+  if (blockIdx.x >= nchunks) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int S = g.S, O = g.O;
+  const int64_t plane_elems = (int64_t)g.ny * g.nx;
+  unsigned char *ring = ring_all + (size_t)warp * kTmaRing;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < NW; ++w)
+      for (int q = 0; q < kTmaQ; ++q) mbar_init(&s_bar[w][q], 1);
+    mbar_init(&s_gbar, 1);
+    fence_mbar_init();
+  }
+  build_tap_table(tab, S);
+  __syncthreads();
+  // Warp-uniform FIFO state: bytes allocated / released (monotone), pieces
+  // issued / consumed.
+  uint32_t tail = 0, head = 0, qi = 0, qc = 0;
+  uint32_t gphase = 0;  // phase parity of the grid-tile barrier
+  bool ok = true;
+
+  // Issue piece i of step st if the ring and the barrier window have room.
+  auto try_issue = [&](const TmaStep &st, int i) -> bool {
+    int h = 0, k = 0;
+    {
+      int c = i;
+      bool found = false;
+      for (int kk = 0; kk < 4 && !found; ++kk)
+        for (int r = 0; r < st.n && !found; ++r)
+          if (kk < st.np[r]) {
+            if (c == 0) {
+              h = r;
+              k = kk;
+              found = true;
+            } else {
+              --c;
+            }
+          }
+    }
+    const uint32_t bytes = (uint32_t)st.bw[h] * 64u;
+    uint32_t o = tail % kTmaRing;
+    const uint32_t skip = o + bytes > (uint32_t)kTmaRing ? kTmaRing - o : 0u;
+    if (tail + skip + bytes - head > (uint32_t)kTmaRing || qi - qc >= (uint32_t)kTmaQ) return false;
+    tail += skip;
+    o = tail % kTmaRing;
+    const int slot = qi % kTmaQ;
+    if (lane == 0) {
+      s_poff[warp][slot] = o;
+      s_pend[warp][slot] = tail + bytes;
+      fence_proxy_async();  // earlier generic reads of this ring space come first
+      mbar_expect_tx(&s_bar[warp][slot], bytes);
+      tma_load_2d(ring + o, &tmd.tap[st.bw[h] / 2 - 1], st.x[h], st.y[h] + 8 * k, &s_bar[warp][slot]);
+    }
+    tail += bytes;
+    ++qi;
+    return true;
+  };
+  // Release the first `cnt` unconsumed pieces (in order).
+  auto release = [&](int cnt) {
+    for (int c = 0; c < cnt; ++c) {
+      head = s_pend[warp][qc % kTmaQ];
+      ++qc;
+    }
+  };
+
+  int parity = 0;
+  for (uint64_t cb = blockIdx.x; cb < nchunks; cb = next_chunk(cb, queue, &s_chunk)) {
+  const uint32_t c0 = (uint32_t)(cb * chunk);
+  if (c0 + chunk > nvalid) {  // rows the plan rejected: zero output
+    const uint32_t b = max(c0, nvalid), e = (uint32_t)min((uint64_t)c0 + chunk, (uint64_t)nvis);
+    for (uint32_t r = b + threadIdx.x; r < e; r += blockDim.x) vis_out[sidx[r]] = make_float2(0.f, 0.f);
+    if (c0 >= nvalid) continue;
+  }
+  const uint32_t c1 = min(c0 + chunk, nvalid);
+  uint32_t pos = c0;
+  while (pos < c1) {
+    const SegInfo sg = seg_at(pos, c1, smap, off, g);
+    if (threadIdx.x == 0) s_next[parity] = pos;  // published by the barrier in seg_box
+    uint32_t *next_row = &s_next[parity];
+    // The footprint pass ends in a barrier: every warp has finished the
+    // previous segment (its ring drained, its grid reads done).
+    const SegBox box = seg_box<NW, 1, false>(sg, pos, smap, sidx, nullptr, nullptr, g, s_red[parity]);
+    parity ^= 1;
+    const bool direct = seg_direct(box, sg.end - pos);
+    const int64_t gplane = (int64_t)sg.ch * g.nw + sg.zg;
+    if (!direct) {
+      const int gx0 = sg.u0 & ~1, xs = sg.u0 - gx0;  // the copy starts on an even column
+      if (threadIdx.x == 0) {
+        fence_proxy_async();
+        mbar_expect_tx(&s_gbar, (uint32_t)(RW * SG * 8));
+        tma_load_3d(ring_all, &tmd.grid, gx0, sg.v0, (int)gplane, &s_gbar);
+      }
+      if (!mbar_wait(&s_gbar, gphase)) ok = false;
+      gphase ^= 1;
+      const float2 *raw = reinterpret_cast<const float2 *>(ring_all);
+      for (int y = box.y0 + warp; y < box.y1; y += NW)
+        for (int x = box.x0 + lane; x < box.x1; x += 32) {
+          const float2 v = raw[y * RW + x + xs];
+          sub4[y * SG + x] = make_float4(v.x, v.x, v.y, v.y);
+        }
+      __syncthreads();  // the tile is expanded; the rings may be refilled
+    }
+    auto row_loop = [&](auto lpr_c) {
+      constexpr int LP = decltype(lpr_c)::value;
+      constexpr int RP = 32 / LP;
+      const int hl = lane & (LP - 1), half = lane / LP;
+      // Row metadata of a step starting at r: this lane's own row (m, idx)
+      // and the warp-uniform copy geometry of every row.
+      auto load_step = [&](uint32_t r, RowMap &m, uint32_t &idx, TmaStep &st) {
+        const bool act = r + half < sg.end;
+        int np = 0, bw = 2, x = 0, y = 0;
+        if (act) {
+          m = smap[r + half];
+          idx = sidx[r + half];
+          const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+          const int sz = plane_sz(g, zc), toff = (S - sz) >> 1;
+          const int64_t e = sg.ch * g.cf_chan_stride + zc * g.cf_z_stride + (int64_t)(vf * O + uf) * S * S;
+          np = (sz + 7) >> 3;
+          bw = sz + 2 * (toff & 1);
+          x = toff & ~1;
+          y = (int)(e / S) + toff;
+        }
+        st.n = 0;
+        st.total = 0;
+        st.maxk = 0;
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int src = h < RP ? h * LP : 0;
+          const int nph = __shfl_sync(0xffffffffu, np, src);
+          st.np[h] = h < RP ? nph : 0;
+          st.bw[h] = __shfl_sync(0xffffffffu, bw, src);
+          st.x[h] = __shfl_sync(0xffffffffu, x, src);
+          st.y[h] = __shfl_sync(0xffffffffu, y, src);
+          if (h < RP && r + h < sg.end) st.n = h + 1;
+          st.total += st.np[h];
+          st.maxk = max(st.maxk, st.np[h]);
+        }
+      };
+      uint32_t rbase = 0;
+      if (lane == 0) rbase = atomicAdd(next_row, (uint32_t)RP);
+      rbase = __shfl_sync(0xffffffffu, rbase, 0);
+      RowMap m{};
+      uint32_t idx = 0;
+      TmaStep cur;
+      load_step(rbase, m, idx, cur);
+      int ci = 0;  // pieces of cur issued
+      while (ci < cur.total && try_issue(cur, ci)) ++ci;
+      uint32_t cq0 = qi - ci;  // sequence number of cur's first piece
+      __syncwarp();
+      while (rbase < sg.end) {
+        uint32_t rn = 0;
+        if (lane == 0) rn = atomicAdd(next_row, (uint32_t)RP);
+        rn = __shfl_sync(0xffffffffu, rn, 0);
+        RowMap mn{};
+        uint32_t idxn = 0;
+        TmaStep nxt;
+        load_step(rn, mn, idxn, nxt);
+        int ni = 0;
+        // the rest of cur, then nxt, as far as the ring allows
+        auto refill = [&]() {
+          while (ci < cur.total && try_issue(cur, ci)) ++ci;
+          if (ci == cur.total)
+            while (ni < nxt.total && try_issue(nxt, ni)) ++ni;
+          __syncwarp();
+        };
+        refill();
+        const bool act = rbase + half < sg.end;
+        const int zc = m.sub >> 16;
+        const int sz = act ? plane_sz(g, zc) : 0;
+        const int bwr = sz + 2 * (((S - sz) >> 1) & 1), xsr = ((S - sz) >> 1) & 1;
+        const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
+        const int wofs4 = (wv - sg.v0) * SG + (wu - sg.u0) + hl, dg = SG - sz;
+        const unsigned char *tj = tab + tap_base(sz > 0 ? sz : 2) + hl;
+        unsigned long long pa = 0ull, pb = 0ull;
+        for (int k = 0; k < cur.maxk; ++k) {
+          // column k of cur must be in flight before anyone waits on it
+          while (ci < cur.total && ci <= tma_piece_index(cur, cur.n - 1, k) && try_issue(cur, ci)) ++ci;
+          __syncwarp();
+          const bool mine = act && k * 8 < sz;
+          if (mine) {
+            const uint32_t q = cq0 + (uint32_t)tma_piece_index(cur, half, k);
+            const int slot = q % kTmaQ;
+            if (!mbar_wait(&s_bar[warp][slot], (q / kTmaQ) & 1)) ok = false;
+            const float2 *kl = reinterpret_cast<const float2 *>(ring + s_poff[warp][slot]) + xsr - 8 * k * bwr + hl;
+            const int dk = bwr - sz;
+            const int t1 = min(8 * k + 8, sz) * sz;
+            auto group = [&](int t, auto kk, auto masked) {
+              constexpr int K = decltype(kk)::value;
+              int j[K];
+              bool on[K];
+              unsigned long long tp[K];
+              ulonglong2 gv[K];
+#pragma unroll
+              for (int u = 0; u < K; ++u) {
+                on[u] = !decltype(masked)::value || t + LP * u + hl < t1;
+                j[u] = on[u] ? tj[t + LP * u] : 0;
+                tp[u] = on[u] ? *reinterpret_cast<const unsigned long long *>(kl + t + LP * u + j[u] * dk) : 0ull;
+                gv[u] = on[u] ? *reinterpret_cast<const ulonglong2 *>(sub4 + wofs4 + t + LP * u + j[u] * dg)
+                              : make_ulonglong2(0ull, 0ull);
+              }
+#pragma unroll
+              for (int u = 0; u < K; ++u) {
+                pa = ffma2(gv[u].x, tp[u], pa);
+                pb = ffma2(gv[u].y, tp[u], pb);
+              }
+            };
+            int t = 8 * k * sz;
+            for (; t + 4 * LP <= t1; t += 4 * LP) group(t, IntC<4>(), BoolC<false>());
+            switch ((t1 - t + LP - 1) / LP) {
+              case 1: group(t, IntC<1>(), BoolC<true>()); break;
+              case 2: group(t, IntC<2>(), BoolC<true>()); break;
+              case 3: group(t, IntC<3>(), BoolC<true>()); break;
+              case 4: group(t, IntC<4>(), BoolC<true>()); break;
+              default: break;
+            }
+          }
+          __syncwarp();  // every lane is done with column k
+          int cnt = 0;
+          for (int h = 0; h < cur.n; ++h) cnt += k < cur.np[h];
+          release(cnt);
+          refill();
+        }
+        const float2 a2 = *reinterpret_cast<const float2 *>(&pa);
+        const float2 b2 = *reinterpret_cast<const float2 *>(&pb);
+        float sx = a2.x - b2.y, sy = a2.y + b2.x;
+        for (int o = LP / 2; o > 0; o >>= 1) {
+          sx += __shfl_xor_sync(0xffffffffu, sx, o);
+          sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        }
+        if (act && hl == 0) vis_out[idx] = make_float2(sx, sy);
+        // nxt becomes cur
+        cq0 += (uint32_t)cur.total;
+        cur = nxt;
+        ci = ni;
+        m = mn;
+        idx = idxn;
+        rbase = rn;
+      }
+    };
+    if (direct) {
+      // Few rows for the footprint: taps and grid cells straight from global
+      // memory, one row per warp.
+      const float2 *gp = grid + gplane * plane_elems;
+      uint32_t r = 0;
+      if (lane == 0) r = atomicAdd(next_row, 1u);
+      r = __shfl_sync(0xffffffffu, r, 0);
+      while (r < sg.end) {
+        const RowMap mr = smap[r];
+        const uint32_t ir = sidx[r];
+        const int uf = mr.sub & 0xff, vf = (mr.sub >> 8) & 0xff, zc = mr.sub >> 16;
+        const int sz = plane_sz(g, zc), toff = (S - sz) >> 1;
+        const float2 *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
+                           ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+        const int wu = mr.pu - (sz >> 1), wv = mr.pv - (sz >> 1);
+        float ax = 0.f, ay = 0.f;
+        for (int t = lane; t < sz * sz; t += 32) {
+          const int j = t / sz, i = t - j * sz;
+          const float2 tp = kb[j * S + i];
+          const float2 gv = gp[(int64_t)(wv + j) * g.nx + wu + i];
+          ax += gv.x * tp.x - gv.y * tp.y;
+          ay += gv.x * tp.y + gv.y * tp.x;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          ax += __shfl_xor_sync(0xffffffffu, ax, o);
+          ay += __shfl_xor_sync(0xffffffffu, ay, o);
+        }
+        if (lane == 0) vis_out[ir] = make_float2(ax, ay);
+        if (lane == 0) r = atomicAdd(next_row, 1u);
+        r = __shfl_sync(0xffffffffu, r, 0);
+      }
+    } else if (box.sz <= 8) {
+      row_loop(IntC<8>());
+    } else if (box.sz <= 16) {
+      row_loop(IntC<16>());
+    } else {
+      row_loop(IntC<32>());
+    }
+    pos = sg.end;
+  }
+  }
+  // Leave no copy in flight: every piece this warp issued has completed
+  // (immediate unless a wait above gave up).
+  if (lane == 0)
+    for (uint32_t q = qi > (uint32_t)kTmaQ ? qi - kTmaQ : 0u; q < qi; ++q)
+      if (!mbar_wait(&s_bar[warp][q % kTmaQ], (q / kTmaQ) & 1)) ok = false;
+  if (!ok) atomicOr(err, 1u);
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 static double rcp(double x) { return 1.0 / x; }
@@ -2128,19 +2534,113 @@ static int launch_grid(const Geom &g, const PlanBufs &b, int64_t nvis, const voi
   return ARLGPU_OK;
 }
 
+// The driver's tensor-map encoder, looked up once through the runtime (no
+// link against libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// Tensor maps of the TMA degridder, or false when this call cannot take it
+// (alignment, sizes, or no encoder).
+static bool make_tma_desc(const Geom &g, const void *cf, const void *grid, TmaDesc *d) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  if ((reinterpret_cast<uintptr_t>(cf) & 15) || (reinterpret_cast<uintptr_t>(grid) & 15)) return false;
+  // Row strides of both tables a multiple of 16 bytes (S and nx even), and
+  // every sub-kernel starting on a table row (channel stride a multiple of S).
+  if (g.S > kTmaMaxS || g.S < 2 || (g.S & 1) || g.cf_chan_stride < 0 || (g.cf_chan_stride % g.S) != 0 ||
+      (g.nx & 1))
+    return false;
+  const int64_t elems = (int64_t)(g.cf_nchan - 1) * g.cf_chan_stride + (int64_t)(g.cf_npol - 1) * g.cf_pol_stride +
+                        (int64_t)g.nz * g.cf_z_stride;
+  const int64_t rows = elems / g.S;
+  if (rows < 1 || rows > 0x7fffffffll) return false;
+  memset(d, 0, sizeof *d);
+  for (int m = 0; m < 16; ++m) {
+    const int bw = 2 * m + 2;
+    if (bw > g.S) break;
+    const cuuint64_t dims[2] = {(cuuint64_t)g.S, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)g.S * 8};
+    const cuuint32_t box[2] = {(cuuint32_t)bw, 8};
+    const cuuint32_t es[2] = {1, 1};
+    if (enc(&d->tap[m], CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<void *>(cf), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  const int64_t planes = (int64_t)g.nchan * g.npol * g.nw;
+  const cuuint64_t gdims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)planes};
+  const cuuint64_t gstr[2] = {(cuuint64_t)g.nx * 8, (cuuint64_t)g.nx * g.ny * 8};
+  const cuuint32_t gbox[3] = {(cuuint32_t)(kTmaSG + 2), (cuuint32_t)kTmaSG, 1};
+  const cuuint32_t ges[3] = {1, 1, 1};
+  return enc(&d->grid, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<void *>(grid), gdims, gstr, gbox, ges,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// degrid_kernel 4: the TMA degridder where it applies (FP32C, one
+// polarisation, support <= 32, subgrid edge 48, aligned tables); *launched
+// stays false (nothing launched) otherwise, and the caller runs the packed one.
+static int launch_degrid_tma(const Geom &g, const PlanBufs &b, int64_t nvis, const void *cf, const void *grid,
+                             void *vis_out, cudaStream_t st, bool *launched) {
+  *launched = false;
+  if (g.npol != 1 || g.SG != kTmaSG || g.S > kTmaMaxS) return ARLGPU_OK;
+  TmaDesc d;
+  if (!make_tma_desc(g, cf, grid, &d)) return ARLGPU_OK;
+  auto kern = k_degrid_tma<kWarps>;
+  const size_t smem = 128 + (size_t)kTmaSG * kTmaSG * 16 + (size_t)kWarps * kTmaRing + tap_table_bytes(g.S);
+  ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const uint32_t chunk = chunk_rows();
+  const unsigned blocks = chunk_grid(kern, smem, nvis, chunk);
+  if (blocks == 0) {
+    *launched = true;
+    return ARLGPU_OK;
+  }
+  uint32_t *queue = work_queue(b, 1, st);
+  if (queue) ARL_CUDA(cudaMemsetAsync(queue, 0, 4, st));
+  ARL_CUDA(cudaMemsetAsync(b.queue + 2, 0, 4, st));
+  kern<<<blocks, kWarps * 32, smem, st>>>(d, g, b.smap, b.sidx, b.offsets, chunk, nvis,
+                                          static_cast<const float2 *>(cf), static_cast<const float2 *>(grid),
+                                          static_cast<float2 *>(vis_out), queue, b.queue + 2);
+  ARL_LAUNCH_CHECK();
+  count_launch(1);
+  *launched = true;
+  return ARLGPU_OK;
+}
+
 template <typename R>
 static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const void *cf, const void *grid,
                          void *vis_out, cudaStream_t st) {
+  if constexpr (sizeof(R) == 4) {
+    if (g_tune_degrid_kernel.load() == 4) {
+      bool launched = false;
+      ARL_TRY(launch_degrid_tma(g, b, nvis, cf, grid, vis_out, st, &launched));
+      if (launched) return ARLGPU_OK;
+    }
+  }
   size_t smem = (size_t)g.npol * g.SG * g.SG * sizeof(typename Cplx<R>::T);
   auto kern = k_degrid<R, kWarps>;
   if (g_tune_degrid_kernel.load() == 1) {
     kern = k_degrid_batch<R, kWarps>;
-  } else if (g_tune_degrid_kernel.load() == 2 || (g_tune_degrid_kernel.load() == 3 && sizeof(R) == 8)) {
+  } else if (g_tune_degrid_kernel.load() == 2 || (g_tune_degrid_kernel.load() >= 3 && sizeof(R) == 8)) {
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
     kern = g.npol == 1 ? k_degrid_lean<R, 1, kWarps> : g.npol == 2 ? k_degrid_lean<R, 2, kWarps>
                                                                     : k_degrid_lean<R, 4, kWarps>;
     smem += tap_table_bytes(g.S);
-  } else if (g_tune_degrid_kernel.load() == 3) {  // FP32: packed multiply-adds
+  } else if (g_tune_degrid_kernel.load() >= 3) {  // FP32: packed multiply-adds (and where TMA does not apply)
     if (g.npol == 3) return fail(ARLGPU_ERR_UNSUPPORTED, "the lean degridder handles 1, 2 or 4 polarisations");
     // Lanes per row as in the gridder (small_rows_degrid for supports up to 8).
     const int lpr = lanes_per_row(g, true);
@@ -2313,11 +2813,25 @@ extern "C" int arlgpu_plan_plane_mean_w(const double *uvw, int64_t nvis, const a
   return ARLGPU_OK;
 }
 
+extern "C" int arlgpu_plan_flags(int64_t nvis, const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd,
+                                 const void *workspace, size_t workspace_bytes, uint32_t *flags_host, void *stream) {
+  Geom g;
+  ARL_TRY(make_geom(gd, cd, ARLGPU_FP32C, &g));
+  ARL_TRY(check_rows(nvis));
+  if (!flags_host) return fail(ARLGPU_ERR_INVALID, "null flags_host");
+  PlanBufs b;
+  ARL_TRY(plan_carve(const_cast<void *>(workspace), workspace_bytes, nvis, g, &b));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  ARL_CUDA(cudaMemcpyAsync(flags_host, b.queue + 2, 4, cudaMemcpyDeviceToHost, st));
+  ARL_CUDA(cudaStreamSynchronize(st));
+  return ARLGPU_OK;
+}
+
 extern "C" int arlgpu_set_tuning(const char *key, int value) {
   if (!key) return fail(ARLGPU_ERR_INVALID, "null key");
   const std::string k(key);
   if (k == "grid_kernel" && value >= 0 && value <= 5) g_tune_grid_kernel = value;
-  else if (k == "degrid_kernel" && value >= 0 && value <= 3) g_tune_degrid_kernel = value;
+  else if (k == "degrid_kernel" && value >= 0 && value <= 4) g_tune_degrid_kernel = value;
   else if (k == "subgrid" && (value == 0 || (value >= 16 && value <= 128))) g_tune_subgrid = value;
   else if (k == "chunk" && value >= 32 && value <= (1 << 20)) g_tune_chunk = value;
   else if (k == "persistent" && value >= 0 && value <= 2) g_tune_persistent = value;

@@ -15,7 +15,7 @@ from . import _native as nat
 from . import device as dv
 
 GRID_KERNELS = (0, 1, 2, 4)  # shared atomics + TwoSum, band owner + Kahan, lean atomics, fixed point
-DEGRID_KERNELS = (0, 1, 2, 3)  # warp per row, 32-row batches, lean warp per row, lean packed FMA
+DEGRID_KERNELS = (0, 1, 2, 3, 4)  # warp per row, 32-row batches, lean warp per row, lean packed FMA, TMA-staged
 SUBGRIDS = (32, 48, 64)
 CHUNKS = (512, 2048)
 LANES = (0, 8, 16, 32)                          # lanes per row: per segment, or fixed

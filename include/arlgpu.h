@@ -98,7 +98,10 @@ unsigned long long arlgpu_kernel_launches(void);
  *   "degrid_kernel" 0 = one warp per row, 1 = 32-row batches per warp,
  *                   2 = one warp per row, specialised on npol, groups of four steps,
  *                   3 = as 2 with the staged cells duplicated (re, re, im, im) so each tap is
- *                       two packed FP32 multiply-adds (default; FP32C, FP64 uses 2)
+ *                       two packed FP32 multiply-adds (default; FP32C, FP64 uses 2),
+ *                   4 = as 3 with the grid tile and each row's kernel taps brought into shared
+ *                       memory by TMA tensor copies (FP32C, one polarisation, support <= 32,
+ *                       subgrid 48, 16-byte aligned tables, even nx; otherwise 3)
  *   "subgrid"       subgrid edge in cells (16..128), 0 = automatic (48, or 32 when 4 pols)
  *   "chunk"         sorted rows per gridder / degridder CTA (32..2^20, default 512)
  *   "persistent"    1 = the lean and fixed-point kernels run as one grid of resident CTAs,
@@ -158,6 +161,13 @@ int arlgpu_grid_planned(const void *vis, const void *weight, int64_t nvis, int p
 int arlgpu_degrid_planned(int64_t nvis, int precision, const void *cf, const arlgpu_cf_desc *cd, const void *grid,
                           const arlgpu_grid_desc *gd, void *vis_out, const void *workspace,
                           size_t workspace_bytes, void *stream);
+
+/* Status flags the kernels of the last planned call left in the plan's
+ * workspace (same nvis / gd / cd as the plan): bit 0 = a bounded wait of the TMA
+ * degridder (degrid_kernel 4) gave up, so that call's output is not to be
+ * trusted.  Synchronises `stream`.  No reference counterpart. */
+int arlgpu_plan_flags(int64_t nvis, const arlgpu_grid_desc *gd, const arlgpu_cf_desc *cd, const void *workspace,
+                      size_t workspace_bytes, uint32_t *flags_host, void *stream);
 
 /* Mean w of the rows that a plan assigned to each grid w-plane (the slice mean
  * numpy.average(vis.w) of invert/predict_wstack_single, wstack_single.py:43,83);
