@@ -58,6 +58,9 @@ def parse():
     ap.add_argument('--profile-rows', type=int, default=0,
                     help='profiling case for ncu: the workload subsampled to this many rows, --warmup + --steps '
                          'untimed steps with the library defaults, no other arms')
+    ap.add_argument('--tuning', action='append', default=[], metavar='KEY=VALUE',
+                    help='profiling case only: a kernel-variant setting (arlgpu_set_tuning) to profile instead of '
+                         'the default, e.g. degrid_kernel=4; repeatable')
     ap.add_argument('--wstack-profile', action='store_true',
                     help='profiling case for ncu: a 2,000,000-row PSWF w-stack invert onto 4 slices of 4096^2 '
                          '(FP32C, 2.3 GB on the device), run --warmup + --steps times, no other arms')
@@ -1040,12 +1043,15 @@ def arm_reference(args, torch, world, rank):
 def profile_case(args, torch):
     """Small untimed case for ncu captures (one GPU): warmup + steps plan /
     grid / degrid calls on a row subsample, with the library's default
-    kernel variants."""
+    kernel variants or those that --tuning names."""
     arl = importlib.import_module('algorithm-reference-library_gb300')
     sim = importlib.import_module('algorithm-reference-library_gb300.simulation')
     device = torch.device('cuda', 0)
     w = sim.make_workload(args.workload, max_rows=args.profile_rows, device=device)
     w['name'] = args.workload
+    for kv in args.tuning:
+        key, val = kv.split('=', 1)
+        arl.tune.set_tuning(**{key: int(val)})
     ctx = build_context(arl, torch, w, 'fp32c', device)
     st = torch.cuda.current_stream()
     for _ in range(args.warmup + args.steps):
