@@ -10,7 +10,11 @@ Tolerances are max-norm error over max-norm of the reference result:
     white FP32 rounding noise of complex64 taps and grid cells (which, unlike
     the signal, is not tapered): relative to the image peak the error there is
     ~1e-8 x gcf for a noise-like sky, so no FP32 kernel stays within 1e-5 at
-    the edge.
+    the edge.  Measured on the GPU (largest whole-image errors of the suite):
+    2e-4 to 7.4e-4 on 128^2 .. 256^2 test images, 3e-6 to 9e-6 on the
+    1024^2 .. 8192^2 workloads; test_fp32c_edge_error_is_storage_rounding
+    shows that complex64 taps alone, or a complex64 grid alone, give the same
+    edge error to the FP64 path.
 """
 import numpy
 

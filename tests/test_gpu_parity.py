@@ -132,6 +132,43 @@ def test_golden_2d_pswf(arl, golden, precision):
     assert rel(pv.vis, d['predict']) < tolf
 
 
+def test_fp32c_edge_error_is_storage_rounding(arl, golden):
+    """Where the whole-image FP32C error comes from, on the golden 2-D PSWF
+    case (128^2, grid correction up to 6.2e4 at the corners): the FP64 path
+    given the same taps rounded to complex64, or its own grid rounded to
+    complex64 before the transform, shows the same edge error as the FP32C
+    path (each ~2e-4 of the image peak), while rounding the visibilities and
+    weights to FP32 costs ~4e-8.  So the edge error is the FP32 storage of the
+    kernel table and of the grid cells, amplified by the grid correction; the
+    gridder's arithmetic and the double-single transform add nothing
+    visible, and no FP32-storage path meets 1e-5 over the whole field."""
+    from helpers import image_errors
+    d = golden('ref_2d_pswf.npz')
+    im = make_image(arl, int(d['N']), float(d['cell']), [1e8], 1e6)
+    gcf, cf = arl.create_pswf_convolutionfunction(im, oversampling=int(d['O']), support=int(d['S']))
+
+    def image(vis, wt, cfx, grid_prec, round_grid=False):
+        gd = arl.create_griddata_from_image(im)
+        gd, _ = arl.grid_visibility_to_griddata(make_vis(arl, d['uvw'], d['frequency'], vis, wt), gd, cfx,
+                                                precision=grid_prec)
+        g = numpy.asarray(gd.data)
+        gd.data = (g.astype(numpy.complex64) if round_grid else g).astype(numpy.complex128)
+        re = arl.fft_griddata_to_image(gd, gcf, precision='fp64' if grid_prec == 'fp64' else 'fp32c')
+        return image_errors(re.data, d['img_re'], d['gcf'])
+
+    e32, i32 = image(d['vis'], d['wt'], cf, 'fp32c')
+    cf32 = arl.create_pswf_convolutionfunction(im, oversampling=int(d['O']), support=int(d['S']))[1]
+    cf32.data = cf.data.astype(numpy.complex64).astype(numpy.complex128)
+    e_taps, _ = image(d['vis'], d['wt'], cf32, 'fp64')
+    e_grid, _ = image(d['vis'], d['wt'], cf, 'fp64', round_grid=True)
+    e_vis, _ = image(d['vis'].astype(numpy.complex64).astype(numpy.complex128),
+                     d['wt'].astype(numpy.float32).astype(numpy.float64), cf, 'fp64')
+    assert i32 < 1e-5
+    assert e_vis < 1e-6
+    assert min(e_taps, e_grid) > 1e-5
+    assert e32 < 3.0 * max(e_taps, e_grid), (e32, e_taps, e_grid)
+
+
 @pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
 def test_golden_wproj_2chan_2pol(arl, golden, precision):
     d = golden('ref_wproj_2chan_2pol.npz')
