@@ -335,15 +335,41 @@ def invert_list_serial_workflow(vis_list, template_model_imagelist, dopsf=False,
     for i, vis in enumerate(vis_list):
         g = gcfcf[i] if len(gcfcf) > 1 else gcfcf[0]
         im = template_model_imagelist[i]
-        if context == 'wstack':
-            if not normalize:
-                raise NotImplementedError('the serial w-stack workflow with normalize=False weights unnormalised '
-                                          'slice images by their sumwt; only normalize=True is on the GB300 path')
+        if context == 'wstack' and normalize:
             out.append(invert_wstack(vis, im, vis_slices, dopsf=dopsf, normalize=True, gcfcf=g,
                                      precision=precision))
+        elif context == 'wstack':
+            out.append(_invert_wstack_slices_unnormalised(vis, im, vis_slices, dopsf, g, precision))
         else:
             out.append(invert_2d(vis, im, dopsf=dopsf, normalize=normalize, gcfcf=g, precision=precision))
     return out
+
+
+def _invert_wstack_slices_unnormalised(vis, im, vis_slices, dopsf, gcfcf, precision):
+    """The serial w-stack workflow with normalize=False (``imaging_serial.py:186-197``):
+    each slice's rows are inverted without normalisation
+    (``invert_wstack_single``), the slice image is weighted by the slice's own
+    sumwt, and the sum is divided by the total sumwt.  Slices without rows
+    contribute nothing, as ``create_visibility_from_rows`` returns None for
+    them.  One GPU invert per slice; the weighted sum stays on the device
+    (FP64) and comes back once."""
+    if not isinstance(vis, Visibility):
+        raise NotImplementedError('the unnormalised w-stack workflow takes a host Visibility')
+    device = dv.require_cuda()
+    nchan, npol = im.shape[:2]
+    acc = torch.zeros(im.shape, dtype=torch.float64, device=device)
+    total = torch.zeros((nchan, npol), dtype=torch.float64, device=device)
+    for rows in vis_wslice_iter(vis, vis_slices):
+        row_vis = create_visibility_from_rows(vis, rows)
+        if row_vis is None:
+            continue
+        dvis = DeviceVisibility.from_visibility(row_vis, precision, device)
+        img, sw = invert_wstack_single(dvis, im, dopsf, normalize=False, gcfcf=gcfcf, precision=precision)
+        acc += sw[:, :, None, None] * img.data
+        total += sw
+    acc = torch.where(total[:, :, None, None] > 0, acc / torch.where(total > 0, total, 1.0)[:, :, None, None],
+                      torch.zeros_like(acc))
+    return Image(acc.cpu().numpy(), im.wcs.deepcopy(), im.polarisation_frame), total.cpu().numpy()
 
 
 def predict_list_serial_workflow(vis_list, model_imagelist, context, vis_slices=1, facets=1, gcfcf=None,

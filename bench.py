@@ -359,6 +359,81 @@ def e2e_steps(arl, torch, ctx, steps, warmup):
     return e0.elapsed_time(e1) / steps, h2d, d2h
 
 
+def e2e_pipelined(arl, torch, ctx, steps, warmup):
+    """A stream of steps through the C ABI from pinned host buffers, as a
+    caller gridding one batch of rows after another would run it: every step
+    uploads its uvw, frequency, vis and weight and reads back its grid and
+    degridded vis, but the inputs and outputs are double-buffered on the
+    device, so step k + 1's uploads (one copy stream) and step k's read-backs
+    (another) run while the compute stream plans, grids and degrids.  An
+    input set is reused once the gridder of the step before last has read it,
+    an output set once its read-back is done.  Returns ms per step over the
+    timed steps (first upload to last read-back)."""
+    nat = arl._native
+    lib = nat.load()
+    host = {k: ctx[k].cpu().pin_memory() for k in ('uvw', 'freq', 'vis', 'wt')}
+    gh = torch.empty(ctx['grid'].shape, dtype=ctx['grid'].dtype).pin_memory()
+    oh = torch.empty(ctx['out'].shape, dtype=ctx['out'].dtype).pin_memory()
+    sets = [{k: ctx[k] for k in ('uvw', 'freq', 'vis', 'wt', 'grid', 'out', 'sumwt')},
+            {k: torch.empty_like(ctx[k]) for k in ('uvw', 'freq', 'vis', 'wt', 'grid', 'out', 'sumwt')}]
+    comp = torch.cuda.current_stream()
+    dev = ctx['uvw'].device
+    up, down = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    P = nat.PRECISIONS[ctx['precision']]
+    gd, cd, ws = ctx['gd'], ctx['cd'], ctx['ws']
+    sp = ctypes.c_void_p(comp.cuda_stream)
+    inputs_free = [None, None]   # event: the gridder that last read the set has run
+    outputs_free = [None, None]  # event: the set's last read-back is done
+
+    def one(k):
+        b = sets[k % 2]
+        with torch.cuda.stream(up):
+            if inputs_free[k % 2] is not None:
+                up.wait_event(inputs_free[k % 2])
+            b['uvw'].copy_(host['uvw'], non_blocking=True)
+            b['freq'].copy_(host['freq'], non_blocking=True)
+            plan_in = up.record_event()
+            b['vis'].copy_(host['vis'], non_blocking=True)
+            b['wt'].copy_(host['wt'], non_blocking=True)
+            rows_in = up.record_event()
+        comp.wait_event(plan_in)
+        nat.check(lib.arlgpu_plan_build(nat.ptr(b['uvw']), nat.ptr(b['freq']), ctx['n'], ctypes.byref(gd),
+                                        ctypes.byref(cd), nat.ptr(ws), ws.numel(), nat.ptr(ctx['nbad']), sp))
+        comp.wait_event(rows_in)
+        if outputs_free[k % 2] is not None:
+            comp.wait_event(outputs_free[k % 2])
+        nat.check(lib.arlgpu_grid_planned(nat.ptr(b['vis']), nat.ptr(b['wt']), ctx['n'], P, nat.ptr(ctx['cf_t']),
+                                          ctypes.byref(cd), nat.ptr(b['grid']), ctypes.byref(gd),
+                                          nat.ptr(b['sumwt']), nat.ptr(ws), ws.numel(), sp))
+        gridded = comp.record_event()
+        inputs_free[k % 2] = gridded
+        nat.check(lib.arlgpu_degrid_planned(ctx['n'], P, nat.ptr(ctx['cf_t']), ctypes.byref(cd),
+                                            nat.ptr(b['grid']), ctypes.byref(gd), nat.ptr(b['out']),
+                                            nat.ptr(ws), ws.numel(), sp))
+        degridded = comp.record_event()
+        with torch.cuda.stream(down):
+            down.wait_event(gridded)
+            gh.copy_(b['grid'], non_blocking=True)
+            down.wait_event(degridded)
+            oh.copy_(b['out'], non_blocking=True)
+            outputs_free[k % 2] = down.record_event()
+
+    for k in range(warmup):
+        one(k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(comp)
+    up.wait_stream(comp)
+    for k in range(warmup, warmup + steps):
+        one(k)
+    comp.wait_stream(down)
+    e1.record(comp)
+    torch.cuda.synchronize()
+    # the last step's results are the same rows' results as a lone step's
+    assert int(ctx['nbad'].item()) == 0
+    return e0.elapsed_time(e1) / steps
+
+
 def _events(torch, n):
     return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
 
@@ -447,7 +522,23 @@ def gradient_step_rate(arl, torch, device, steps, warmup, flush):
         ev[k][1].record(stream)
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in ev) / steps
-    return {'value': n / (ms / 1e3), 'unit': 'vis/s', 'ms': ms,
+    # Error of the timed FP32C step against the same step in complex128 (FP64
+    # operator, FP64 inputs), after the timing.
+    c32, gx32, gg32 = arl.autograd.gain_chi2_step(x, gains, vobs, op, a1, a2)
+    dvis64 = arl.DeviceVisibility(dvis.uvw, dvis.frequency, torch.zeros((n, 1), dtype=torch.complex128, device=device),
+                                  torch.ones((n, 1), dtype=torch.float64, device=device))
+    op64 = arl.autograd.GriddingOperator(dvis64, im, gcfcf, precision='fp64')
+    c64, gx64, gg64 = arl.autograd.gain_chi2_step(x.double(), gains.to(torch.complex128), vobs.to(torch.complex128),
+                                                  op64, a1, a2)
+
+    def err(a, b):
+        d = (a.to(b.dtype) - b).abs()
+        return {'max_rel': float(d.max() / b.abs().max()),
+                'rms_rel': float(d.pow(2).mean().sqrt() / b.abs().pow(2).mean().sqrt())}
+    errs = {'chi2_rel': float(abs(float(c32) - float(c64)) / abs(float(c64))), 'image_gradient': err(gx32, gx64),
+            'gain_gradient': err(gg32, gg64), 'against': 'the same step through the FP64 (complex128) operator'}
+    del op64, dvis64
+    return {'value': n / (ms / 1e3), 'unit': 'vis/s', 'ms': ms, 'err_vs_fp64': errs,
             'workload': 'C4 gain solve: 128 antennas / 2 km disk, 8 chan 100-120 MHz summed, 240 times, 2048^2, '
                         'PSWF S=8 O=8, %d rows; chi^2 + image and gain gradients, FP32C' % n}
 
@@ -675,7 +766,8 @@ def arm_gb300(args, torch, world, rank, local):
         del ctx64
         torch.cuda.empty_cache()
 
-    e2e_ms, h2d, d2h = e2e_steps(arl, torch, ctx, max(3, args.steps // 2), 2)
+    e2e_seq_ms, h2d, d2h = e2e_steps(arl, torch, ctx, max(3, args.steps // 2), 2)
+    e2e_ms = e2e_pipelined(arl, torch, ctx, max(3, args.steps), 2)
     stages = None
     if not args.no_stages:
         stages = {'grid': {'value': n / (r['grid_ms'] / 1e3), 'unit': 'vis/s', 'ms': r['grid_ms']},
@@ -683,6 +775,7 @@ def arm_gb300(args, torch, world, rank, local):
         stages.update(stage_rates(arl, torch, ctx, max(3, args.steps // 2), 2, flush))
         stages['gradient_step'] = gradient_step_rate(arl, torch, device, 3, 2, flush)
     e2e_ms = max_over_ranks(torch, world, e2e_ms)
+    e2e_seq_ms = max_over_ranks(torch, world, e2e_seq_ms)
 
     # Roofline of the dominant kernel (grid or degrid launch), HBM-bound, with
     # the algorithmic bytes of the gridding / degridding stage: each row's uvw
@@ -720,7 +813,12 @@ def arm_gb300(args, torch, world, rank, local):
                           'frac': step_alg / (ms / 1e3) / 1e9 / peak},
         'e2e': {'value': world * n / (e2e_ms / 1e3), 'unit': 'vis/s', 'h2d_bytes_per_step': h2d,
                 'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_ms, 'path': 'C ABI, pinned host buffers',
-                'overlap': 'uvw H2D first, then vis and weight H2D under the plan; grid D2H under the degrid (second stream)'},
+                'overlap': 'a stream of steps: inputs and outputs double-buffered on the device, step k+1 uploads '
+                           '(copy stream) and step k read-backs (second copy stream) under step k plan / grid / '
+                           'degrid; every step copies all its inputs up and its grid and vis down',
+                'sequential': {'value': world * n / (e2e_seq_ms / 1e3), 'ms_per_step': e2e_seq_ms,
+                               'overlap': 'one step at a time: uvw H2D first, then vis and weight H2D under the '
+                                          'plan; grid D2H under the degrid (second stream)'}},
         'gpu_launches': r['launches'],
         'stages': stages,
         'clocks': clk,

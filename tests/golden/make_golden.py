@@ -185,10 +185,14 @@ def case_wstack(out):
         model[0, 0, rng.integers(N // 4, 3 * N // 4), rng.integers(N // 4, 3 * N // 4)] = rng.uniform(0.5, 3)
     mim = create_image_from_array(model, im.wcs, im.polarisation_frame)
     (pvis,) = predict_list_serial_workflow([vis], [mim], context='wstack', vis_slices=K, gcfcf=[gcfcf])
+    # normalize=False: each slice's unnormalised image, weighted by the
+    # slice's sumwt, summed and divided by the total (imaging_serial.py:186-197)
+    (dirty_nn, sumwt_nn), = invert_list_serial_workflow([vis], [im], context='wstack', vis_slices=K,
+                                                        normalize=False, gcfcf=[gcfcf])
     numpy.savez_compressed(out, N=N, cell=cell, O=O, S=S, K=K, freq0=1e8, dfreq=1e6,
                            uvw=vis.uvw, frequency=vis.frequency, vis=vis.vis, wt=vis.imaging_weight,
                            cf=gcfcf[1].data, gcf=gcfcf[0].data, dirty=dirty.data, sumwt=sumwt,
-                           model=model, predict=pvis.vis)
+                           model=model, predict=pvis.vis, dirty_nonorm=dirty_nn.data, sumwt_nonorm=sumwt_nn)
 
 
 def case_kernels(out):

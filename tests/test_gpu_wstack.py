@@ -45,6 +45,21 @@ def test_wstack_workflow_matches_reference(arl, golden, precision):
 
 
 @pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
+def test_wstack_workflow_unnormalised_matches_reference(arl, golden, precision):
+    """invert_list_serial_workflow(context='wstack', normalize=False): the
+    reference's own result (slice images unnormalised, weighted by each
+    slice's sumwt, divided by the total)."""
+    d = golden('ref_wstack.npz')
+    im, gcf, cf, vis = _case(arl, d)
+    K = int(d['K'])
+    (dirty, sumwt), = arl.imaging.invert_list_serial_workflow([vis], [im], context='wstack', vis_slices=K,
+                                                               normalize=False, gcfcf=[(gcf, cf)],
+                                                               precision=precision)
+    assert_image(dirty.data, d['dirty_nonorm'], d['gcf'], precision)
+    assert numpy.allclose(sumwt, d['sumwt_nonorm'], rtol=1e-12 if precision == 'fp64' else 1e-6)
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
 def test_wstack_single_matches_oracle(arl, oracle, golden, precision):
     d = golden('ref_wstack.npz')
     im, gcf, cf, vis = _case(arl, d)
