@@ -363,75 +363,95 @@ def e2e_pipelined(arl, torch, ctx, steps, warmup):
     """A stream of steps through the C ABI from pinned host buffers, as a
     caller gridding one batch of rows after another would run it: every step
     uploads its uvw, frequency, vis and weight and reads back its grid and
-    degridded vis, but the inputs and outputs are double-buffered on the
-    device, so step k + 1's uploads (one copy stream) and step k's read-backs
-    (another) run while the compute stream plans, grids and degrids.  An
-    input set is reused once the gridder of the step before last has read it,
-    an output set once its read-back is done.  Returns ms per step over the
-    timed steps (first upload to last read-back)."""
+    degridded vis.  Inputs, outputs and plan workspace are double-buffered on
+    the device; consecutive steps run on two compute streams (independent
+    batches, so step k + 1's plan and grid can share the SMs with step k's
+    degrid), step k + 1's uploads run on one copy stream and step k's
+    read-backs on another.  An input set is reused once the gridder of the
+    step before last has read it, an output set once its read-back is done.
+    Returns (ms per step over the timed steps, first upload to last
+    read-back; ms per step of the same two-stream compute with the inputs
+    resident and no copies)."""
     nat = arl._native
     lib = nat.load()
     host = {k: ctx[k].cpu().pin_memory() for k in ('uvw', 'freq', 'vis', 'wt')}
     gh = torch.empty(ctx['grid'].shape, dtype=ctx['grid'].dtype).pin_memory()
     oh = torch.empty(ctx['out'].shape, dtype=ctx['out'].dtype).pin_memory()
-    sets = [{k: ctx[k] for k in ('uvw', 'freq', 'vis', 'wt', 'grid', 'out', 'sumwt')},
-            {k: torch.empty_like(ctx[k]) for k in ('uvw', 'freq', 'vis', 'wt', 'grid', 'out', 'sumwt')}]
-    comp = torch.cuda.current_stream()
+    keys = ('uvw', 'freq', 'vis', 'wt', 'grid', 'out', 'sumwt', 'ws', 'nbad')
+    sets = [{k: ctx[k] for k in keys}, {k: torch.empty_like(ctx[k]) for k in keys}]
+    sets[1]['nbad'].zero_()
+    cur = torch.cuda.current_stream()
     dev = ctx['uvw'].device
+    comp = [torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)]
     up, down = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
     P = nat.PRECISIONS[ctx['precision']]
-    gd, cd, ws = ctx['gd'], ctx['cd'], ctx['ws']
-    sp = ctypes.c_void_p(comp.cuda_stream)
+    gd, cd = ctx['gd'], ctx['cd']
     inputs_free = [None, None]   # event: the gridder that last read the set has run
     outputs_free = [None, None]  # event: the set's last read-back is done
 
+    def compute(b, st, plan_in=None, rows_in=None, free=None):
+        sp = ctypes.c_void_p(st.cuda_stream)
+        if plan_in is not None:
+            st.wait_event(plan_in)
+        nat.check(lib.arlgpu_plan_build(nat.ptr(b['uvw']), nat.ptr(b['freq']), ctx['n'], ctypes.byref(gd),
+                                        ctypes.byref(cd), nat.ptr(b['ws']), b['ws'].numel(), nat.ptr(b['nbad']), sp))
+        if rows_in is not None:
+            st.wait_event(rows_in)
+        if free is not None:
+            st.wait_event(free)
+        nat.check(lib.arlgpu_grid_planned(nat.ptr(b['vis']), nat.ptr(b['wt']), ctx['n'], P, nat.ptr(ctx['cf_t']),
+                                          ctypes.byref(cd), nat.ptr(b['grid']), ctypes.byref(gd),
+                                          nat.ptr(b['sumwt']), nat.ptr(b['ws']), b['ws'].numel(), sp))
+        gridded = st.record_event()
+        nat.check(lib.arlgpu_degrid_planned(ctx['n'], P, nat.ptr(ctx['cf_t']), ctypes.byref(cd),
+                                            nat.ptr(b['grid']), ctypes.byref(gd), nat.ptr(b['out']),
+                                            nat.ptr(b['ws']), b['ws'].numel(), sp))
+        return gridded, st.record_event()
+
     def one(k):
-        b = sets[k % 2]
+        s = k % 2
+        b = sets[s]
         with torch.cuda.stream(up):
-            if inputs_free[k % 2] is not None:
-                up.wait_event(inputs_free[k % 2])
+            if inputs_free[s] is not None:
+                up.wait_event(inputs_free[s])
             b['uvw'].copy_(host['uvw'], non_blocking=True)
             b['freq'].copy_(host['freq'], non_blocking=True)
             plan_in = up.record_event()
             b['vis'].copy_(host['vis'], non_blocking=True)
             b['wt'].copy_(host['wt'], non_blocking=True)
             rows_in = up.record_event()
-        comp.wait_event(plan_in)
-        nat.check(lib.arlgpu_plan_build(nat.ptr(b['uvw']), nat.ptr(b['freq']), ctx['n'], ctypes.byref(gd),
-                                        ctypes.byref(cd), nat.ptr(ws), ws.numel(), nat.ptr(ctx['nbad']), sp))
-        comp.wait_event(rows_in)
-        if outputs_free[k % 2] is not None:
-            comp.wait_event(outputs_free[k % 2])
-        nat.check(lib.arlgpu_grid_planned(nat.ptr(b['vis']), nat.ptr(b['wt']), ctx['n'], P, nat.ptr(ctx['cf_t']),
-                                          ctypes.byref(cd), nat.ptr(b['grid']), ctypes.byref(gd),
-                                          nat.ptr(b['sumwt']), nat.ptr(ws), ws.numel(), sp))
-        gridded = comp.record_event()
-        inputs_free[k % 2] = gridded
-        nat.check(lib.arlgpu_degrid_planned(ctx['n'], P, nat.ptr(ctx['cf_t']), ctypes.byref(cd),
-                                            nat.ptr(b['grid']), ctypes.byref(gd), nat.ptr(b['out']),
-                                            nat.ptr(ws), ws.numel(), sp))
-        degridded = comp.record_event()
+        gridded, degridded = compute(b, comp[s], plan_in, rows_in, outputs_free[s])
+        inputs_free[s] = gridded
         with torch.cuda.stream(down):
             down.wait_event(gridded)
             gh.copy_(b['grid'], non_blocking=True)
             down.wait_event(degridded)
             oh.copy_(b['out'], non_blocking=True)
-            outputs_free[k % 2] = down.record_event()
+            outputs_free[s] = down.record_event()
+
+    def timed(fn, nsteps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(cur)
+        for st in comp + [up, down]:
+            st.wait_stream(cur)
+        fn(nsteps)
+        for st in comp + [up, down]:
+            cur.wait_stream(st)
+        e1.record(cur)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / nsteps
 
     for k in range(warmup):
         one(k)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(comp)
-    up.wait_stream(comp)
-    for k in range(warmup, warmup + steps):
-        one(k)
-    comp.wait_stream(down)
-    e1.record(comp)
-    torch.cuda.synchronize()
-    # the last step's results are the same rows' results as a lone step's
-    assert int(ctx['nbad'].item()) == 0
-    return e0.elapsed_time(e1) / steps
+    ms = timed(lambda m: [one(k) for k in range(warmup, warmup + m)], steps)
+    assert int(sets[0]['nbad'].item()) == 0 and int(sets[1]['nbad'].item()) == 0
+
+    def resident(m):
+        for k in range(m):
+            compute(sets[k % 2], comp[k % 2])
+    ms_resident = timed(resident, steps)
+    return ms, ms_resident
 
 
 def _events(torch, n):
@@ -767,7 +787,7 @@ def arm_gb300(args, torch, world, rank, local):
         torch.cuda.empty_cache()
 
     e2e_seq_ms, h2d, d2h = e2e_steps(arl, torch, ctx, max(3, args.steps // 2), 2)
-    e2e_ms = e2e_pipelined(arl, torch, ctx, max(3, args.steps), 2)
+    e2e_ms, two_stream_ms = e2e_pipelined(arl, torch, ctx, max(3, args.steps), 2)
     stages = None
     if not args.no_stages:
         stages = {'grid': {'value': n / (r['grid_ms'] / 1e3), 'unit': 'vis/s', 'ms': r['grid_ms']},
@@ -813,9 +833,13 @@ def arm_gb300(args, torch, world, rank, local):
                           'frac': step_alg / (ms / 1e3) / 1e9 / peak},
         'e2e': {'value': world * n / (e2e_ms / 1e3), 'unit': 'vis/s', 'h2d_bytes_per_step': h2d,
                 'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_ms, 'path': 'C ABI, pinned host buffers',
-                'overlap': 'a stream of steps: inputs and outputs double-buffered on the device, step k+1 uploads '
-                           '(copy stream) and step k read-backs (second copy stream) under step k plan / grid / '
-                           'degrid; every step copies all its inputs up and its grid and vis down',
+                'overlap': 'a stream of steps: inputs, outputs and plan workspace double-buffered on the device, '
+                           'consecutive steps on two compute streams, step k+1 uploads (copy stream) and step k '
+                           'read-backs (second copy stream) under the compute; every step copies all its inputs '
+                           'up and its grid and vis down',
+                'two_stream_resident': {'value': world * n / (two_stream_ms / 1e3), 'ms_per_step': two_stream_ms,
+                                        'what': 'the same two-stream compute with inputs resident and no copies '
+                                                '(value above is one step at a time)'},
                 'sequential': {'value': world * n / (e2e_seq_ms / 1e3), 'ms_per_step': e2e_seq_ms,
                                'overlap': 'one step at a time: uvw H2D first, then vis and weight H2D under the '
                                           'plan; grid D2H under the degrid (second stream)'}},
