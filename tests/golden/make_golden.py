@@ -446,6 +446,65 @@ def case_rowops(out):
     numpy.savez_compressed(out, **res)
 
 
+# Public functions of the path: (reference module, name).  Their signatures
+# are recorded so the package's functions can be checked against them.
+API = [
+    ('processing_components.griddata.gridding', n) for n in (
+        'convolution_mapping', 'grid_visibility_to_griddata', 'degrid_visibility_from_griddata',
+        'fft_griddata_to_image', 'fft_image_to_griddata', 'grid_weight_to_griddata', 'griddata_merge_weights',
+        'griddata_reweight')] + [
+    ('processing_components.griddata.kernels', 'create_pswf_convolutionfunction'),
+    ('processing_components.griddata.kernels', 'create_awterm_convolutionfunction'),
+    ('processing_components.griddata.convolution_functions', 'calculate_bounding_box_convolutionfunction'),
+    ('processing_components.griddata.convolution_functions', 'apply_bounding_box_convolutionfunction'),
+    ('processing_components.griddata.operations', 'create_griddata_from_image'),
+    ('processing_components.imaging.base', 'invert_2d'),
+    ('processing_components.imaging.base', 'predict_2d'),
+    ('processing_components.imaging.base', 'shift_vis_to_image'),
+    ('processing_components.imaging.base', 'normalize_sumwt'),
+    ('processing_components.imaging.base', 'predict_skycomponent_visibility'),
+    ('processing_components.imaging.wstack_single', 'invert_wstack_single'),
+    ('processing_components.imaging.wstack_single', 'predict_wstack_single'),
+    ('processing_components.visibility.base', 'phaserotate_visibility'),
+    ('processing_components.visibility.iterators', 'vis_wslice_iter'),
+    ('processing_components.visibility.iterators', 'vis_null_iter'),
+    ('processing_components.calibration.operations', 'apply_gaintable'),
+    ('processing_components.visibility.coalesce', 'convert_blockvisibility_to_visibility'),
+    ('processing_components.visibility.coalesce', 'convert_visibility_to_blockvisibility'),
+    ('processing_components.image.deconvolution', 'deconvolve_cube'),
+    ('processing_library.arrays.cleaners', 'hogbom'),
+    ('processing_library.arrays.cleaners', 'msclean'),
+    ('workflows.shared.imaging.imaging_shared', 'imaging_contexts'),
+    ('workflows.shared.imaging.imaging_shared', 'imaging_context'),
+    ('workflows.serial.imaging.imaging_serial', 'invert_list_serial_workflow'),
+    ('workflows.serial.imaging.imaging_serial', 'predict_list_serial_workflow'),
+]
+
+
+def case_api(out):
+    """Signatures of the path's public functions: parameter names, kinds and
+    defaults (literal defaults as values, anything else as its type name)."""
+    import importlib
+    import inspect
+    import json
+    rec = []
+    for mod, name in API:
+        fn = getattr(importlib.import_module(mod), name)
+        params = []
+        for p in inspect.signature(fn).parameters.values():
+            d = p.default
+            if d is inspect.Parameter.empty:
+                dv = None
+                has = False
+            else:
+                has = True
+                dv = d if isinstance(d, (int, float, str, bool, type(None))) else '<%s>' % type(d).__name__
+            params.append({'name': p.name, 'kind': p.kind.name, 'has_default': has, 'default': dv})
+        rec.append({'module': mod, 'name': name, 'params': params})
+    with open(out[:-4] + '.json', 'w') as f:
+        json.dump(rec, f, indent=1)
+
+
 ALL_CASES = {
     'ref_2d_pswf': case_2d_pswf,
     'ref_wproj_2chan_2pol': case_wproj_2chan_2pol,
@@ -456,6 +515,7 @@ ALL_CASES = {
     'ref_hogbom': case_hogbom,
     'ref_msclean': case_msclean,
     'ref_rowops': case_rowops,
+    'ref_api': case_api,
 }
 
 if __name__ == '__main__':
@@ -463,4 +523,5 @@ if __name__ == '__main__':
     for name, fn in ALL_CASES.items():
         if not CASES or name in CASES:
             fn(os.path.join(OUT, name + '.npz'))
-            print(name, os.path.getsize(os.path.join(OUT, name + '.npz')))
+            made = [f for f in (name + '.npz', name + '.json') if os.path.exists(os.path.join(OUT, f))]
+            print(name, [(f, os.path.getsize(os.path.join(OUT, f))) for f in made])
