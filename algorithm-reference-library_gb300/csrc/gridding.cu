@@ -59,6 +59,7 @@ static std::atomic<int> g_tune_dsfft{1};          // FP32C inverse transforms: 1
 static std::atomic<int> g_tune_small_rows{2};     // rows per warp in the FP32C gridder when S <= 8
 static std::atomic<int> g_tune_small_rows_dg{4};  // rows per warp in the packed degridder when S <= 8
 static std::atomic<int> g_tune_lanes{0};          // lanes per row for every segment (0: by support)
+static std::atomic<int> g_tune_gather{1};         // FP32C gridder, one polarisation: rows copied into bin order first
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 bool tune_dsfft() { return g_tune_dsfft.load() != 0; }
 
@@ -387,7 +388,7 @@ struct SegBox {
   float vmax;
 };
 
-template <int NW, int NPOL, bool VMAX>
+template <int NW, int NPOL, bool VMAX, bool SORTED = false>
 __device__ __forceinline__ SegBox seg_box(const SegInfo &sg, uint32_t pos, const RowMap *__restrict__ smap,
                                           const uint32_t *__restrict__ sidx, const float2 *__restrict__ vis,
                                           const float *__restrict__ wt, const Geom &g, int *s_red) {
@@ -402,7 +403,7 @@ __device__ __forceinline__ SegBox seg_box(const SegInfo &sg, uint32_t pos, const
     y0 = min(y0, ly);
     y1 = max(y1, ly + sz);
     if (VMAX) {
-      const uint32_t idx = sidx[r];
+      const uint32_t idx = SORTED ? r : sidx[r];  // SORTED: vis / wt already in bin order
 #pragma unroll
       for (int p = 0; p < NPOL; ++p) {
         const float2 v = vis[(size_t)idx * NPOL + p];
@@ -1205,6 +1206,23 @@ k_grid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict_
   }
 }
 
+// Bin-order copies of one-polarisation rows' vis and weight for the FP32C
+// gridder.  They go into the plan's mapping scratch (the per-row keys and
+// RowMaps k_map writes for k_scatter), which is dead once the plan is built,
+// so the gridder reads vis and weight contiguously by sorted position instead
+// of gathering them through the sort index inside its row loop.  Copies, not
+// products: the gridder forms vis * weight exactly as before.
+__global__ void k_gather_rows(const uint32_t *__restrict__ sidx, const uint32_t *__restrict__ off, uint32_t nbins,
+                              const float2 *__restrict__ vis, const float *__restrict__ wt,
+                              float2 *__restrict__ vis_s, float *__restrict__ wt_s) {
+  const uint32_t nvalid = off[nbins];
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nvalid; r += gridDim.x * blockDim.x) {
+    const uint32_t i = sidx[r];
+    vis_s[r] = vis[i];
+    wt_s[r] = wt[i];
+  }
+}
+
 // K3 (fixed-point variant, FP32C only; grid_kernel 4 and 5).
 //
 // Each staged segment (the rows of one bin inside one chunk) is accumulated in
@@ -1252,7 +1270,7 @@ __device__ __forceinline__ void fx_add(int *q, int *r, float x, float scale, flo
   }
 }
 
-template <int NPOL, int NW, bool RESID, int LPR = 0, int SGC = 0>
+template <int NPOL, int NW, bool RESID, int LPR = 0, int SGC = 0, bool SORTED = false>
 __global__ void __launch_bounds__(NW * 32)
 k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
           const uint32_t *__restrict__ off, uint32_t chunk, const float2 *__restrict__ vis,
@@ -1292,7 +1310,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
     if (threadIdx.x == 0) s_next[parity] = pos;  // published by the barrier in seg_box
     uint32_t *next_row = &s_next[parity];
-    const SegBox box = seg_box<NW, NPOL, true>(sg, pos, smap, sidx, vis, wt, g, s_red[parity]);
+    const SegBox box = seg_box<NW, NPOL, true, SORTED>(sg, pos, smap, sidx, vis, wt, g, s_red[parity]);
     parity ^= 1;
     const uint32_t rows = sg.end - pos;
     const bool direct = seg_direct(box, rows);
@@ -1339,7 +1357,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       uint32_t inext = 0;
       if (rbase + half < sg.end) {
         mnext = smap[rbase + half];
-        inext = sidx[rbase + half];
+        inext = SORTED ? rbase + half : sidx[rbase + half];
       }
       while (rbase < sg.end) {
         const RowMap m = mnext;
@@ -1350,7 +1368,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         rn = __shfl_sync(0xffffffffu, rn, 0);
         if (rn + half < sg.end) {
           mnext = smap[rn + half];
-          inext = sidx[rn + half];
+          inext = SORTED ? rn + half : sidx[rn + half];
         }
         rbase = rn;
         if (!act) continue;
@@ -2458,20 +2476,27 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
   // compile-time-edge instantiation; other edges (autotuner trials) the
   // runtime-edge one, with lanes per row chosen per segment.
   const bool csg = g.SG == (g.npol == 4 ? 32 : 48);
+  // One polarisation: vis and weight copied into bin order first (into the
+  // plan's dead mapping scratch: 8 + 4 bytes per row against its 20) and
+  // read by sorted position (the SORTED instantiations).
+  const bool sorted = g.npol == 1 && g_tune_gather.load() != 0;
   auto pick = [&](auto resid_c) {
     constexpr bool RS = decltype(resid_c)::value;
-    auto by_lpr = [&](auto npol_c, auto sg_c) {
+    auto by_lpr = [&](auto npol_c, auto sg_c, auto sorted_c) {
       constexpr int NP = decltype(npol_c)::value, SGV = decltype(sg_c)::value;
-      return lpr == 8 ? k_grid_fx<NP, kWarps, RS, 8, SGV>
-                      : lpr == 16 ? k_grid_fx<NP, kWarps, RS, 16, SGV>
-                                  : lpr == 32 ? k_grid_fx<NP, kWarps, RS, 32, SGV> : k_grid_fx<NP, kWarps, RS, 0, SGV>;
+      constexpr bool SO = decltype(sorted_c)::value;
+      return lpr == 8 ? k_grid_fx<NP, kWarps, RS, 8, SGV, SO>
+                      : lpr == 16 ? k_grid_fx<NP, kWarps, RS, 16, SGV, SO>
+                                  : lpr == 32 ? k_grid_fx<NP, kWarps, RS, 32, SGV, SO>
+                                              : k_grid_fx<NP, kWarps, RS, 0, SGV, SO>;
     };
     if (csg) {
-      if (g.npol == 4) return by_lpr(IntC<4>(), IntC<32>());
-      if (g.npol == 2) return by_lpr(IntC<2>(), IntC<48>());
-      return by_lpr(IntC<1>(), IntC<48>());
+      if (g.npol == 4) return by_lpr(IntC<4>(), IntC<32>(), BoolC<false>());
+      if (g.npol == 2) return by_lpr(IntC<2>(), IntC<48>(), BoolC<false>());
+      return sorted ? by_lpr(IntC<1>(), IntC<48>(), BoolC<true>()) : by_lpr(IntC<1>(), IntC<48>(), BoolC<false>());
     }
-    return g.npol == 1 ? k_grid_fx<1, kWarps, RS> : g.npol == 2 ? k_grid_fx<2, kWarps, RS> : k_grid_fx<4, kWarps, RS>;
+    if (g.npol == 1) return sorted ? k_grid_fx<1, kWarps, RS, 0, 0, true> : k_grid_fx<1, kWarps, RS>;
+    return g.npol == 2 ? k_grid_fx<2, kWarps, RS> : k_grid_fx<4, kWarps, RS>;
   };
   kern = resid ? pick(BoolC<true>()) : pick(BoolC<false>());
   ARL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -2480,8 +2505,20 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
   if (blocks == 0) return ARLGPU_OK;
   uint32_t *queue = work_queue(b, 0, st);
   if (queue) ARL_CUDA(cudaMemsetAsync(queue, 0, 4, st));
-  kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk, static_cast<const float2 *>(vis),
-                                          static_cast<const float *>(wt), static_cast<const float2 *>(cf),
+  const void *vis_k = vis, *wt_k = wt;
+  if (sorted) {
+    float2 *vis_s = reinterpret_cast<float2 *>(b.maps);
+    float *wt_s = reinterpret_cast<float *>(b.keys);
+    const int gblocks = (int)std::min<int64_t>((nvis + 255) / 256, (int64_t)num_sms() * 8);
+    k_gather_rows<<<gblocks, 256, 0, st>>>(b.sidx, b.offsets, g.nbins, static_cast<const float2 *>(vis),
+                                           static_cast<const float *>(wt), vis_s, wt_s);
+    ARL_LAUNCH_CHECK();
+    count_launch(1);
+    vis_k = vis_s;
+    wt_k = wt_s;
+  }
+  kern<<<blocks, kWarps * 32, smem, st>>>(g, b.smap, b.sidx, b.offsets, chunk, static_cast<const float2 *>(vis_k),
+                                          static_cast<const float *>(wt_k), static_cast<const float2 *>(cf),
                                           static_cast<float2 *>(grid), sumwt, queue);
   ARL_LAUNCH_CHECK();
   count_launch(1);
@@ -2839,6 +2876,7 @@ extern "C" int arlgpu_set_tuning(const char *key, int value) {
   else if (k == "small_rows" && (value == 1 || value == 2 || value == 4)) g_tune_small_rows = value;
   else if (k == "small_rows_degrid" && (value == 1 || value == 2 || value == 4)) g_tune_small_rows_dg = value;
   else if (k == "lanes_per_row" && (value == 0 || value == 8 || value == 16 || value == 32)) g_tune_lanes = value;
+  else if (k == "gather_rows" && (value == 0 || value == 1)) g_tune_gather = value;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key or value: %s = %d", key, value);
   return ARLGPU_OK;
 }
@@ -2855,6 +2893,7 @@ extern "C" int arlgpu_get_tuning(const char *key, int *value) {
   else if (k == "small_rows") *value = g_tune_small_rows;
   else if (k == "small_rows_degrid") *value = g_tune_small_rows_dg;
   else if (k == "lanes_per_row") *value = g_tune_lanes;
+  else if (k == "gather_rows") *value = g_tune_gather;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key: %s", key);
   return ARLGPU_OK;
 }

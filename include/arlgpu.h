@@ -120,6 +120,10 @@ unsigned long long arlgpu_kernel_launches(void);
  *                   FP32C fixed-point gridder and packed degridder at the default subgrid edge
  *                   Otherwise both kernels choose per segment: two rows per warp when the
  *                   segment's largest support is at most 16, four (degridder) at most 8.
+ *   "gather_rows"   1 = the FP32C fixed-point gridder with one polarisation first copies the
+ *                   rows' vis and weight into bin order, into the plan workspace's mapping
+ *                   scratch, and reads them contiguously (default); 0 = it gathers them
+ *                   through the sort index in its row loop.  Either way the grid is the same.
  * No reference counterpart (ARL has one Python loop per function). */
 int arlgpu_set_tuning(const char *key, int value);
 int arlgpu_get_tuning(const char *key, int *value);
@@ -151,7 +155,10 @@ int arlgpu_grid(const double *uvw, const double *frequency, const void *vis, con
  * shared by the planned gridder and degridder (ARL recomputes the mapping in
  * each of grid_visibility_to_griddata and degrid_visibility_from_griddata,
  * gridding.py:113-114,243-244).  The plan lives in `workspace`; the planned
- * calls must be given the same nvis, gd and cd as arlgpu_plan_build. */
+ * calls must be given the same nvis, gd and cd as arlgpu_plan_build.  The
+ * planned gridder writes scratch into the workspace (bin-order row copies,
+ * work-queue words), so planned calls that share a workspace must not overlap
+ * on the GPU: order them on one stream. */
 int arlgpu_plan_build(const double *uvw, const double *frequency, int64_t nvis, const arlgpu_grid_desc *gd,
                       const arlgpu_cf_desc *cd, void *workspace, size_t workspace_bytes, int64_t *n_bad_dev,
                       void *stream);

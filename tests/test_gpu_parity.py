@@ -522,6 +522,50 @@ def test_work_queue_and_lanes_per_row_vs_oracle(arl, oracle, persistent, lanes_p
         arl.tune.set_tuning(**before)
 
 
+@pytest.mark.parametrize('gather_rows,persistent', [(0, 0), (1, 0), (1, 2)])
+def test_bin_order_rows_vs_oracle(arl, oracle, gather_rows, persistent):
+    """The FP32C gridder with one polarisation reading vis and weight from a
+    bin-order copy in the plan workspace (gather_rows 1, the default) or
+    through the sort index (0), against the oracle; a plan gridded twice and
+    then degridded, so the copy in the plan's mapping scratch must leave the
+    plan itself intact."""
+    import ctypes
+    before = arl.tune.get_tuning()
+    try:
+        arl.tune.set_tuning(gather_rows=gather_rows, persistent=persistent)
+        rng = numpy.random.default_rng(63)
+        im, cf, vis, maps, gax = _random_case(arl, oracle, rng, 128, 4e-3, 8, 12, 40000, 2, 1, 3, 20.0, True)
+        arl.set_plane_support(cf, [12, 8, 4])
+        g_ref, sw_ref = oracle.grid_vec(vis.vis, vis.imaging_weight, maps, cf.data, gax['shape'])
+        nat, dv = arl._native, arl.device
+        dev = torch.device('cuda')
+        cf_t, cs, ps, psup = dv.device_cf(cf, 'fp32c', dev)
+        cd = dv.cf_desc(cf.grid_wcs, cf.data.shape, cs, ps, psup, table=cf_t)
+        gd = dv.grid_desc(arl.create_griddata_from_image(im).grid_wcs, g_ref.shape)
+        n = vis.nvis
+        uvw = torch.as_tensor(vis.uvw, device=dev)
+        f = torch.as_tensor(vis.frequency, device=dev)
+        v = torch.as_tensor(vis.vis, device=dev).to(torch.complex64)
+        w = torch.as_tensor(vis.imaging_weight, device=dev).to(torch.float32)
+        ws = torch.empty(dv.plan_bytes(n, gd, cd), dtype=torch.uint8, device=dev)
+        grid = torch.empty(g_ref.shape, dtype=torch.complex64, device=dev)
+        sumwt = torch.empty(sw_ref.shape, dtype=torch.float64, device=dev)
+        sp = nat.stream_ptr()
+        nat.call('arlgpu_plan_build', nat.ptr(uvw), nat.ptr(f), n, ctypes.byref(gd), ctypes.byref(cd), nat.ptr(ws),
+                 ws.numel(), None, sp)
+        for _ in range(2):
+            nat.call('arlgpu_grid_planned', nat.ptr(v), nat.ptr(w), n, nat.FP32C, nat.ptr(cf_t), ctypes.byref(cd),
+                     nat.ptr(grid), ctypes.byref(gd), nat.ptr(sumwt), nat.ptr(ws), ws.numel(), sp)
+            assert rel(grid.to(torch.complex128).cpu().numpy(), g_ref) < TOL['fp32c']
+            assert rel(sumwt.cpu().numpy(), sw_ref) < TOLW['fp32c']
+        out = torch.empty((n, 1), dtype=torch.complex64, device=dev)
+        nat.call('arlgpu_degrid_planned', n, nat.FP32C, nat.ptr(cf_t), ctypes.byref(cd), nat.ptr(grid),
+                 ctypes.byref(gd), nat.ptr(out), nat.ptr(ws), ws.numel(), sp)
+        assert rel(out.to(torch.complex128).cpu().numpy(), oracle.degrid_vec(g_ref, maps, cf.data)) < TOL['fp32c']
+    finally:
+        arl.tune.set_tuning(**before)
+
+
 def _degrid_planned_with_flags(arl, vis, gd_h, cf, precision='fp32c'):
     """Degrid through the C ABI (plan_build + degrid_planned on this test's own
     workspace) and read the plan's status flags afterwards."""
