@@ -60,6 +60,7 @@ static std::atomic<int> g_tune_small_rows{2};     // rows per warp in the FP32C 
 static std::atomic<int> g_tune_small_rows_dg{4};  // rows per warp in the packed degridder when S <= 8
 static std::atomic<int> g_tune_lanes{0};          // lanes per row for every segment (0: by support)
 static std::atomic<int> g_tune_gather{1};         // FP32C gridder, one polarisation: rows copied into bin order first
+static std::atomic<int> g_tune_stash{1};          // packed degridder, one polarisation: row set-up from the footprint pass
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 bool tune_dsfft() { return g_tune_dsfft.load() != 0; }
 
@@ -388,16 +389,34 @@ struct SegBox {
   float vmax;
 };
 
-template <int NW, int NPOL, bool VMAX, bool SORTED = false>
+// STASH: the pass also leaves each row's set-up in shared memory for the row
+// loop (RowStash, indexed by sorted position - pos), computed here one row per
+// lane instead of once per row by a whole warp.
+constexpr int kStashRows = 512;  // rows a stash holds: chunks of at most this many rows
+struct RowStash {
+  int *koff;      // offset of the row's sub-kernel window in the cf table (its (toff, toff) tap)
+  int *geo;       // window origin in the subgrid (x | y << 8) and support (<< 16)
+  uint32_t *idx;  // the row's index in the caller's arrays
+};
+
+template <int NW, int NPOL, bool VMAX, bool SORTED = false, bool STASH = false>
 __device__ __forceinline__ SegBox seg_box(const SegInfo &sg, uint32_t pos, const RowMap *__restrict__ smap,
                                           const uint32_t *__restrict__ sidx, const float2 *__restrict__ vis,
-                                          const float *__restrict__ wt, const Geom &g, int *s_red) {
+                                          const float *__restrict__ wt, const Geom &g, int *s_red,
+                                          RowStash rs = RowStash{nullptr, nullptr, nullptr}) {
   int x0 = 0x7fffffff, y0 = 0x7fffffff, x1 = -0x7fffffff, y1 = -0x7fffffff, sz = 0;
   float vm = 0.f;
   for (uint32_t r = pos + threadIdx.x; r < sg.end; r += blockDim.x) {
     const RowMap m = smap[r];
     sz = plane_sz(g, m.sub >> 16);
     const int lx = m.pu - (sz >> 1) - sg.u0, ly = m.pv - (sz >> 1) - sg.v0;
+    if (STASH) {
+      const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16, toff = (g.S - sz) >> 1;
+      rs.koff[r - pos] = (int)(sg.ch * g.cf_chan_stride + zc * g.cf_z_stride) + ((vf * g.O + uf) * g.S + toff) * g.S +
+                         toff;
+      rs.geo[r - pos] = lx | (ly << 8) | (sz << 16);
+      if (!SORTED) rs.idx[r - pos] = sidx[r];
+    }
     x0 = min(x0, lx);
     x1 = max(x1, lx + sz);
     y0 = min(y0, ly);
@@ -1270,7 +1289,7 @@ __device__ __forceinline__ void fx_add(int *q, int *r, float x, float scale, flo
   }
 }
 
-template <int NPOL, int NW, bool RESID, int LPR = 0, int SGC = 0, bool SORTED = false>
+template <int NPOL, int NW, bool RESID, int LPR = 0, int SGC = 0, bool SORTED = false, bool STASH = false>
 __global__ void __launch_bounds__(NW * 32)
 k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
           const uint32_t *__restrict__ off, uint32_t chunk, const float2 *__restrict__ vis,
@@ -1302,6 +1321,10 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   build_tap_table(tab, S);
 
   __shared__ uint32_t s_next[2], s_chunk;
+  // Row set-up records (STASH, with SORTED rows), double-buffered like s_red.
+  static_assert(!STASH || SORTED, "the gridder's stash holds no row index");
+  constexpr int kSR = STASH ? kStashRows : 1;
+  __shared__ int s_koff[2][kSR], s_geo[2][kSR];
   int parity = 0;
   for (uint64_t cb = blockIdx.x; cb * chunk < nvalid; cb = next_chunk(cb, queue, &s_chunk)) {
   const uint32_t c0 = (uint32_t)(cb * chunk), c1 = min(c0 + chunk, nvalid);
@@ -1310,7 +1333,8 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
     if (threadIdx.x == 0) s_next[parity] = pos;  // published by the barrier in seg_box
     uint32_t *next_row = &s_next[parity];
-    const SegBox box = seg_box<NW, NPOL, true, SORTED>(sg, pos, smap, sidx, vis, wt, g, s_red[parity]);
+    const RowStash rs{s_koff[parity], s_geo[parity], nullptr};
+    const SegBox box = seg_box<NW, NPOL, true, SORTED, STASH>(sg, pos, smap, sidx, vis, wt, g, s_red[parity], rs);
     parity ^= 1;
     const uint32_t rows = sg.end - pos;
     const bool direct = seg_direct(box, rows);
@@ -1356,7 +1380,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       RowMap mnext;
       uint32_t inext = 0;
       if (rbase + half < sg.end) {
-        mnext = smap[rbase + half];
+        if constexpr (!STASH) mnext = smap[rbase + half];
         inext = SORTED ? rbase + half : sidx[rbase + half];
       }
       while (rbase < sg.end) {
@@ -1367,15 +1391,27 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         if (lane == 0) rn = atomicAdd(next_row, (uint32_t)RP);
         rn = __shfl_sync(0xffffffffu, rn, 0);
         if (rn + half < sg.end) {
-          mnext = smap[rn + half];
+          if constexpr (!STASH) mnext = smap[rn + half];
           inext = SORTED ? rn + half : sidx[rn + half];
         }
         rbase = rn;
         if (!act) continue;
-        const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-        const int sz = plane_sz(g, zc);
-        const int toff = (S - sz) >> 1;
-        const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
+        int sz, wu, wv;
+        const float2 *kb;
+        if constexpr (STASH) {
+          const int geo = rs.geo[idx - pos];  // SORTED: idx is the sorted position
+          sz = geo >> 16;
+          wu = sg.u0 + (geo & 0xff);
+          wv = sg.v0 + ((geo >> 8) & 0xff);
+          kb = cf + rs.koff[idx - pos];
+        } else {
+          const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+          sz = plane_sz(g, zc);
+          const int toff = (S - sz) >> 1;
+          wu = m.pu - (sz >> 1);
+          wv = m.pv - (sz >> 1);
+          kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride + ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+        }
         float2 vw[NPOL];
   #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
@@ -1389,8 +1425,6 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
             wsum[p] = s2;
           }
         }
-        const float2 *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
-                           ((int64_t)(vf * O + uf) * S + toff) * S + toff;
         const int n = sz * sz, dk = S - sz;
         const unsigned char *tj = tab + tap_base(sz) + hl;
         const float2 *kl = kb + hl;
@@ -1531,7 +1565,9 @@ __device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsign
 // DUP (FP32 only, degrid_kernel 3): the staged subgrid holds each cell as
 // (re, re, im, im), so a tap is two packed multiply-adds,
 // (sum re t.re, sum re t.im) and (sum im t.re, sum im t.im), instead of four.
-template <typename R, int NPOL, int NW, bool DUP = false, int LPR = 0, int SGC = 0>
+// STASH (with a chunk of at most kStashRows rows and a cf table of fewer than
+// 2^31 taps): the footprint pass leaves each row's set-up in shared memory.
+template <typename R, int NPOL, int NW, bool DUP = false, int LPR = 0, int SGC = 0, bool STASH = false>
 __global__ void __launch_bounds__(NW * 32)
 k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ sidx,
               const uint32_t *__restrict__ off, uint32_t chunk, int64_t nvis,
@@ -1556,6 +1592,11 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
 
   __shared__ int s_red[2][NW * 6];
   __shared__ uint32_t s_next[2], s_chunk;
+  // Row set-up records, double-buffered like s_red (segment s + 2 rewrites a
+  // buffer only after every warp has passed segment s + 1's barrier).
+  constexpr int kSR = STASH ? kStashRows : 1;
+  __shared__ int s_koff[2][kSR], s_geo[2][kSR];
+  __shared__ uint32_t s_idx[2][kSR];
   build_tap_table(tab, S);  // ordered before first use by the barrier in seg_box
   int parity = 0;
   for (uint64_t cb = blockIdx.x; cb < nchunks; cb = next_chunk(cb, queue, &s_chunk)) {
@@ -1572,9 +1613,10 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
     if (threadIdx.x == 0) s_next[parity] = pos;  // published by the barrier in seg_box
     uint32_t *next_row = &s_next[parity];
+    const RowStash rs{s_koff[parity], s_geo[parity], s_idx[parity]};
     // The footprint pass ends in a barrier, which also orders the previous
     // segment's reads of the subgrid before this segment's staging.
-    const SegBox box = seg_box<NW, 1, false>(sg, pos, smap, sidx, nullptr, nullptr, g, s_red[parity]);
+    const SegBox box = seg_box<NW, 1, false, false, STASH>(sg, pos, smap, sidx, nullptr, nullptr, g, s_red[parity], rs);
     parity ^= 1;
     const bool direct = seg_direct(box, sg.end - pos);
     const CT *gplane = grid + (int64_t)(sg.ch * NPOL) * g.nw * plane_elems + (int64_t)sg.zg * plane_elems;
@@ -1615,32 +1657,48 @@ k_degrid_lean(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restric
       rbase = __shfl_sync(0xffffffffu, rbase, 0);
       RowMap mnext;
       uint32_t inext = 0;
-      if (rbase + half < sg.end) {
-        mnext = smap[rbase + half];
-        inext = sidx[rbase + half];
+      if constexpr (!STASH) {
+        if (rbase + half < sg.end) {
+          mnext = smap[rbase + half];
+          inext = sidx[rbase + half];
+        }
       }
       while (rbase < sg.end) {
         const RowMap m = mnext;
-        const uint32_t idx = inext;
+        uint32_t idx = inext;
         const bool act = rbase + half < sg.end;
+        const uint32_t rk = rbase + half - pos;  // this lane's row in the stash (STASH)
         uint32_t rn = 0;
         if (lane == 0) rn = atomicAdd(next_row, (uint32_t)RP);
         rn = __shfl_sync(0xffffffffu, rn, 0);
-        if (rn + half < sg.end) {
-          mnext = smap[rn + half];
-          inext = sidx[rn + half];
+        if constexpr (!STASH) {
+          if (rn + half < sg.end) {
+            mnext = smap[rn + half];
+            inext = sidx[rn + half];
+          }
         }
         rbase = rn;
         R ax[NPOL], ay[NPOL];
   #pragma unroll
         for (int p = 0; p < NPOL; ++p) ax[p] = ay[p] = 0;
         if (act) {
-        const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
-        const int sz = plane_sz(g, zc);
-        const int toff = (S - sz) >> 1;
-        const int wu = m.pu - (sz >> 1), wv = m.pv - (sz >> 1);
-        const CT *kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride +
-                       ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+        int sz, wu, wv;
+        const CT *kb;
+        if constexpr (STASH) {
+          const int geo = rs.geo[rk];
+          idx = rs.idx[rk];
+          sz = geo >> 16;
+          wu = sg.u0 + (geo & 0xff);
+          wv = sg.v0 + ((geo >> 8) & 0xff);
+          kb = cf + rs.koff[rk];
+        } else {
+          const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
+          sz = plane_sz(g, zc);
+          const int toff = (S - sz) >> 1;
+          wu = m.pu - (sz >> 1);
+          wv = m.pv - (sz >> 1);
+          kb = cf + sg.ch * g.cf_chan_stride + zc * g.cf_z_stride + ((int64_t)(vf * O + uf) * S + toff) * S + toff;
+        }
         const CT *gl;
         int64_t pstride;
         int dg;
@@ -2462,6 +2520,12 @@ static uint32_t *work_queue(const PlanBufs &b, int which, cudaStream_t) {
   return g_tune_persistent.load() == 2 ? b.queue + which : nullptr;
 }
 
+// Elements of the cf table the geometry addresses.
+static int64_t cf_elems(const Geom &g) {
+  return (int64_t)(g.cf_nchan - 1) * g.cf_chan_stride + (int64_t)(g.cf_npol - 1) * g.cf_pol_stride +
+         (int64_t)g.nz * g.cf_z_stride;
+}
+
 static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const void *vis, const void *wt,
                           const void *cf, void *grid, double *sumwt, bool resid, cudaStream_t st) {
   const size_t smem = (size_t)(resid ? 4 : 2) * g.npol * g.SG * fx_pitch(g.SG) * 4 + tap_table_bytes(g.S);
@@ -2480,20 +2544,27 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
   // plan's dead mapping scratch: 8 + 4 bytes per row against its 20) and
   // read by sorted position (the SORTED instantiations).
   const bool sorted = g.npol == 1 && g_tune_gather.load() != 0;
+  // With sorted rows, supports above 8, chunks of at most kStashRows rows and
+  // a cf table addressable in 32 bits: the row set-up comes from the
+  // footprint pass (as in the packed degridder).
+  const bool stash = sorted && g.S > 8 && g_tune_stash.load() != 0 && chunk_rows() <= (uint32_t)kStashRows &&
+                     cf_elems(g) < 0x7fffffffll;
   auto pick = [&](auto resid_c) {
     constexpr bool RS = decltype(resid_c)::value;
-    auto by_lpr = [&](auto npol_c, auto sg_c, auto sorted_c) {
+    auto by_lpr = [&](auto npol_c, auto sg_c, auto sorted_c, auto stash_c) {
       constexpr int NP = decltype(npol_c)::value, SGV = decltype(sg_c)::value;
-      constexpr bool SO = decltype(sorted_c)::value;
-      return lpr == 8 ? k_grid_fx<NP, kWarps, RS, 8, SGV, SO>
-                      : lpr == 16 ? k_grid_fx<NP, kWarps, RS, 16, SGV, SO>
-                                  : lpr == 32 ? k_grid_fx<NP, kWarps, RS, 32, SGV, SO>
-                                              : k_grid_fx<NP, kWarps, RS, 0, SGV, SO>;
+      constexpr bool SO = decltype(sorted_c)::value, ST = decltype(stash_c)::value;
+      return lpr == 8 ? k_grid_fx<NP, kWarps, RS, 8, SGV, SO, ST>
+                      : lpr == 16 ? k_grid_fx<NP, kWarps, RS, 16, SGV, SO, ST>
+                                  : lpr == 32 ? k_grid_fx<NP, kWarps, RS, 32, SGV, SO, ST>
+                                              : k_grid_fx<NP, kWarps, RS, 0, SGV, SO, ST>;
     };
     if (csg) {
-      if (g.npol == 4) return by_lpr(IntC<4>(), IntC<32>(), BoolC<false>());
-      if (g.npol == 2) return by_lpr(IntC<2>(), IntC<48>(), BoolC<false>());
-      return sorted ? by_lpr(IntC<1>(), IntC<48>(), BoolC<true>()) : by_lpr(IntC<1>(), IntC<48>(), BoolC<false>());
+      if (g.npol == 4) return by_lpr(IntC<4>(), IntC<32>(), BoolC<false>(), BoolC<false>());
+      if (g.npol == 2) return by_lpr(IntC<2>(), IntC<48>(), BoolC<false>(), BoolC<false>());
+      if (!sorted) return by_lpr(IntC<1>(), IntC<48>(), BoolC<false>(), BoolC<false>());
+      return stash ? by_lpr(IntC<1>(), IntC<48>(), BoolC<true>(), BoolC<true>())
+                   : by_lpr(IntC<1>(), IntC<48>(), BoolC<true>(), BoolC<false>());
     }
     if (g.npol == 1) return sorted ? k_grid_fx<1, kWarps, RS, 0, 0, true> : k_grid_fx<1, kWarps, RS>;
     return g.npol == 2 ? k_grid_fx<2, kWarps, RS> : k_grid_fx<4, kWarps, RS>;
@@ -2686,19 +2757,25 @@ static int launch_degrid(const Geom &g, const PlanBufs &b, int64_t nvis, const v
       // the default subgrid edge as a compile-time constant (see the gridder)
       if (g.SG == (g.npol == 4 ? 32 : 48)) {
         done = true;
-        auto by_lpr = [&](auto npol_c, auto sg_c) {
+        auto by_lpr = [&](auto npol_c, auto sg_c, auto stash_c) {
           constexpr int NP = decltype(npol_c)::value, SGV = decltype(sg_c)::value;
-          return lpr == 8 ? k_degrid_lean<R, NP, kWarps, true, 8, SGV>
-                          : lpr == 16 ? k_degrid_lean<R, NP, kWarps, true, 16, SGV>
-                                      : lpr == 32 ? k_degrid_lean<R, NP, kWarps, true, 32, SGV>
-                                                  : k_degrid_lean<R, NP, kWarps, true, 0, SGV>;
+          constexpr bool ST = decltype(stash_c)::value;
+          return lpr == 8 ? k_degrid_lean<R, NP, kWarps, true, 8, SGV, ST>
+                          : lpr == 16 ? k_degrid_lean<R, NP, kWarps, true, 16, SGV, ST>
+                                      : lpr == 32 ? k_degrid_lean<R, NP, kWarps, true, 32, SGV, ST>
+                                                  : k_degrid_lean<R, NP, kWarps, true, 0, SGV, ST>;
         };
+        // One polarisation, chunks of at most kStashRows rows and a cf table
+        // addressable in 32 bits: the row set-up comes from the footprint pass.
+        // (Supports above 8: with four rows per warp the set-up is already shared.)
+        const bool stash = g.npol == 1 && g.S > 8 && g_tune_stash.load() != 0 &&
+                           chunk_rows() <= (uint32_t)kStashRows && cf_elems(g) < 0x7fffffffll;
         if (g.npol == 4)
-          kern = by_lpr(IntC<4>(), IntC<32>());
+          kern = by_lpr(IntC<4>(), IntC<32>(), BoolC<false>());
         else if (g.npol == 2)
-          kern = by_lpr(IntC<2>(), IntC<48>());
+          kern = by_lpr(IntC<2>(), IntC<48>(), BoolC<false>());
         else
-          kern = by_lpr(IntC<1>(), IntC<48>());
+          kern = stash ? by_lpr(IntC<1>(), IntC<48>(), BoolC<true>()) : by_lpr(IntC<1>(), IntC<48>(), BoolC<false>());
       }
     }
     if (!done)  // runtime edge: rows per warp chosen per segment only
@@ -2877,6 +2954,7 @@ extern "C" int arlgpu_set_tuning(const char *key, int value) {
   else if (k == "small_rows_degrid" && (value == 1 || value == 2 || value == 4)) g_tune_small_rows_dg = value;
   else if (k == "lanes_per_row" && (value == 0 || value == 8 || value == 16 || value == 32)) g_tune_lanes = value;
   else if (k == "gather_rows" && (value == 0 || value == 1)) g_tune_gather = value;
+  else if (k == "stash_rows" && (value == 0 || value == 1)) g_tune_stash = value;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key or value: %s = %d", key, value);
   return ARLGPU_OK;
 }
@@ -2894,6 +2972,7 @@ extern "C" int arlgpu_get_tuning(const char *key, int *value) {
   else if (k == "small_rows_degrid") *value = g_tune_small_rows_dg;
   else if (k == "lanes_per_row") *value = g_tune_lanes;
   else if (k == "gather_rows") *value = g_tune_gather;
+  else if (k == "stash_rows") *value = g_tune_stash;
   else return fail(ARLGPU_ERR_INVALID, "unknown tuning key: %s", key);
   return ARLGPU_OK;
 }

@@ -32,7 +32,7 @@ def get_tuning():
     lib = nat.load()
     out = {}
     for k in ('grid_kernel', 'degrid_kernel', 'subgrid', 'chunk', 'persistent', 'dsfft', 'small_rows', 'small_rows_degrid',
-              'lanes_per_row', 'gather_rows'):
+              'lanes_per_row', 'gather_rows', 'stash_rows'):
         v = ctypes.c_int()
         nat.check(lib.arlgpu_get_tuning(k.encode(), ctypes.byref(v)))
         out[k] = v.value

@@ -522,17 +522,21 @@ def test_work_queue_and_lanes_per_row_vs_oracle(arl, oracle, persistent, lanes_p
         arl.tune.set_tuning(**before)
 
 
-@pytest.mark.parametrize('gather_rows,persistent', [(0, 0), (1, 0), (1, 2)])
-def test_bin_order_rows_vs_oracle(arl, oracle, gather_rows, persistent):
+@pytest.mark.parametrize('gather_rows,persistent,stash_rows,chunk',
+                         [(0, 0, 0, 512), (1, 0, 0, 512), (1, 0, 1, 512), (1, 2, 1, 128), (0, 2, 1, 256),
+                          (1, 0, 1, 2048)])
+def test_bin_order_rows_vs_oracle(arl, oracle, gather_rows, persistent, stash_rows, chunk):
     """The FP32C gridder with one polarisation reading vis and weight from a
     bin-order copy in the plan workspace (gather_rows 1, the default) or
-    through the sort index (0), against the oracle; a plan gridded twice and
-    then degridded, so the copy in the plan's mapping scratch must leave the
-    plan itself intact."""
+    through the sort index (0), and the gridder and packed degridder taking
+    each row's set-up from the footprint pass (stash_rows 1, the default for
+    supports above 8 with chunks of at most 512 rows; chunk 2048 falls back),
+    against the oracle; a plan gridded twice and then degridded, so the copy
+    in the plan's mapping scratch must leave the plan itself intact."""
     import ctypes
     before = arl.tune.get_tuning()
     try:
-        arl.tune.set_tuning(gather_rows=gather_rows, persistent=persistent)
+        arl.tune.set_tuning(gather_rows=gather_rows, persistent=persistent, stash_rows=stash_rows, chunk=chunk)
         rng = numpy.random.default_rng(63)
         im, cf, vis, maps, gax = _random_case(arl, oracle, rng, 128, 4e-3, 8, 12, 40000, 2, 1, 3, 20.0, True)
         arl.set_plane_support(cf, [12, 8, 4])
