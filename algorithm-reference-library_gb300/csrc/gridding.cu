@@ -54,7 +54,7 @@ static std::atomic<int> g_tune_grid_kernel{4};    // 0: atomics + TwoSum, 1: ban
 static std::atomic<int> g_tune_degrid_kernel{3};  // 0: warp per row, 1: batched rows, 2: lean, 3: lean packed FMA
 static std::atomic<int> g_tune_subgrid{0};        // subgrid edge SG (0: automatic)
 static std::atomic<int> g_tune_chunk{512};        // sorted rows per gridder / degridder CTA
-static std::atomic<int> g_tune_persistent{0};     // lean / fixed-point kernels: 1 = one resident grid looping over chunks
+static std::atomic<int> g_tune_persistent{2};     // lean / fixed-point kernels: 0 = one CTA per chunk, 1 = resident grid taking every gridDim-th chunk, 2 = resident grid fed by a device work queue
 static std::atomic<int> g_tune_dsfft{1};          // FP32C inverse transforms: 1 = double-single FFT, 0 = cuFFT FP64
 static std::atomic<int> g_tune_small_rows{2};     // rows per warp in the FP32C gridder when S <= 8
 static std::atomic<int> g_tune_small_rows_dg{4};  // rows per warp in the packed degridder when S <= 8

@@ -141,7 +141,7 @@ def autotune(uvw, freq, vis, wt, cf_t, cd, gd, precision, reps=2, subgrids=SUBGR
     # largest support (0), or fixed for every segment; for supports up to 8
     # also the rows-per-warp keys.  Gridder and degridder are timed apart, so
     # each keeps its own best.
-    set_tuning(persistent=0, **best)
+    set_tuning(persistent=2, **best)
     lanes_opts = [dict(lanes_per_row=v) for v in LANES]
     if cd.support <= 8:
         lanes_opts += [dict(lanes_per_row=0, small_rows=a, small_rows_degrid=b) for a, b in SMALL_ROWS]

@@ -107,8 +107,8 @@ unsigned long long arlgpu_kernel_launches(void);
  *   "persistent"    1 = the lean and fixed-point kernels run as one grid of resident CTAs,
  *                   each looping over every gridDim-th chunk; 2 = the same resident grid fed by
  *                   a device work queue (each CTA takes the next unclaimed chunk with one
- *                   atomic); 0 = one CTA per chunk, which the hardware schedules dynamically
- *                   (default)
+ *                   atomic; the default); 0 = one CTA per chunk, which the hardware schedules
+ *                   dynamically
  *   "dsfft"         FP32C inverse transforms (invert_2d and w-stacking): 1 = double-single
  *                   FFT on the FP32 pipes for power-of-two sizes 64..8192 (default),
  *                   0 = cuFFT complex128
