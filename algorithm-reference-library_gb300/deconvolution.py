@@ -105,6 +105,40 @@ def msclean(dirty, psf, window, gain, thresh, niter, scales, fracthresh, prefix=
     return comps.cpu().numpy(), res.cpu().numpy()
 
 
+def _band(n, lo, hi):
+    """Boolean mask of the indices lo <= i < hi of an axis of length n."""
+    i = numpy.arange(n)
+    return (i >= lo) & (i < hi)
+
+
+def clean_window(shape, window_shape, edge=16):
+    """The CLEAN window of each (channel, polarisation) plane, as
+    ``deconvolution.py:82-100`` defines them: 'quarter' keeps rows and columns
+    q + 1 .. 3 q - 1 with q a quarter of the axis, 'no_edge' drops the first
+    edge + 1 and the last edge of each axis, None cleans everywhere (returns
+    None).  Other names raise ValueError."""
+    if window_shape is None:
+        return None
+    ny, nx = shape[-2], shape[-1]
+    if window_shape == 'quarter':
+        rows, cols = _band(ny, ny // 4 + 1, 3 * (ny // 4)), _band(nx, nx // 4 + 1, 3 * (nx // 4))
+    elif window_shape == 'no_edge':
+        rows, cols = _band(ny, edge + 1, ny - edge), _band(nx, edge + 1, nx - edge)
+    else:
+        raise ValueError("Window shape %s is not recognized" % window_shape)
+    return numpy.broadcast_to(numpy.outer(rows, cols).astype(numpy.float64), tuple(shape)).copy()
+
+
+def crop_psf_to_support(psf, support):
+    """Keep the 2 support x 2 support pixels around the PSF's centre pixel
+    (``deconvolution.py:108-113``), in place, when both axes are at least that
+    large."""
+    ny, nx = psf.data.shape[2], psf.data.shape[3]
+    if support <= ny // 2 and support <= nx // 2:
+        y0, x0 = ny // 2 - support, nx // 2 - support
+        psf.data = psf.data[..., y0:y0 + 2 * support, x0:x0 + 2 * support]
+
+
 def deconvolve_cube(dirty, psf, prefix='', **kwargs):
     """``deconvolution.py:43-300`` with algorithm='hogbom': window shapes
     'quarter' / 'no_edge' / None or a mask Image, PSF cropped to psf_support,
@@ -113,27 +147,12 @@ def deconvolve_cube(dirty, psf, prefix='', **kwargs):
     assert isinstance(dirty, Image), dirty
     assert isinstance(psf, Image), psf
     dd = dirty.data.cpu().numpy() if isinstance(dirty.data, torch.Tensor) else numpy.asarray(dirty.data)
-    window_shape = get_parameter(kwargs, 'window_shape', None)
-    ny, nx = dd.shape[2], dd.shape[3]
-    if window_shape == 'quarter':
-        qx, qy = nx // 4, ny // 4
-        window = numpy.zeros_like(dd)
-        window[..., (qy + 1):3 * qy, (qx + 1):3 * qx] = 1.0
-    elif window_shape == 'no_edge':
-        edge = get_parameter(kwargs, 'window_edge', 16)
-        window = numpy.zeros_like(dd)
-        window[..., (edge + 1):(ny - edge), (edge + 1):(nx - edge)] = 1.0
-    elif window_shape is None:
-        window = None
-    else:
-        raise ValueError("Window shape %s is not recognized" % window_shape)
+    window = clean_window(dd.shape, get_parameter(kwargs, 'window_shape', None),
+                          get_parameter(kwargs, 'window_edge', 16))
     mask = get_parameter(kwargs, 'mask', None)
     if isinstance(mask, Image):
         window = numpy.asarray(mask.data)
-    psf_support = get_parameter(kwargs, 'psf_support', max(dd.shape[2] // 2, dd.shape[3] // 2))
-    if psf_support <= psf.data.shape[2] // 2 and psf_support <= psf.data.shape[3] // 2:
-        c = [psf.data.shape[2] // 2, psf.data.shape[3] // 2]
-        psf.data = psf.data[..., (c[0] - psf_support):(c[0] + psf_support), (c[1] - psf_support):(c[1] + psf_support)]
+    crop_psf_to_support(psf, get_parameter(kwargs, 'psf_support', max(dd.shape[2] // 2, dd.shape[3] // 2)))
     algorithm = get_parameter(kwargs, 'algorithm', 'msclean')
     if algorithm not in ('hogbom', 'msclean'):
         raise NotImplementedError("deconvolve_cube algorithm %r is outside the GB300 path ('hogbom', 'msclean')"

@@ -170,3 +170,29 @@ def test_workload_shapes(arl):
     c4 = sim.make_workload('C4', max_rows=1000)
     assert c4['vis'] is None and c4['model_image'].shape == (1, 1, 2048, 2048)
     assert abs(numpy.abs(c4['gains']).mean() - 1.0) < 0.05
+
+
+def test_clean_windows_and_psf_crop(arl):
+    """deconvolve_cube's windows: 'quarter' keeps rows / columns q + 1 .. 3 q - 1
+    (q = n // 4), 'no_edge' keeps edge + 1 .. n - edge - 1; the PSF crop keeps
+    2 support pixels around the centre (deconvolution.py:82-113)."""
+    import numpy
+    dc = arl.deconvolution
+    w = dc.clean_window((1, 1, 32, 20), 'quarter')
+    rows, cols = numpy.nonzero(w[0, 0])
+    assert (rows.min(), rows.max(), cols.min(), cols.max()) == (9, 23, 6, 14)
+    assert w.sum() == 15 * 9
+    w = dc.clean_window((2, 1, 32, 20), 'no_edge', 3)
+    rows, cols = numpy.nonzero(w[1, 0])
+    assert (rows.min(), rows.max(), cols.min(), cols.max()) == (4, 28, 4, 16)
+    assert dc.clean_window((1, 1, 8, 8), 'no_edge', 6).sum() == 0
+    assert dc.clean_window((1, 1, 8, 8), None) is None
+    with pytest.raises(ValueError):
+        dc.clean_window((1, 1, 8, 8), 'circle')
+    psf = arl.create_image_from_array(numpy.arange(16 * 12, dtype=float).reshape(1, 1, 16, 12),
+                                      arl.create_image(npixel=16).wcs, arl.PolarisationFrame('stokesI'))
+    full = psf.data.copy()
+    dc.crop_psf_to_support(psf, 4)
+    assert psf.data.shape == (1, 1, 8, 8) and numpy.array_equal(psf.data, full[..., 4:12, 2:10])
+    dc.crop_psf_to_support(psf, 5)  # larger than half the cropped PSF: unchanged
+    assert psf.data.shape == (1, 1, 8, 8)
