@@ -2544,10 +2544,10 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
   // plan's dead mapping scratch: 8 + 4 bytes per row against its 20) and
   // read by sorted position (the SORTED instantiations).
   const bool sorted = g.npol == 1 && g_tune_gather.load() != 0;
-  // With sorted rows, supports above 8, chunks of at most kStashRows rows and
-  // a cf table addressable in 32 bits: the row set-up comes from the
-  // footprint pass (as in the packed degridder).
-  const bool stash = sorted && g.S > 8 && g_tune_stash.load() != 0 && chunk_rows() <= (uint32_t)kStashRows &&
+  // With sorted rows, chunks of at most kStashRows rows and a cf table
+  // addressable in 32 bits: the row set-up comes from the footprint pass (as
+  // in the packed degridder, which takes it for supports above 8 only).
+  const bool stash = sorted && g_tune_stash.load() != 0 && chunk_rows() <= (uint32_t)kStashRows &&
                      cf_elems(g) < 0x7fffffffll;
   auto pick = [&](auto resid_c) {
     constexpr bool RS = decltype(resid_c)::value;
