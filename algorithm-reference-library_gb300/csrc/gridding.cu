@@ -1321,10 +1321,11 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   build_tap_table(tab, S);
 
   __shared__ uint32_t s_next[2], s_chunk;
-  // Row set-up records (STASH, with SORTED rows), double-buffered like s_red.
-  static_assert(!STASH || SORTED, "the gridder's stash holds no row index");
+  // Row set-up records (STASH), double-buffered like s_red; without SORTED
+  // rows they carry each row's index in the caller's arrays too.
   constexpr int kSR = STASH ? kStashRows : 1;
   __shared__ int s_koff[2][kSR], s_geo[2][kSR];
+  __shared__ uint32_t s_idx[2][STASH && !SORTED ? kStashRows : 1];
   int parity = 0;
   for (uint64_t cb = blockIdx.x; cb * chunk < nvalid; cb = next_chunk(cb, queue, &s_chunk)) {
   const uint32_t c0 = (uint32_t)(cb * chunk), c1 = min(c0 + chunk, nvalid);
@@ -1333,7 +1334,7 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
     const SegInfo sg = seg_at(pos, c1, smap, off, g);
     if (threadIdx.x == 0) s_next[parity] = pos;  // published by the barrier in seg_box
     uint32_t *next_row = &s_next[parity];
-    const RowStash rs{s_koff[parity], s_geo[parity], nullptr};
+    const RowStash rs{s_koff[parity], s_geo[parity], s_idx[parity]};
     const SegBox box = seg_box<NW, NPOL, true, SORTED, STASH>(sg, pos, smap, sidx, vis, wt, g, s_red[parity], rs);
     parity ^= 1;
     const uint32_t rows = sg.end - pos;
@@ -1379,9 +1380,11 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
       rbase = __shfl_sync(0xffffffffu, rbase, 0);
       RowMap mnext;
       uint32_t inext = 0;
+      // With STASH the sorted position goes into inext (the record's index);
+      // the caller's row index comes from the record.
       if (rbase + half < sg.end) {
         if constexpr (!STASH) mnext = smap[rbase + half];
-        inext = SORTED ? rbase + half : sidx[rbase + half];
+        inext = SORTED || STASH ? rbase + half : sidx[rbase + half];
       }
       while (rbase < sg.end) {
         const RowMap m = mnext;
@@ -1392,18 +1395,20 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         rn = __shfl_sync(0xffffffffu, rn, 0);
         if (rn + half < sg.end) {
           if constexpr (!STASH) mnext = smap[rn + half];
-          inext = SORTED ? rn + half : sidx[rn + half];
+          inext = SORTED || STASH ? rn + half : sidx[rn + half];
         }
         rbase = rn;
         if (!act) continue;
         int sz, wu, wv;
         const float2 *kb;
+        uint32_t ridx = idx;  // the row's index into vis / wt
         if constexpr (STASH) {
-          const int geo = rs.geo[idx - pos];  // SORTED: idx is the sorted position
+          const int geo = rs.geo[idx - pos];  // idx is the sorted position here
           sz = geo >> 16;
           wu = sg.u0 + (geo & 0xff);
           wv = sg.v0 + ((geo >> 8) & 0xff);
           kb = cf + rs.koff[idx - pos];
+          if constexpr (!SORTED) ridx = rs.idx[idx - pos];
         } else {
           const int uf = m.sub & 0xff, vf = (m.sub >> 8) & 0xff, zc = m.sub >> 16;
           sz = plane_sz(g, zc);
@@ -1415,8 +1420,8 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         float2 vw[NPOL];
   #pragma unroll
         for (int p = 0; p < NPOL; ++p) {
-          const float2 v = vis[(size_t)idx * NPOL + p];
-          const float w = wt[(size_t)idx * NPOL + p];
+          const float2 v = vis[(size_t)ridx * NPOL + p];
+          const float w = wt[(size_t)ridx * NPOL + p];
           vw[p].x = v.x * w;
           vw[p].y = v.y * w;
           if (hl == 0) {
@@ -2549,6 +2554,10 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
   // in the packed degridder, which takes it for supports above 8 only).
   const bool stash = sorted && g_tune_stash.load() != 0 && chunk_rows() <= (uint32_t)kStashRows &&
                      cf_elems(g) < 0x7fffffffll;
+  // Four polarisations (rows gathered through the sort index): the stash
+  // carries each row's index too.
+  const bool stash4 = g.npol == 4 && g_tune_stash.load() != 0 && chunk_rows() <= (uint32_t)kStashRows &&
+                      cf_elems(g) < 0x7fffffffll;
   auto pick = [&](auto resid_c) {
     constexpr bool RS = decltype(resid_c)::value;
     auto by_lpr = [&](auto npol_c, auto sg_c, auto sorted_c, auto stash_c) {
@@ -2560,7 +2569,9 @@ static int launch_grid_fx(const Geom &g, const PlanBufs &b, int64_t nvis, const 
                                               : k_grid_fx<NP, kWarps, RS, 0, SGV, SO, ST>;
     };
     if (csg) {
-      if (g.npol == 4) return by_lpr(IntC<4>(), IntC<32>(), BoolC<false>(), BoolC<false>());
+      if (g.npol == 4)
+        return stash4 ? by_lpr(IntC<4>(), IntC<32>(), BoolC<false>(), BoolC<true>())
+                      : by_lpr(IntC<4>(), IntC<32>(), BoolC<false>(), BoolC<false>());
       if (g.npol == 2) return by_lpr(IntC<2>(), IntC<48>(), BoolC<false>(), BoolC<false>());
       if (!sorted) return by_lpr(IntC<1>(), IntC<48>(), BoolC<false>(), BoolC<false>());
       return stash ? by_lpr(IntC<1>(), IntC<48>(), BoolC<true>(), BoolC<true>())

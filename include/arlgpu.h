@@ -124,8 +124,9 @@ unsigned long long arlgpu_kernel_launches(void);
  *                   rows' vis and weight into bin order, into the plan workspace's mapping
  *                   scratch, and reads them contiguously (default); 0 = it gathers them
  *                   through the sort index in its row loop.  Either way the grid is the same.
- *   "stash_rows"    1 = with one polarisation and chunks of at most 512 rows, the FP32C
- *                   fixed-point gridder (and, for supports above 8, the packed degridder) take
+ *   "stash_rows"    1 = with one or four polarisations and chunks of at most 512 rows, the
+ *                   FP32C fixed-point gridder (and, for one polarisation and supports above 8,
+ *                   the packed degridder) take
  *                   each row's set-up (kernel-window offset, window origin, support, row index)
  *                   from the footprint pass, which computes it one row per lane, instead of
  *                   a whole warp computing it per row (default); 0 = per row in the row loop.
