@@ -66,6 +66,8 @@ SIGNATURES = {
     'arlgpu_dft_adjoint': (ctypes.c_int, [_vp, _i64, _vp, _i32, _i32, ctypes.c_int, _vp, _vp, _vp]),
     'arlgpu_hogbom': (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _f64, _f64, _i32, _f64, _f64, _f64,
                                      _vp, _vp, _P(_i32), _vp]),
+    'arlgpu_hogbom_complex': (ctypes.c_int, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _f64, _f64, _i32, _f64,
+                                             _f64, _f64, _vp, _vp, _vp, _vp, _P(_i32), _vp]),
     'arlgpu_msclean_setup_bytes': (ctypes.c_int, [_i32, _i32, _i32, _i32, _i32, _P(_sz)]),
     'arlgpu_msclean_setup': (ctypes.c_int, [_vp, _i32, _i32, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp,
                                             _vp, _vp, _vp, _sz, _vp]),

@@ -2,6 +2,7 @@
 //
 // Reference behaviour:
 //   hogbom, overlapIndices    processing_library/arrays/cleaners.py:12-69, :134-154
+//   hogbom_complex            processing_library/arrays/cleaners.py:72-131
 //   deconvolve_cube('hogbom') processing_components/image/deconvolution.py:43-300
 //
 // Each minor-cycle iteration is two launches on one stream, with no host
@@ -127,6 +128,113 @@ __global__ void k_hog_sub(double *__restrict__ res, int nx, int ny, const double
     if (ri == peak) {
       st->iters += 1;
       if (fabs(nv) < stop_level) st->stop = 1;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Complex Hogbom CLEAN of Q + iU (processing_library/arrays/cleaners.py:72-131):
+// the same two launches per iteration on a residual held as two planes
+// (real, imaginary).  The peak is the first largest |res * window| (or |res|)
+// with |.| the hypotenuse of the two parts, as numpy.absolute; the component
+// res[peak] * gain / pmax and the PSF subtraction are taken part by part
+// (the PSF is real), and the loop stops when |res[peak]| after the
+// subtraction falls below the threshold itself (no 0.9 factor here).
+// ---------------------------------------------------------------------------
+struct HogCState {
+  double mre, mim;
+  long long peak;
+  int stop;
+  int iters;
+  unsigned int counter;
+};
+
+__global__ void __launch_bounds__(kFindThreads)
+k_hogc_find(const double *__restrict__ rre, const double *__restrict__ rim, const double *__restrict__ window,
+            long long n, double gain, double pmax, double *__restrict__ cre, double *__restrict__ cim,
+            Best *__restrict__ partial, HogCState *__restrict__ st) {
+  if (st->stop) return;
+  __shared__ Best s_best[kFindThreads / 32];
+  __shared__ bool s_last;
+  Best b{-1.0, 0x7fffffffffffffffll};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double a = window ? hypot(__dmul_rn(rre[i], window[i]), __dmul_rn(rim[i], window[i])) : hypot(rre[i], rim[i]);
+    b = better(b, Best{a, i});
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    Best c;
+    c.v = __shfl_xor_sync(0xffffffffu, b.v, o);
+    c.i = __shfl_xor_sync(0xffffffffu, b.i, o);
+    b = better(b, c);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) s_best[warp] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Best t = s_best[0];
+    for (int k = 1; k < kFindThreads / 32; ++k) t = better(t, s_best[k]);
+    partial[blockIdx.x] = t;
+    __threadfence();
+    s_last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  Best t{-1.0, 0x7fffffffffffffffll};
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    Best q;
+    q.v = __ldcg(&partial[k].v);
+    q.i = __ldcg(&partial[k].i);
+    t = better(t, q);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    Best c;
+    c.v = __shfl_xor_sync(0xffffffffu, t.v, o);
+    c.i = __shfl_xor_sync(0xffffffffu, t.i, o);
+    t = better(t, c);
+  }
+  if (lane == 0) s_best[warp] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Best f = s_best[0];
+    for (int k = 1; k < kFindThreads / 32; ++k) f = better(f, s_best[k]);
+    const double mre = __ddiv_rn(__dmul_rn(rre[f.i], gain), pmax);
+    const double mim = __ddiv_rn(__dmul_rn(rim[f.i], gain), pmax);
+    cre[f.i] = __dadd_rn(cre[f.i], mre);
+    cim[f.i] = __dadd_rn(cim[f.i], mim);
+    st->mre = mre;
+    st->mim = mim;
+    st->peak = f.i;
+    st->counter = 0;
+  }
+}
+
+__global__ void k_hogc_sub(double *__restrict__ rre, double *__restrict__ rim, int nx, int ny,
+                           const double *__restrict__ psf, int pnx, int pny, double stop_level,
+                           HogCState *__restrict__ st) {
+  if (st->stop) return;
+  const long long peak = st->peak;
+  const int mx = (int)(peak / ny), my = (int)(peak - (long long)mx * ny);
+  const double mre = st->mre, mim = st->mim;
+  const int wx = pnx / 2, wy = pny / 2;
+  const int r0 = max(0, mx - wx), r1 = min(nx, mx + wx);
+  const int c0 = max(0, my - wy), c1 = min(my + wy, ny);
+  const int p0 = max(0, wx + (r0 - mx)), q0 = max(0, wy + (c0 - my));
+  const int p1 = min(pnx, wx + (r1 - mx)), q1 = min(wy + (c1 - my), pny);
+  const int h = min(r1 - r0, p1 - p0), w = min(c1 - c0, q1 - q0);
+  const long long total = (long long)h * w;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+       k += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(k / w), j = (int)(k - (long long)i * w);
+    const long long ri = (long long)(r0 + i) * ny + (c0 + j);
+    const double pv = psf[(long long)(p0 + i) * pny + (q0 + j)];
+    const double nre = __dsub_rn(rre[ri], __dmul_rn(pv, mre));
+    const double nim = __dsub_rn(rim[ri], __dmul_rn(pv, mim));
+    rre[ri] = nre;
+    rim[ri] = nim;
+    if (ri == peak) {
+      st->iters += 1;
+      if (hypot(nre, nim) < stop_level) st->stop = 1;
     }
   }
 }
@@ -320,6 +428,69 @@ extern "C" int arlgpu_hogbom(const double *dirty, const double *psf, const doubl
       if (cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess) {
         rc = fail(ARLGPU_ERR_CUDA, "hogbom state read failed");
+        break;
+      }
+      if (hs.stop) break;
+    }
+  } while (false);
+  *iterations = hs.iters;
+  cudaFreeAsync(partial, st);
+  cudaFreeAsync(state, st);
+  return rc;
+}
+
+extern "C" int arlgpu_hogbom_complex(const double *dirty_q, const double *dirty_u, const double *psf,
+                                     const double *window, int32_t nx, int32_t ny, int32_t psf_nx, int32_t psf_ny,
+                                     double gain, double thresh, int32_t niter, double fracthresh,
+                                     double dirty_absmax, double psf_max, double *comps_q, double *comps_u,
+                                     double *res_q, double *res_u, int32_t *iterations, void *stream) {
+  if (!dirty_q || !dirty_u || !psf || !comps_q || !comps_u || !res_q || !res_u || !iterations)
+    return fail(ARLGPU_ERR_INVALID, "null array argument");
+  if (nx < 1 || ny < 1 || psf_nx < 2 || psf_ny < 2) return fail(ARLGPU_ERR_INVALID, "bad image or psf shape");
+  if (!(gain > 0.0 && gain < 2.0)) return fail(ARLGPU_ERR_INVALID, "gain must be in (0, 2)");
+  if (niter < 1) return fail(ARLGPU_ERR_INVALID, "niter must be > 0");
+  if (!(psf_max > 0.0)) return fail(ARLGPU_ERR_INVALID, "psf maximum must be > 0");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long long n = (long long)nx * ny;
+  const int fblocks = nblk(n, 152 * 4);
+  const int sblocks = nblk((long long)psf_nx * psf_ny, 152 * 8);
+  HogCState *state = nullptr;
+  Best *partial = nullptr;
+  ARL_CUDA(cudaMallocAsync(&state, sizeof(HogCState), st));
+  int rc = ARLGPU_OK;
+  if (cudaMallocAsync(&partial, sizeof(Best) * fblocks, st) != cudaSuccess) {
+    cudaFreeAsync(state, st);
+    return fail(ARLGPU_ERR_CUDA, "cudaMallocAsync failed");
+  }
+  const double absthresh = fmax(thresh, fracthresh * dirty_absmax);
+  constexpr int kCheck = 64;
+  int it = 0;
+  HogCState hs{};
+  do {
+    if (cudaMemsetAsync(state, 0, sizeof(HogCState), st) != cudaSuccess ||
+        cudaMemcpyAsync(res_q, dirty_q, sizeof(double) * n, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(res_u, dirty_u, sizeof(double) * n, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(comps_q, 0, sizeof(double) * n, st) != cudaSuccess ||
+        cudaMemsetAsync(comps_u, 0, sizeof(double) * n, st) != cudaSuccess) {
+      rc = fail(ARLGPU_ERR_CUDA, "hogbom_complex set-up failed");
+      break;
+    }
+    while (it < niter) {
+      const int batch = niter - it < kCheck ? niter - it : kCheck;
+      for (int k = 0; k < batch; ++k) {
+        k_hogc_find<<<fblocks, kFindThreads, 0, st>>>(res_q, res_u, window, n, gain, psf_max, comps_q, comps_u,
+                                                       partial, state);
+        k_hogc_sub<<<sblocks, 256, 0, st>>>(res_q, res_u, nx, ny, psf, psf_nx, psf_ny, absthresh, state);
+      }
+      count_launch(2 * batch);
+      it += batch;
+      if (cudaGetLastError() != cudaSuccess) {
+        rc = fail(ARLGPU_ERR_CUDA, "hogbom_complex launch failed");
+        break;
+      }
+      if (cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess) {
+        rc = fail(ARLGPU_ERR_CUDA, "hogbom_complex state read failed");
         break;
       }
       if (hs.stop) break;

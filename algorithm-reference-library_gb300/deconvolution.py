@@ -2,6 +2,7 @@
 
 Reference behaviour:
   hogbom, overlapIndices    processing_library/arrays/cleaners.py:12-69, :134-154
+  hogbom_complex            processing_library/arrays/cleaners.py:72-131
   msclean and its helpers   processing_library/arrays/cleaners.py:165-440
   deconvolve_cube           processing_components/image/deconvolution.py:43-300 ('hogbom', 'msclean')
 
@@ -11,8 +12,10 @@ equal NumPy's bit for bit.  The multiscale set-up (scale images, their
 convolutions with the dirty image and the PSF as complex128 cuFFT transforms,
 the coupling matrix, the window stack) is ``csrc/msclean_setup.cu``; it
 rounds differently from NumPy's FFTs, so msclean agrees with the reference to
-a stated FP64 tolerance rather than bit for bit.  deconvolve_cube's other
-algorithms raise NotImplementedError.
+a stated FP64 tolerance rather than bit for bit.  The complex Hogbom of
+Q + iU (``cleaners.py:72-131``, deconvolve_cube 'hogbom-complex') runs the
+same way on two residual planes.  deconvolve_cube's other algorithms raise
+NotImplementedError.
 """
 import ctypes
 
@@ -21,7 +24,7 @@ import torch
 
 from . import _native as nat
 from . import device as dv
-from .data_models import Image, create_image_from_array
+from .data_models import Image, PolarisationFrame, create_image_from_array
 from .imaging import get_parameter
 
 
@@ -59,6 +62,32 @@ def hogbom(dirty, psf, window, gain, thresh, niter, fracthresh, prefix=''):
     if isinstance(dirty, torch.Tensor):
         return comps, res
     return comps.cpu().numpy(), res.cpu().numpy()
+
+
+def hogbom_complex(dirty_q, dirty_u, psf_q, psf_u, window, gain, thresh, niter, fracthresh):
+    """``cleaners.py:72-131``: complex Hogbom CLEAN of Q + iU with the (common)
+    PSF; returns (Q components, U components, Q residual, U residual).  Inputs
+    are arrays or CUDA tensors; the minor cycle runs on the device
+    (``arlgpu_hogbom_complex``)."""
+    assert 0.0 < gain < 2.0
+    assert niter > 0
+    device = dv.require_cuda()
+    dq, du = _plane(dirty_q, device), _plane(dirty_u, device)
+    pq, pu = _plane(psf_q, device), _plane(psf_u, device)
+    assert bool(torch.equal(pq, pu))
+    w = None if window is None else _plane(window, device)
+    nx, ny = dq.shape
+    pmax = float(pq.max().item())
+    assert pmax > 0.0
+    dmax = float(torch.hypot(dq, du).max().item())
+    cq, cu, rq, ru = (torch.empty_like(dq) for _ in range(4))
+    iters = ctypes.c_int32(0)
+    nat.call('arlgpu_hogbom_complex', nat.ptr(dq), nat.ptr(du), nat.ptr(pq), nat.ptr(w), nx, ny, pq.shape[0],
+             pq.shape[1], float(gain), float(thresh), int(niter), float(fracthresh), dmax, pmax, nat.ptr(cq),
+             nat.ptr(cu), nat.ptr(rq), nat.ptr(ru), ctypes.byref(iters), nat.stream_ptr())
+    if isinstance(dirty_q, torch.Tensor):
+        return cq, cu, rq, ru
+    return cq.cpu().numpy(), cu.cpu().numpy(), rq.cpu().numpy(), ru.cpu().numpy()
 
 
 def msclean(dirty, psf, window, gain, thresh, niter, scales, fracthresh, prefix=''):
@@ -139,6 +168,34 @@ def crop_psf_to_support(psf, support):
         psf.data = psf.data[..., y0:y0 + 2 * support, x0:x0 + 2 * support]
 
 
+def _deconvolve_cube_complex(dd, psf, window, kwargs, wcs):
+    """``deconvolution.py:244-292``: per channel, polarisations 0 and 3 by
+    Hogbom, 1 and 2 together as Q + iU by complex Hogbom (with polarisation 1's
+    window); components and residuals in the stokesIQUV frame."""
+    gain = get_parameter(kwargs, 'gain', 0.7)
+    assert 0.0 < gain < 2.0, "Loop gain must be between 0 and 2"
+    thresh = get_parameter(kwargs, 'threshold', 0.0)
+    assert thresh >= 0.0
+    niter = get_parameter(kwargs, 'niter', 100)
+    assert niter > 0
+    fracthresh = get_parameter(kwargs, 'fractional_threshold', 0.1)
+    assert 0.0 <= fracthresh < 1.0
+    pd = psf.data.cpu().numpy() if isinstance(psf.data, torch.Tensor) else numpy.asarray(psf.data)
+    comp = numpy.zeros(dd.shape)
+    resid = numpy.zeros(dd.shape)
+    for ch in range(dd.shape[0]):
+        for pol in (0, 3):
+            if pol < dd.shape[1] and pd[ch, pol].max():
+                w = None if window is None else window[ch, pol]
+                comp[ch, pol], resid[ch, pol] = hogbom(dd[ch, pol], pd[ch, pol], w, gain, thresh, niter, fracthresh)
+        if dd.shape[1] > 2 and pd[ch, 1:2].max():
+            w = None if window is None else window[ch, 1]
+            comp[ch, 1], comp[ch, 2], resid[ch, 1], resid[ch, 2] = hogbom_complex(
+                dd[ch, 1], dd[ch, 2], pd[ch, 1], pd[ch, 2], w, gain, thresh, niter, fracthresh)
+    frame = PolarisationFrame('stokesIQUV')
+    return create_image_from_array(comp, wcs, frame), create_image_from_array(resid, wcs, frame)
+
+
 def deconvolve_cube(dirty, psf, prefix='', **kwargs):
     """``deconvolution.py:43-300`` with algorithm='hogbom': window shapes
     'quarter' / 'no_edge' / None or a mask Image, PSF cropped to psf_support,
@@ -154,9 +211,11 @@ def deconvolve_cube(dirty, psf, prefix='', **kwargs):
         window = numpy.asarray(mask.data)
     crop_psf_to_support(psf, get_parameter(kwargs, 'psf_support', max(dd.shape[2] // 2, dd.shape[3] // 2)))
     algorithm = get_parameter(kwargs, 'algorithm', 'msclean')
+    if algorithm == 'hogbom-complex':
+        return _deconvolve_cube_complex(dd, psf, window, kwargs, dirty.wcs)
     if algorithm not in ('hogbom', 'msclean'):
-        raise NotImplementedError("deconvolve_cube algorithm %r is outside the GB300 path ('hogbom', 'msclean')"
-                                  % algorithm)
+        raise NotImplementedError("deconvolve_cube algorithm %r is outside the GB300 path ('hogbom', "
+                                  "'hogbom-complex', 'msclean')" % algorithm)
     gain = get_parameter(kwargs, 'gain', 0.7)
     assert 0.0 < gain < 2.0, "Loop gain must be between 0 and 2"
     thresh = get_parameter(kwargs, 'threshold', 0.0)

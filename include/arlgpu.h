@@ -318,6 +318,18 @@ int arlgpu_hogbom(const double *dirty, const double *psf, const double *window, 
                   double dirty_absmax, double psf_max, double *comps, double *res, int32_t *iterations,
                   void *stream);
 
+/* ---- (f4) hogbom_complex (processing_library/arrays/cleaners.py:72-131): CLEAN of Q + iU ----
+ * dirty_q, dirty_u, comps_q, comps_u, res_q, res_u [nx][ny] (device, FP64): the residual
+ * Q + iU starts as the dirty pair and the components at zero; psf [psf_nx][psf_ny] is
+ * the (common, real) PSF; window [nx][ny] or NULL.  The peak is the first largest
+ * |res * window| (|.| the hypotenuse); the loop stops after niter iterations or when
+ * |res[peak]| < max(thresh, fracthresh * dirty_absmax), dirty_absmax = max |Q + iU|.
+ * *iterations (host) receives the count. */
+int arlgpu_hogbom_complex(const double *dirty_q, const double *dirty_u, const double *psf, const double *window,
+                          int32_t nx, int32_t ny, int32_t psf_nx, int32_t psf_ny, double gain, double thresh,
+                          int32_t niter, double fracthresh, double dirty_absmax, double psf_max, double *comps_q,
+                          double *comps_u, double *res_q, double *res_u, int32_t *iterations, void *stream);
+
 /* ---- (f4) msclean (processing_library/arrays/cleaners.py:165-280): the minor cycle ----
  * stack [nscales][nx][ny] is the scale-convolved residual (updated in place), psf_ss
  * [nscales][nscales][psf_nx][psf_ny] the twice-convolved PSF stack, pscale [nscales]

@@ -313,6 +313,49 @@ def case_hogbom(out):
                            cube_comp=comp.data, cube_resid=resid.data)
 
 
+def case_hogbom_complex(out):
+    """Complex Hogbom CLEAN of Q + iU (``processing_library/arrays/cleaners.py:72-131``)
+    and ``deconvolve_cube(algorithm='hogbom-complex')`` on a four-polarisation
+    cube (``processing_components/image/deconvolution.py:244-292``: I and V
+    by Hogbom, Q and U together)."""
+    from processing_library.arrays.cleaners import hogbom_complex
+    from processing_components.image.deconvolution import deconvolve_cube
+    rng = numpy.random.default_rng(5151)
+    N = 96
+    samp = numpy.zeros((N, N))
+    samp[rng.integers(N // 2 - 24, N // 2 + 24, 2500), rng.integers(N // 2 - 24, N // 2 + 24, 2500)] = 1.0
+    samp = samp + samp[::-1, ::-1]
+    psf = numpy.real(numpy.fft.fftshift(numpy.fft.ifft2(numpy.fft.ifftshift(samp))))
+    psf /= psf.max()
+
+    def dirty_of(sky):
+        return numpy.real(numpy.fft.fftshift(numpy.fft.ifft2(numpy.fft.fft2(numpy.fft.ifftshift(sky)) *
+                                                             numpy.fft.fft2(numpy.fft.ifftshift(psf)))))
+    pos = (rng.integers(N // 4, 3 * N // 4, 10), rng.integers(N // 4, 3 * N // 4, 10))
+    sky_i, sky_q, sky_u, sky_v = (numpy.zeros((N, N)) for _ in range(4))
+    sky_i[pos] = rng.uniform(1.0, 4.0, 10)
+    sky_q[pos] = rng.uniform(-1.0, 1.0, 10)
+    sky_u[pos] = rng.uniform(-1.0, 1.0, 10)
+    sky_v[pos] = rng.uniform(-0.2, 0.2, 10)
+    dq = dirty_of(sky_q) + 0.01 * rng.normal(size=(N, N))
+    du = dirty_of(sky_u) + 0.01 * rng.normal(size=(N, N))
+    window = numpy.zeros((N, N))
+    window[N // 8:7 * N // 8, N // 8:7 * N // 8] = 1.0
+    cq1, cu1, rq1, ru1 = hogbom_complex(dq, du, psf, psf, None, 0.1, 0.0, 300, 0.01)
+    cq2, cu2, rq2, ru2 = hogbom_complex(dq, du, psf, psf, window, 0.5, 0.02, 200, 0.001)
+    im = make_image(N, 0.001, numpy.array([1e8]), 1e7, 'stokesIQUV')
+    d4 = numpy.stack([dirty_of(sky_i) + 0.01 * rng.normal(size=(N, N)), dq, du,
+                      dirty_of(sky_v) + 0.01 * rng.normal(size=(N, N))])[None]
+    p4 = numpy.stack([psf] * 4)[None]
+    dim = create_image_from_array(d4, im.wcs, im.polarisation_frame)
+    pim = create_image_from_array(p4.copy(), im.wcs, im.polarisation_frame)
+    comp, resid = deconvolve_cube(dim, pim, algorithm='hogbom-complex', niter=150, gain=0.2, threshold=0.0,
+                                  fractional_threshold=0.05, window_shape='quarter', psf_support=30)
+    numpy.savez_compressed(out, dq=dq, du=du, psf=psf, window=window, cq1=cq1, cu1=cu1, rq1=rq1, ru1=ru1,
+                           cq2=cq2, cu2=cu2, rq2=rq2, ru2=ru2, di=d4[0, 0], dv=d4[0, 3], cube_comp=comp.data,
+                           cube_resid=resid.data)
+
+
 def case_msclean(out):
     """Multiscale CLEAN (``processing_library/arrays/cleaners.py:165-280``) and
     ``deconvolve_cube(algorithm='msclean')`` on the Hogbom case's dirty image."""
@@ -473,6 +516,7 @@ API = [
     ('processing_components.visibility.coalesce', 'convert_visibility_to_blockvisibility'),
     ('processing_components.image.deconvolution', 'deconvolve_cube'),
     ('processing_library.arrays.cleaners', 'hogbom'),
+    ('processing_library.arrays.cleaners', 'hogbom_complex'),
     ('processing_library.arrays.cleaners', 'msclean'),
     ('workflows.shared.imaging.imaging_shared', 'imaging_contexts'),
     ('workflows.shared.imaging.imaging_shared', 'imaging_context'),
@@ -513,6 +557,7 @@ ALL_CASES = {
     'ref_weighting': case_weighting,
     'ref_blocks': case_blocks,
     'ref_hogbom': case_hogbom,
+    'ref_hogbom_complex': case_hogbom_complex,
     'ref_msclean': case_msclean,
     'ref_rowops': case_rowops,
     'ref_api': case_api,
