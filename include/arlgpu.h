@@ -41,7 +41,7 @@ enum {
   ARLGPU_ERR_INVALID = 1,       /* bad argument (shape, pointer, precision) */
   ARLGPU_ERR_CUDA = 2,          /* a CUDA runtime call failed */
   ARLGPU_ERR_OUT_OF_GRID = 3,   /* rows whose kernel window leaves the grid */
-  ARLGPU_ERR_UNSUPPORTED = 4,   /* valid ARL input this build does not handle */
+  ARLGPU_ERR_UNSUPPORTED = 4,   /* valid ARL input this library does not handle */
   ARLGPU_ERR_WORKSPACE = 5,     /* workspace missing or too small */
   ARLGPU_ERR_CUFFT = 6          /* a cuFFT call failed */
 };
