@@ -35,6 +35,7 @@ from .coalesce import (convert_blockvisibility_to_visibility, convert_visibility
 from .data_models import GainTable, ReceptorFrame, Skycomponent, copy_blockvisibility  # noqa: F401
 from .calibration import apply_gaintable, vis_timeslice_iter  # noqa: F401
 from .skycomponents import predict_skycomponent_visibility  # noqa: F401
-from .deconvolution import deconvolve_cube, hogbom, hogbom_complex, msclean  # noqa: F401
+from .deconvolution import (deconvolve_cube, hogbom, hogbom_complex, msclean, msmfsclean,  # noqa: F401
+                            calculate_image_frequency_moments, calculate_image_from_frequency_moments)
 
 __version__ = '0.1.0'

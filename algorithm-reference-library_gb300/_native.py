@@ -69,6 +69,11 @@ SIGNATURES = {
     'arlgpu_hogbom_complex': (ctypes.c_int, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _f64, _f64, _i32, _f64,
                                              _f64, _f64, _vp, _vp, _vp, _vp, _P(_i32), _vp]),
     'arlgpu_msclean_setup_bytes': (ctypes.c_int, [_i32, _i32, _i32, _i32, _i32, _P(_sz)]),
+    'arlgpu_scale_stack': (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp, _vp]),
+    'arlgpu_scale_convolve_bytes': (ctypes.c_int, [_i32, _i32, _i32, _P(_sz)]),
+    'arlgpu_scale_convolve': (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp, _i32, _i32, _f64, _vp, _vp, _sz, _vp]),
+    'arlgpu_msmfsclean': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _f64,
+                                         _f64, _i32, _i32, _vp, _P(_i32), _vp]),
     'arlgpu_msclean_setup': (ctypes.c_int, [_vp, _i32, _i32, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp,
                                             _vp, _vp, _vp, _sz, _vp]),
     'arlgpu_msclean': (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _f64, _f64, _i32, _vp,

@@ -240,6 +240,192 @@ __global__ void k_hogc_sub(double *__restrict__ rre, double *__restrict__ rim, i
 }
 
 // ---------------------------------------------------------------------------
+// Multi-scale multi-frequency CLEAN minor cycle (processing_library/arrays/
+// cleaners.py:469-600 with find_global_optimum :601-634,
+// update_scale_moment_residual :636-646, update_moment_model :648-661,
+// calculate_scale_moment_principal_solution :722-735 and
+// find_optimum_scale_zero_moment :738-767).  Inputs from the set-up: the
+// scale-moment residual smres [ns][nm][n0][n1], the scale-scale-moment-moment
+// PSF ssm [ns][ns][nm][nm][p0][p1], the PSF-sized scale images pscale
+// [ns][p0][p1], an optional window stack [ns][n0][n1] and the moment-moment
+// Hessian and its inverse [ns][nm][nm].  Per iteration:
+//   k_mfs_find  for each scale, the principal solution
+//               smpsol[s][n] = sum_m ih[s][m][n] smres[s][m] at every pixel and
+//               the search image (ARL: smpsol[s][0] smres[s][0]; Algorithm1:
+//               smpsol[s][0]; CASA: the chi^2 change); the scale whose search
+//               image has the largest |. * window| (first scale on ties, 0 if
+//               none exceeds 0) wins, at the first largest signed (unwindowed)
+//               search value -- the reference's argmax; the last block forms
+//               mval = smpsol[scale][:, peak] and stops the loop when
+//               max |mval| falls below the threshold;
+//   k_mfs_sub   smres[:, :, lhs] -= gain * sum_q ssm[scale, :, :, q, rhs] mval[q]
+//               and model[t, lhs] += pscale[scale, rhs] * gain * mval[t].
+// FP64 with each operation rounded on its own, in the reference's order.
+// ---------------------------------------------------------------------------
+constexpr int kMfsMaxScales = 16, kMfsMaxMoments = 8;
+
+struct MfsState {
+  double mval[kMfsMaxMoments];
+  long long peak;
+  int scale;
+  int stop;
+  int iters;
+  unsigned int counter;
+};
+
+struct MfsBest {
+  double absmax;  // largest |search * window| (value only)
+  Best vmax;      // first largest signed search value
+};
+
+__device__ __forceinline__ void mfs_solution(const double *__restrict__ smres, const double *__restrict__ ihess,
+                                             int s, int nm, long long plane, long long i, double *sol) {
+  // einsum("smn,smxy->snxy"): sum over m in order
+  for (int n = 0; n < nm; ++n) {
+    double acc = 0.0;
+    for (int m = 0; m < nm; ++m)
+      acc = __dadd_rn(acc, __dmul_rn(ihess[(s * nm + m) * nm + n], smres[((long long)s * nm + m) * plane + i]));
+    sol[n] = acc;
+  }
+}
+
+__device__ __forceinline__ double mfs_search(const double *__restrict__ smres, const double *__restrict__ hess,
+                                             const double *sol, int s, int nm, long long plane, long long i,
+                                             int findpeak) {
+  if (findpeak == 1) return sol[0];  // Algorithm1
+  if (findpeak == 2) {               // CASA: dchisq
+    double d = 0.0;
+    for (int m1 = 0; m1 < nm; ++m1) {
+      d = __dadd_rn(d, __dmul_rn(__dmul_rn(2.0, sol[m1]), smres[((long long)s * nm + m1) * plane + i]));
+      for (int m2 = 0; m2 < nm; ++m2)
+        d = __dsub_rn(d, __dmul_rn(__dmul_rn(hess[(s * nm + m1) * nm + m2], sol[m1]), sol[m2]));
+    }
+    return d;
+  }
+  return __dmul_rn(sol[0], smres[(long long)s * nm * plane + i]);  // ARL
+}
+
+__global__ void __launch_bounds__(kFindThreads)
+k_mfs_find(const double *__restrict__ smres, const double *__restrict__ windowstack, const double *__restrict__ hess,
+           const double *__restrict__ ihess, int ns, int nm, long long plane, int findpeak, double absthresh,
+           MfsBest *__restrict__ partial, MfsState *__restrict__ st) {
+  if (st->stop) return;
+  __shared__ double s_abs[kFindThreads / 32];
+  __shared__ Best s_best[kFindThreads / 32];
+  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double sol[kMfsMaxMoments];
+  for (int s = 0; s < ns; ++s) {
+    double am = 0.0;
+    Best b{-INFINITY, 0x7fffffffffffffffll};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < plane;
+         i += (long long)gridDim.x * blockDim.x) {
+      mfs_solution(smres, ihess, s, nm, plane, i, sol);
+      const double v = mfs_search(smres, hess, sol, s, nm, plane, i, findpeak);
+      const double vw = windowstack ? __dmul_rn(v, windowstack[(long long)s * plane + i]) : v;
+      am = fmax(am, fabs(vw));
+      b = better(b, Best{v, i});
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      am = fmax(am, __shfl_xor_sync(0xffffffffu, am, o));
+      Best c;
+      c.v = __shfl_xor_sync(0xffffffffu, b.v, o);
+      c.i = __shfl_xor_sync(0xffffffffu, b.i, o);
+      b = better(b, c);
+    }
+    if (lane == 0) {
+      s_abs[warp] = am;
+      s_best[warp] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      MfsBest t{s_abs[0], s_best[0]};
+      for (int k = 1; k < kFindThreads / 32; ++k) {
+        t.absmax = fmax(t.absmax, s_abs[k]);
+        t.vmax = better(t.vmax, s_best[k]);
+      }
+      partial[(long long)blockIdx.x * ns + s] = t;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  // Last block, one thread: per scale the reduction over blocks, then the
+  // scale search of find_optimum_scale_zero_moment.
+  __threadfence();
+  double optimum = 0.0;
+  int sscale = 0;
+  long long sidx = 0;
+  for (int s = 0; s < ns; ++s) {
+    double am = 0.0;
+    Best b{-INFINITY, 0x7fffffffffffffffll};
+    for (int k = 0; k < (int)gridDim.x; ++k) {
+      const MfsBest *q = &partial[(long long)k * ns + s];
+      am = fmax(am, __ldcg(&q->absmax));
+      b = better(b, Best{__ldcg(&q->vmax.v), __ldcg(&q->vmax.i)});
+    }
+    if (am > optimum) {
+      optimum = am;
+      sscale = s;
+      sidx = b.i;
+    }
+  }
+  mfs_solution(smres, ihess, sscale, nm, plane, sidx, sol);
+  double peak = 0.0;
+  for (int n = 0; n < nm; ++n) {
+    st->mval[n] = sol[n];
+    peak = fmax(peak, fabs(sol[n]));
+  }
+  st->scale = sscale;
+  st->peak = sidx;
+  st->counter = 0;
+  st->iters += 1;
+  if (peak < absthresh) st->stop = 2;  // stop before this iteration's update
+}
+
+__global__ void k_mfs_sub(double *__restrict__ smres, double *__restrict__ model, const double *__restrict__ ssm,
+                          const double *__restrict__ pscale, int ns, int nm, int n0, int n1, int p0n, int p1n,
+                          double gain, MfsState *__restrict__ st) {
+  if (st->stop) return;
+  const long long peak = st->peak;
+  const int mx = (int)(peak / n1), my = (int)(peak - (long long)mx * n1);
+  const int ms = st->scale;
+  const int wx = p0n / 2, wy = p1n / 2;
+  const int r0 = max(0, mx - wx), r1 = min(n0, mx + wx);
+  const int c0 = max(0, my - wy), c1 = min(my + wy, n1);
+  const int q0 = max(0, wx + (r0 - mx)), s0 = max(0, wy + (c0 - my));
+  const int q1 = min(p0n, wx + (r1 - mx)), s1 = min(wy + (c1 - my), p1n);
+  const int h = min(r1 - r0, q1 - q0), w = min(c1 - c0, s1 - s0);
+  const long long plane = (long long)n0 * n1, pplane = (long long)p0n * p1n;
+  const long long total = (long long)h * w;
+  double mv[kMfsMaxMoments];
+  for (int t = 0; t < nm; ++t) mv[t] = st->mval[t];
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+       k += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(k / w), j = (int)(k - (long long)i * w);
+    const long long ri = (long long)(r0 + i) * n1 + (c0 + j);
+    const long long pi = (long long)(q0 + i) * p1n + (s0 + j);
+    for (int s = 0; s < ns; ++s)
+      for (int t = 0; t < nm; ++t) {
+        double acc = 0.0;  // einsum("stqxy,q->stxy"): sum over q in order
+        for (int q = 0; q < nm; ++q)
+          acc = __dadd_rn(acc, __dmul_rn(ssm[((((long long)ms * ns + s) * nm + t) * nm + q) * pplane + pi], mv[q]));
+        double *r = smres + ((long long)s * nm + t) * plane + ri;
+        *r = __dsub_rn(*r, __dmul_rn(gain, acc));
+      }
+    const double ps = pscale[(long long)ms * pplane + pi];
+    for (int t = 0; t < nm; ++t) {
+      double *m = model + (long long)t * plane + ri;
+      *m = __dadd_rn(*m, __dmul_rn(__dmul_rn(ps, gain), mv[t]));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Multiscale CLEAN (processing_library/arrays/cleaners.py:165-280): the
 // minor-cycle loop over the scale stack.  The scale images, the twice-
 // convolved PSF stack and the coupling matrix come from the caller (the
@@ -491,6 +677,68 @@ extern "C" int arlgpu_hogbom_complex(const double *dirty_q, const double *dirty_
       if (cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess) {
         rc = fail(ARLGPU_ERR_CUDA, "hogbom_complex state read failed");
+        break;
+      }
+      if (hs.stop) break;
+    }
+  } while (false);
+  *iterations = hs.iters;
+  cudaFreeAsync(partial, st);
+  cudaFreeAsync(state, st);
+  return rc;
+}
+
+extern "C" int arlgpu_msmfsclean(double *smres, const double *ssm, const double *pscale, const double *windowstack,
+                                 const double *hess, const double *ihess, int32_t nscales, int32_t nmoment,
+                                 int32_t n0, int32_t n1, int32_t psf_n0, int32_t psf_n1, double gain, double absthresh,
+                                 int32_t niter, int32_t findpeak, double *model, int32_t *iterations, void *stream) {
+  if (!smres || !ssm || !pscale || !hess || !ihess || !model || !iterations)
+    return fail(ARLGPU_ERR_INVALID, "null array argument");
+  if (nscales < 1 || nscales > kMfsMaxScales || nmoment < 1 || nmoment > kMfsMaxMoments)
+    return fail(ARLGPU_ERR_UNSUPPORTED, "msmfsclean takes 1..%d scales and 1..%d moments", kMfsMaxScales,
+                kMfsMaxMoments);
+  if (n0 < 1 || n1 < 1 || psf_n0 < 2 || psf_n1 < 2) return fail(ARLGPU_ERR_INVALID, "bad image or psf shape");
+  if (!(gain > 0.0 && gain < 2.0)) return fail(ARLGPU_ERR_INVALID, "gain must be in (0, 2)");
+  if (niter < 1) return fail(ARLGPU_ERR_INVALID, "niter must be > 0");
+  if (findpeak < 0 || findpeak > 2) return fail(ARLGPU_ERR_INVALID, "findpeak must be 0 (ARL), 1 (Algorithm1), 2 (CASA)");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long long plane = (long long)n0 * n1;
+  const int fblocks = nblk(plane, 152 * 2);
+  const int sblocks = nblk((long long)psf_n0 * psf_n1, 152 * 8);
+  MfsState *state = nullptr;
+  MfsBest *partial = nullptr;
+  ARL_CUDA(cudaMallocAsync(&state, sizeof(MfsState), st));
+  int rc = ARLGPU_OK;
+  if (cudaMallocAsync(&partial, sizeof(MfsBest) * fblocks * nscales, st) != cudaSuccess) {
+    cudaFreeAsync(state, st);
+    return fail(ARLGPU_ERR_CUDA, "cudaMallocAsync failed");
+  }
+  constexpr int kCheck = 32;
+  int it = 0;
+  MfsState hs{};
+  do {
+    if (cudaMemsetAsync(state, 0, sizeof(MfsState), st) != cudaSuccess ||
+        cudaMemsetAsync(model, 0, sizeof(double) * plane * nmoment, st) != cudaSuccess) {
+      rc = fail(ARLGPU_ERR_CUDA, "msmfsclean set-up failed");
+      break;
+    }
+    while (it < niter) {
+      const int batch = niter - it < kCheck ? niter - it : kCheck;
+      for (int k = 0; k < batch; ++k) {
+        k_mfs_find<<<fblocks, kFindThreads, 0, st>>>(smres, windowstack, hess, ihess, nscales, nmoment, plane,
+                                                      findpeak, absthresh, partial, state);
+        k_mfs_sub<<<sblocks, 256, 0, st>>>(smres, model, ssm, pscale, nscales, nmoment, n0, n1, psf_n0, psf_n1,
+                                           gain, state);
+      }
+      count_launch(2 * batch);
+      it += batch;
+      if (cudaGetLastError() != cudaSuccess) {
+        rc = fail(ARLGPU_ERR_CUDA, "msmfsclean launch failed");
+        break;
+      }
+      if (cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess) {
+        rc = fail(ARLGPU_ERR_CUDA, "msmfsclean state read failed");
         break;
       }
       if (hs.stop) break;

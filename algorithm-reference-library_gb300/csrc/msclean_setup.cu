@@ -337,3 +337,95 @@ extern "C" int arlgpu_msclean_setup(const double *dirty, int32_t nx, int32_t ny,
   count_launch(launches);
   return ARLGPU_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Building blocks of the multi-scale multi-frequency CLEAN set-up
+// (cleaners.py:469-540): scale basis stacks of any shape, and images
+// convolved once (convolve_scalestack, :319-335) or twice
+// (convolve_convolve_scalestack, :338-360) with a given stack, through the
+// same shift / transform / spectra passes as the msclean set-up above.
+// ---------------------------------------------------------------------------
+extern "C" int arlgpu_scale_stack(const double *scales_host, int32_t nscales, int32_t n0, int32_t n1, double *stack,
+                                  void *stream) {
+  if (!scales_host || !stack) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  if (n0 < 1 || n1 < 1 || nscales < 1 || nscales > 64) return fail(ARLGPU_ERR_INVALID, "bad scale-stack shape");
+  for (int s = 0; s < nscales; ++s) {
+    const double sc = scales_host[s];
+    if (!(sc >= 0.0) || sc > 1e6) return fail(ARLGPU_ERR_INVALID, "scale %d is %g", s, sc);
+    const int w = sc > 0.0 ? 2 * (int)ceil(sc / 2.0) + 2 : 1;
+    if (w > n0 || w > n1) return fail(ARLGPU_ERR_UNSUPPORTED, "scale %g is wider than the image", sc);
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double *scales = nullptr;
+  ARL_CUDA(cudaMallocAsync(&scales, sizeof(double) * nscales, st));
+  int rc = ARLGPU_OK;
+  if (cudaMemcpyAsync(scales, scales_host, sizeof(double) * nscales, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemsetAsync(stack, 0, sizeof(double) * n0 * n1 * nscales, st) != cudaSuccess) {
+    rc = fail(ARLGPU_ERR_CUDA, "scale-stack set-up failed");
+  } else {
+    k_scale_basis<<<nscales, 256, 0, st>>>(scales, n0, n1, stack);
+    k_scale_norm<<<nscales, 256, 0, st>>>(scales, n0, n1, stack);
+    if (cudaGetLastError() != cudaSuccess) rc = fail(ARLGPU_ERR_CUDA, "scale-stack launch failed");
+    count_launch(2);
+  }
+  // the caller's host array is staged before cudaMemcpyAsync returns; the
+  // device copy is freed in stream order
+  cudaFreeAsync(scales, st);
+  return rc;
+}
+
+static size_t conv_bytes(int n0, int n1, int ns) {
+  const size_t d = (size_t)n0 * n1;
+  return al(16 * d) + 2 * al(16 * d * ns);
+}
+
+extern "C" int arlgpu_scale_convolve_bytes(int32_t n0, int32_t n1, int32_t nscales, size_t *bytes_host) {
+  if (n0 < 1 || n1 < 1 || nscales < 1 || !bytes_host) return fail(ARLGPU_ERR_INVALID, "bad scale-convolve shape");
+  *bytes_host = conv_bytes(n0, n1, nscales);
+  return ARLGPU_OK;
+}
+
+extern "C" int arlgpu_scale_convolve(const double *img, int32_t nimg, int32_t n0, int32_t n1, const double *stack,
+                                     int32_t nscales, int32_t twice, double thresh, double *out, void *workspace,
+                                     size_t workspace_bytes, void *stream) {
+  if (!img || !stack || !out) return fail(ARLGPU_ERR_INVALID, "null array argument");
+  if (nimg < 1 || n0 < 1 || n1 < 1 || nscales < 1 || nscales > 64) return fail(ARLGPU_ERR_INVALID, "bad shapes");
+  const size_t need = conv_bytes(n0, n1, nscales);
+  if (!workspace || workspace_bytes < need)
+    return fail(ARLGPU_ERR_WORKSPACE, "scale convolution needs %zu bytes of workspace, got %zu", need,
+                workspace_bytes);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int64_t d = (int64_t)n0 * n1;
+  char *w = static_cast<char *>(workspace);
+  double2 *fd = reinterpret_cast<double2 *>(w);
+  w += al(16 * d);
+  double2 *fs = reinterpret_cast<double2 *>(w);
+  w += al(16 * d * nscales);
+  double2 *td = reinterpret_cast<double2 *>(w);
+  const double sd = (1.0 / n0) * (1.0 / n1);
+  unsigned launches = 0;
+  k_shift_in<<<nblk(d * nscales), 256, 0, st>>>(stack, nscales, n0, n1, nullptr, fs);
+  ++launches;
+  ARL_LAUNCH_CHECK();
+  ARL_TRY(fft_z2z(fs, n0, n1, nscales, CUFFT_FORWARD, st));
+  for (int i = 0; i < nimg; ++i) {
+    k_shift_in<<<nblk(d), 256, 0, st>>>(img + (int64_t)i * d, 1, n0, n1, nullptr, fd);
+    ++launches;
+    ARL_LAUNCH_CHECK();
+    ARL_TRY(fft_z2z(fd, n0, n1, 1, CUFFT_FORWARD, st));
+    const int nouter = twice ? nscales : 1;
+    for (int s = 0; s < nouter; ++s) {
+      k_spectra<<<nblk(d * nscales), 256, 0, st>>>(fd, fs, twice ? fs + (int64_t)s * d : nullptr, nscales, d, td);
+      ++launches;
+      ARL_LAUNCH_CHECK();
+      ARL_TRY(fft_z2z(td, n0, n1, nscales, CUFFT_INVERSE, st));
+      double *o = out + ((int64_t)i * nouter + s) * nscales * d;
+      k_shift_out<<<nblk(d * nscales), 256, 0, st>>>(td, nscales, n0, n1, sd, twice ? -1.0 : thresh, o);
+      ++launches;
+      ARL_LAUNCH_CHECK();
+    }
+  }
+  count_launch(launches);
+  return ARLGPU_OK;
+}
+

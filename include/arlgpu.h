@@ -330,6 +330,34 @@ int arlgpu_hogbom_complex(const double *dirty_q, const double *dirty_u, const do
                           int32_t niter, double fracthresh, double dirty_absmax, double psf_max, double *comps_q,
                           double *comps_u, double *res_q, double *res_u, int32_t *iterations, void *stream);
 
+/* ---- (f4) msmfsclean (processing_library/arrays/cleaners.py:469-600): the minor cycle ----
+ * smres [nscales][nmoment][n0][n1] is the scale-moment residual (updated in place), ssm
+ * [nscales][nscales][nmoment][nmoment][psf_n0][psf_n1] the scale-scale-moment-moment PSF,
+ * pscale [nscales][psf_n0][psf_n1] the PSF-sized scale images, windowstack [nscales][n0][n1]
+ * or NULL, hess / ihess [nscales][nmoment][nmoment] the moment-moment Hessian at the PSF
+ * centre and its inverse; model [nmoment][n0][n1] is written.  findpeak: 0 'ARL', 1
+ * 'Algorithm1', 2 'CASA' (find_global_optimum, cleaners.py:601-634).  At most 16 scales and
+ * 8 moments.  Stops after niter iterations or when max |mval| < absthresh. */
+int arlgpu_msmfsclean(double *smres, const double *ssm, const double *pscale, const double *windowstack,
+                      const double *hess, const double *ihess, int32_t nscales, int32_t nmoment, int32_t n0,
+                      int32_t n1, int32_t psf_n0, int32_t psf_n1, double gain, double absthresh, int32_t niter,
+                      int32_t findpeak, double *model, int32_t *iterations, void *stream);
+
+/* Scale basis stack [nscales][n0][n1] (create_scalestack, cleaners.py:283-316) from the
+ * caller's host array of scales (pixels). */
+int arlgpu_scale_stack(const double *scales_host, int32_t nscales, int32_t n0, int32_t n1, double *stack,
+                       void *stream);
+
+/* img [nimg][n0][n1] convolved with every plane of stack [nscales][n0][n1]:
+ * convolve_scalestack (cleaners.py:319-335) into out [nimg][nscales][n0][n1], or with twice
+ * != 0 convolve_convolve_scalestack (:338-360) into out [nimg][nscales][nscales][n0][n1].
+ * thresh >= 0 (once only) writes 1 where the result exceeds thresh and 0 elsewhere, as the
+ * window stacks are made.  Device workspace of arlgpu_scale_convolve_bytes. */
+int arlgpu_scale_convolve_bytes(int32_t n0, int32_t n1, int32_t nscales, size_t *bytes_host);
+int arlgpu_scale_convolve(const double *img, int32_t nimg, int32_t n0, int32_t n1, const double *stack,
+                          int32_t nscales, int32_t twice, double thresh, double *out, void *workspace,
+                          size_t workspace_bytes, void *stream);
+
 /* ---- (f4) msclean (processing_library/arrays/cleaners.py:165-280): the minor cycle ----
  * stack [nscales][nx][ny] is the scale-convolved residual (updated in place), psf_ss
  * [nscales][nscales][psf_nx][psf_ny] the twice-convolved PSF stack, pscale [nscales]

@@ -182,6 +182,7 @@ class _WcsPrm:
     def __init__(self, naxis):
         self.naxis = naxis
         self.ctype = [''] * naxis
+        self.cunit = [''] * naxis
         self.axis_types = [0] * naxis
         self._crval = numpy.zeros(naxis)
         self._crpix = numpy.zeros(naxis)
@@ -213,6 +214,16 @@ class WCS:
         return copy.deepcopy(self)
 
     def sub(self, axes):
+        # 'spectral' / 'celestial' select axes by type, as astropy's sub does
+        named = []
+        for a in axes:
+            if a == 'spectral':
+                named += [k + 1 for k in range(self.naxis) if str(self.wcs.ctype[k]).startswith('FREQ')]
+            elif a == 'celestial':
+                named += [k + 1 for k in range(self.naxis) if str(self.wcs.ctype[k])[:2] in ('RA', 'DE')]
+            else:
+                named.append(a)
+        axes = named
         out = WCS(naxis=len(axes))
         for i, a in enumerate(axes):
             out.wcs.ctype[i] = self.wcs.ctype[a - 1]

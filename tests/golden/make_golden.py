@@ -373,6 +373,60 @@ def case_msclean(out):
     numpy.savez_compressed(out, c1=c1, r1=r1, c2=c2, r2=r2, cube_comp=comp.data, cube_resid=resid.data)
 
 
+def case_msmfsclean(out):
+    """Multi-scale multi-frequency CLEAN (``processing_library/arrays/cleaners.py:469-760``,
+    each findpeak), the image frequency moments (``processing_components/image/
+    operations.py:239-330``) and ``deconvolve_cube(algorithm='msmfsclean')`` on a
+    five-channel cube whose PSF scales with frequency."""
+    from processing_library.arrays.cleaners import msmfsclean
+    from processing_components.image.deconvolution import deconvolve_cube
+    from processing_components.image.operations import calculate_image_frequency_moments
+    rng = numpy.random.default_rng(6262)
+    N, nchan = 64, 5
+    freqs = numpy.linspace(0.9e8, 1.1e8, nchan)
+    u = rng.normal(0.0, 7.0, 1500)
+    v = rng.normal(0.0, 7.0, 1500)
+
+    def psf_at(f):
+        samp = numpy.zeros((N, N))
+        iu = numpy.round(u * f / 1e8).astype(int) + N // 2
+        iv = numpy.round(v * f / 1e8).astype(int) + N // 2
+        ok = (iu > 0) & (iu < N) & (iv > 0) & (iv < N)
+        numpy.add.at(samp, (iu[ok], iv[ok]), 1.0)
+        samp = samp + samp[::-1, ::-1]
+        p = numpy.real(numpy.fft.fftshift(numpy.fft.ifft2(numpy.fft.ifftshift(samp))))
+        return p / p.max()
+
+    psfs = numpy.stack([psf_at(f) for f in freqs])
+    pos = (rng.integers(N // 4, 3 * N // 4, 6), rng.integers(N // 4, 3 * N // 4, 6))
+    flux, alpha = rng.uniform(1.0, 3.0, 6), rng.uniform(-1.0, 0.5, 6)
+    cube = numpy.zeros((nchan, 1, N, N))
+    for c, f in enumerate(freqs):
+        sky = numpy.zeros((N, N))
+        sky[pos] = flux * (f / 1e8) ** alpha
+        cube[c, 0] = numpy.real(numpy.fft.fftshift(numpy.fft.ifft2(numpy.fft.fft2(numpy.fft.ifftshift(sky)) *
+                                                                   numpy.fft.fft2(numpy.fft.ifftshift(psfs[c])))))
+    cube += 0.005 * rng.normal(size=cube.shape)
+    im = make_image(N, 0.001, freqs, freqs[1] - freqs[0], 'stokesI')
+    dim = create_image_from_array(cube, im.wcs, im.polarisation_frame)
+    pim = create_image_from_array(psfs[:, None].copy(), im.wcs, im.polarisation_frame)
+    dmom = calculate_image_frequency_moments(dim, nmoment=2).data[:, 0]
+    pmom = calculate_image_frequency_moments(pim, nmoment=4).data[:, 0]
+    res = dict(cube=cube, psfs=psfs, freqs=freqs, dmom=dmom, pmom=pmom)
+    window = numpy.zeros((N, N))
+    window[8:56, 8:56] = 1.0
+    res['window'] = window
+    for tag, fp, win in (('arl', 'ARL', None), ('casa', 'CASA', None), ('alg1', 'Algorithm1', None),
+                         ('arlw', 'ARL', window)):
+        c, r = msmfsclean(dmom.copy(), pmom.copy(), win, 0.3, 0.0, 80, [0, 3, 8], 0.02, fp)
+        res['c_' + tag], res['r_' + tag] = c, r
+    comp, resid = deconvolve_cube(dim, create_image_from_array(psfs[:, None].copy(), im.wcs, im.polarisation_frame),
+                                  algorithm='msmfsclean', nmoment=2, niter=60, gain=0.3, threshold=0.0,
+                                  fractional_threshold=0.05, scales=[0, 3, 8])
+    res['cube_comp'], res['cube_resid'] = comp.data, resid.data
+    numpy.savez_compressed(out, **res)
+
+
 def case_rowops(out):
     """Row operations on the path's edges, from the reference's own code:
 
@@ -518,6 +572,9 @@ API = [
     ('processing_library.arrays.cleaners', 'hogbom'),
     ('processing_library.arrays.cleaners', 'hogbom_complex'),
     ('processing_library.arrays.cleaners', 'msclean'),
+    ('processing_library.arrays.cleaners', 'msmfsclean'),
+    ('processing_components.image.operations', 'calculate_image_frequency_moments'),
+    ('processing_components.image.operations', 'calculate_image_from_frequency_moments'),
     ('workflows.shared.imaging.imaging_shared', 'imaging_contexts'),
     ('workflows.shared.imaging.imaging_shared', 'imaging_context'),
     ('workflows.serial.imaging.imaging_serial', 'invert_list_serial_workflow'),
@@ -559,6 +616,7 @@ ALL_CASES = {
     'ref_hogbom': case_hogbom,
     'ref_hogbom_complex': case_hogbom_complex,
     'ref_msclean': case_msclean,
+    'ref_msmfsclean': case_msmfsclean,
     'ref_rowops': case_rowops,
     'ref_api': case_api,
 }
