@@ -85,7 +85,7 @@ SIGNATURES = {
     'arlgpu_fft_grid_to_image': (ctypes.c_int, [_vp, _P(GridDesc), ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     'arlgpu_fft_image_to_grid': (ctypes.c_int, [_vp, _vp, _P(GridDesc), ctypes.c_int, _vp, _vp]),
     'arlgpu_make_pswf': (ctypes.c_int, [_i32, _i32, _i32, _i32, _vp, _vp, _vp]),
-    'arlgpu_make_wkernels': (ctypes.c_int, [_i32, _f64, _i32, _i32, _i32, _i32, _f64, _vp, _vp]),
+    'arlgpu_make_wkernels': (ctypes.c_int, [_i32, _f64, _i32, _i32, _i32, _i32, _f64, _i32, _vp, _vp]),
     'arlgpu_apply_gains': (ctypes.c_int, [_vp, _i64, _i32, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, _vp]),
     'arlgpu_apply_gaintable': (ctypes.c_int, [_vp, _i32, _i32, _i32, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int,
                                               _vp]),

@@ -128,9 +128,11 @@ __global__ void k_wscreen(int nb, int z0, int nw, double wstep, int qnx, int nx,
         sincos(ph, &s, &co);
         val = make_double2(co, s);
       }
-      const double nv = norm[qy * qnx + qx];
-      val.x *= nv;
-      val.y *= nv;
+      if (norm) {  // the anti-aliasing function's inverse (use_aaf)
+        const double nv = norm[qy * qnx + qx];
+        val.x *= nv;
+        val.y *= nv;
+      }
     }
     const double sg = ((x + y) & 1) ? -1.0 : 1.0;
     pad[t] = make_double2(val.x * sg, val.y * sg);
@@ -232,8 +234,8 @@ extern "C" int arlgpu_make_pswf(int32_t oversampling, int32_t support, int32_t n
 }
 
 extern "C" int arlgpu_make_wkernels(int32_t nw, double wstep, int32_t oversampling, int32_t support,
-                                    int32_t maxsupport, int32_t image_nx, double cdelt_ra_deg, void *cf_out,
-                                    void *stream) {
+                                    int32_t maxsupport, int32_t image_nx, double cdelt_ra_deg, int32_t use_aaf,
+                                    void *cf_out, void *stream) {
   if (nw < 1 || oversampling < 1 || support < 2 || (support & 1) || image_nx < 2 || !cf_out)
     return fail(ARLGPU_ERR_INVALID, "bad w-kernel arguments");
   const int nx = maxsupport > 2 * oversampling * support ? maxsupport : 2 * oversampling * support;
@@ -245,15 +247,15 @@ extern "C" int arlgpu_make_wkernels(int32_t nw, double wstep, int32_t oversampli
   const double sub_cell = fabs(-ccell / d2r) * M_PI / 180.0;
   const double fov = qnx * sub_cell;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // norm = 1 / gcf_pswf(qnx) (kernels.py:153-155)
+  // norm = 1 / gcf_pswf(qnx) with use_aaf, else 1 (kernels.py:153-156)
   const int batch = 8;
   double *norm = nullptr, *scratch = nullptr;
   double2 *pad = nullptr;
   ARL_CUDA(cudaMallocAsync(&norm, (size_t)qnx * qnx * sizeof(double), st));
   ARL_CUDA(cudaMallocAsync(&scratch, (size_t)(qnx + 2) * sizeof(double), st));
   ARL_CUDA(cudaMallocAsync(&pad, (size_t)batch * nx * nx * sizeof(double2), st));
-  int rc = make_gcf(qnx, norm, scratch, st);
-  if (rc == ARLGPU_OK) {
+  int rc = use_aaf ? make_gcf(qnx, norm, scratch, st) : ARLGPU_OK;
+  if (rc == ARLGPU_OK && use_aaf) {
     k_recip<<<nblk((int64_t)qnx * qnx), 256, 0, st>>>((int64_t)qnx * qnx, norm);
   count_launch(1);
     cudaError_t e = cudaGetLastError();
@@ -267,7 +269,8 @@ extern "C" int arlgpu_make_wkernels(int32_t nw, double wstep, int32_t oversampli
   }
   for (int z0 = 0; rc == ARLGPU_OK && z0 < nw; z0 += batch) {
     const int nb = nw - z0 < batch ? nw - z0 : batch;
-    k_wscreen<<<nblk((int64_t)batch * nx * nx), 256, 0, st>>>(batch, z0, nw, wstep, qnx, nx, fov, norm, pad);
+    k_wscreen<<<nblk((int64_t)batch * nx * nx), 256, 0, st>>>(batch, z0, nw, wstep, qnx, nx, fov,
+                                                              use_aaf ? norm : nullptr, pad);
   count_launch(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -49,16 +49,33 @@ def normalize_sumwt(im, sumwt):
     return im
 
 
+def _reproject_uvw(uvw, old, new):
+    """uvw [..., 3] on the tangent plane of ``old`` re-expressed on that of
+    ``new``: ``uvw_to_xyz`` with (ha, dec) = (-ra, dec) of ``old``, then
+    ``xyz_to_uvw`` with those of ``new`` (``util/coordinate_support.py:59-113``),
+    each product and sum rounded on its own as there.  On the device."""
+    c0, s0 = float(numpy.cos(-old.ra_rad)), float(numpy.sin(-old.ra_rad))
+    cd0, sd0 = float(numpy.cos(old.dec_rad)), float(numpy.sin(old.dec_rad))
+    c1, s1 = float(numpy.cos(-new.ra_rad)), float(numpy.sin(-new.ra_rad))
+    cd1, sd1 = float(numpy.cos(new.dec_rad)), float(numpy.sin(new.dec_rad))
+    u, v, w = uvw[..., 0], uvw[..., 1], uvw[..., 2]
+    v0 = v * sd0 - w * cd0
+    z = v * cd0 + w * sd0
+    x = u * c0 + v0 * s0
+    y = -u * s0 + v0 * c0
+    v0 = x * s1 + y * c1
+    return torch.stack([x * c1 - y * s1, z * cd1 + v0 * sd1, z * sd1 - v0 * cd1], dim=-1)
+
+
 def phaserotate_visibility(vis, newphasecentre, tangent=True, inverse=False):
-    """``visibility/base.py:295-381`` on the tangent plane: a copy of ``vis``
-    whose rows are multiplied by conj(exp(-2 pi i (u l + v m + w (n - 1)))) (by
-    the phasor itself with ``inverse``), (l, m, n - 1) the direction cosines of
+    """``visibility/base.py:295-381``: a copy of ``vis`` whose rows are
+    multiplied by conj(exp(-2 pi i (u l + v m + w (n - 1)))) (by the phasor
+    itself with ``inverse``), (l, m, n - 1) the direction cosines of
     ``newphasecentre`` relative to ``vis.phasecentre``; ``vis`` itself when
-    |n - 1| < 1e-15.  Visibility, DeviceVisibility or BlockVisibility (per
-    channel uvw = metres x f / c).  The rotation runs on the GPU in FP64
-    phase.  ``tangent=False`` (re-projected uvw) raises NotImplementedError."""
-    if not tangent:
-        raise NotImplementedError('phaserotate_visibility: only tangent-plane rotation runs on the GB300 path')
+    |n - 1| < 1e-15.  With ``tangent=False`` the uvw are then re-projected onto
+    the new phase centre's tangent plane and the copy takes that phase centre.
+    Visibility, DeviceVisibility or BlockVisibility (per channel uvw = metres x
+    f / c).  Runs on the GPU in FP64."""
     l, m, n1 = newphasecentre.lmn(vis.phasecentre)
     if numpy.abs(n1) < 1e-15:
         return vis
@@ -67,8 +84,11 @@ def phaserotate_visibility(vis, newphasecentre, tangent=True, inverse=False):
         out = vis.vis.clone()
         nat.call('arlgpu_phaserotate', nat.ptr(out), nat.ptr(vis.uvw), vis.nvis, vis.npol,
                  nat.PRECISIONS[vis.precision], float(l), float(m), int(inverse), nat.stream_ptr())
-        return DeviceVisibility(vis.uvw, vis.frequency, out, vis.imaging_weight, vis.polarisation_frame,
-                                vis.phasecentre)
+        if tangent:
+            return DeviceVisibility(vis.uvw, vis.frequency, out, vis.imaging_weight, vis.polarisation_frame,
+                                    vis.phasecentre)
+        return DeviceVisibility(_reproject_uvw(vis.uvw, vis.phasecentre, newphasecentre).contiguous(),
+                                vis.frequency, out, vis.imaging_weight, vis.polarisation_frame, newphasecentre)
     if isinstance(vis, Visibility):
         newvis = copy_visibility(vis)
         v = dv.to_device(vis.vis, torch.complex128, device)
@@ -76,6 +96,9 @@ def phaserotate_visibility(vis, newphasecentre, tangent=True, inverse=False):
         nat.call('arlgpu_phaserotate', nat.ptr(v), nat.ptr(uvw), vis.nvis, vis.npol, nat.FP64, float(l), float(m),
                  int(inverse), nat.stream_ptr())
         newvis.data['vis'][...] = v.cpu().numpy()
+        if not tangent:
+            newvis.data['uvw'][...] = _reproject_uvw(uvw, vis.phasecentre, newphasecentre).cpu().numpy()
+            newvis.phasecentre = newphasecentre
         return newvis
     from .data_models import BlockVisibility, copy_blockvisibility
     from .skycomponents import C_M_S
@@ -89,6 +112,9 @@ def phaserotate_visibility(vis, newphasecentre, tangent=True, inverse=False):
     nat.call('arlgpu_phaserotate', nat.ptr(v), nat.ptr(uvw), uvw.shape[0], npol, nat.FP64, float(l), float(m),
              int(inverse), nat.stream_ptr())
     newvis.data['vis'][...] = v.cpu().numpy().reshape(vis.vis.shape)
+    if not tangent:
+        newvis.data['uvw'][...] = _reproject_uvw(buvw, vis.phasecentre, newphasecentre).cpu().numpy()
+        newvis.phasecentre = newphasecentre
     return newvis
 
 

@@ -106,14 +106,14 @@ def create_pswf_convolutionfunction(im, oversampling=8, support=6):
 
 def create_awterm_convolutionfunction(im, make_pb=None, nw=1, wstep=1e15, oversampling=8, support=6, use_aaf=True,
                                       maxsupport=512, plane_support=None):
-    """``kernels.py:100-200`` without a primary beam and with the anti-aliasing
-    function: the w-kernel stack [nchan, npol, nw, O, O, S, S] generated in FP64
-    on the GPU.  ``plane_support`` (optional, even values <= support) crops
-    plane z to its central plane_support[z] taps (see ``set_plane_support``)."""
+    """``kernels.py:100-200`` without a primary beam: the w-kernel stack
+    [nchan, npol, nw, O, O, S, S] generated in FP64 on the GPU, the w-screens
+    divided by the anti-aliasing function (use_aaf, the default; the returned
+    gcf is then the PSWF grid correction) or not (gcf all ones).
+    ``plane_support`` (optional, even values <= support) crops plane z to its
+    central plane_support[z] taps (see ``set_plane_support``)."""
     if make_pb is not None:
         raise NotImplementedError('primary-beam (A-term) kernels are outside the GB300 path')
-    if not use_aaf:
-        raise NotImplementedError('use_aaf=False is outside the GB300 path')
     assert isinstance(oversampling, int) and oversampling > 0
     nchan, npol, ony, onx = im.data.shape
     cf = create_convolutionfunction_from_image(im, oversampling=oversampling, support=support)
@@ -123,14 +123,17 @@ def create_awterm_convolutionfunction(im, make_pb=None, nw=1, wstep=1e15, oversa
     device = dv.require_cuda()
     t = torch.empty((nw, oversampling, oversampling, support, support), dtype=torch.complex128, device=device)
     nat.call('arlgpu_make_wkernels', nw, float(wstep), oversampling, support, maxsupport, onx,
-             float(im.wcs.wcs.cdelt[0]), nat.ptr(t), nat.stream_ptr())
+             float(im.wcs.wcs.cdelt[0]), int(bool(use_aaf)), nat.ptr(t), nat.stream_ptr())
     k = t.cpu().numpy()
     cf.data = numpy.broadcast_to(k[None, None], (nchan, npol) + k.shape).copy()
     if plane_support is not None:
         set_plane_support(cf, plane_support)
-    _, g = _pswf_on_device(1, 6, onx)
-    gcf = Image(numpy.broadcast_to(g.cpu().numpy(), (nchan, npol, ony, onx)).copy(), cf.projection_wcs.deepcopy(),
-                im.polarisation_frame)
+    if use_aaf:
+        _, g = _pswf_on_device(1, 6, onx)
+        gdata = numpy.broadcast_to(g.cpu().numpy(), (nchan, npol, ony, onx)).copy()
+    else:
+        gdata = numpy.ones((nchan, npol, ony, onx))
+    gcf = Image(gdata, cf.projection_wcs.deepcopy(), im.polarisation_frame)
     return gcf, cf
 
 

@@ -395,12 +395,13 @@ int arlgpu_msclean_setup(const double *dirty, int32_t nx, int32_t ny, const doub
 int arlgpu_make_pswf(int32_t oversampling, int32_t support, int32_t ny, int32_t nx,
                      void *cf_out, double *gcf_out, void *stream);
 
-/* ---- a9: create_awterm_convolutionfunction without primary beam, use_aaf=True
+/* ---- a9: create_awterm_convolutionfunction without primary beam
  * (griddata/kernels.py:100-200), FP64 ----
  * cf_out: [nw][O][O][S][S] complex128; image_nx / cdelt_ra_deg describe the image
- * template; maxsupport as in ARL (512). */
+ * template; maxsupport as in ARL (512); use_aaf != 0 divides the w-screens by the
+ * PSWF grid correction of the padded sub-image (ARL's default), 0 leaves them as they are. */
 int arlgpu_make_wkernels(int32_t nw, double wstep, int32_t oversampling, int32_t support,
-                         int32_t maxsupport, int32_t image_nx, double cdelt_ra_deg,
+                         int32_t maxsupport, int32_t image_nx, double cdelt_ra_deg, int32_t use_aaf,
                          void *cf_out, void *stream);
 
 /* ---- a17: apply_gaintable, scalar gains (calibration/operations.py:134-137) ----

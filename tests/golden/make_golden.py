@@ -211,6 +211,16 @@ def case_kernels(out):
                            wker=cfw.data[0, 0], bbox=numpy.array([[b[0], *b[1], *b[2]] for b in bb]))
 
 
+def case_wkernels_noaaf(out):
+    """``create_awterm_convolutionfunction(use_aaf=False)`` (``processing_components/
+    griddata/kernels.py:100-200``): w-screens not divided by the anti-aliasing
+    function, and an all-ones grid correction."""
+    im = make_image(256, 0.001, numpy.array([1e8]), 1e6, 'stokesI')
+    gcf, cfw = kernels.create_awterm_convolutionfunction(im, nw=5, wstep=20.0, oversampling=4, support=8,
+                                                         use_aaf=False, maxsupport=128)
+    numpy.savez_compressed(out, gcf=gcf.data[0, 0], wker=cfw.data[0, 0])
+
+
 def case_weighting(out):
     """grid_weight_to_griddata and weight_visibility (uniform weighting,
     ``processing_components/griddata/gridding.py:161-230``,
@@ -427,6 +437,31 @@ def case_msmfsclean(out):
     numpy.savez_compressed(out, **res)
 
 
+def case_rotate_uvw(out):
+    """``phaserotate_visibility(tangent=False)`` (``processing_components/visibility/
+    base.py:295-343``) forward and inverse on the phase-rotation rows of
+    ``ref_rowops``: the phases as on the tangent plane, then uvw re-projected
+    through earth coordinates (``uvw_to_xyz`` / ``xyz_to_uvw``,
+    ``processing_library/util/coordinate_support.py:59-113``) and the phase
+    centre moved."""
+    from processing_components.visibility.base import phaserotate_visibility
+    d = numpy.load(os.path.join(OUT, 'ref_rowops.npz'))
+    uvw, vis = d['rot_uvw'], d['rot_vis']
+    n = uvw.shape[0]
+    z = numpy.zeros(n)
+    res = {}
+    for tag, inverse in (('fwd', False), ('inv', True)):
+        v = Visibility(uvw=uvw.copy(), time=z, frequency=z + 1e8, channel_bandwidth=z + 1e6, vis=vis.copy(),
+                       weight=z[:, None] + 1.0, imaging_weight=z[:, None] + 1.0, integration_time=z + 1.0,
+                       antenna1=z.astype(int), antenna2=z.astype(int), polarisation_frame=PolarisationFrame('stokesIQ'))
+        v.phasecentre = SkyCoord(*d['rot_vis_pc'])
+        r = phaserotate_visibility(v, SkyCoord(*d['rot_far_pc']), tangent=False, inverse=inverse)
+        res['vis_' + tag] = r.vis.copy()
+        res['uvw_' + tag] = r.uvw.copy()
+        res['pc_' + tag] = numpy.array([r.phasecentre.ra.deg, r.phasecentre.dec.deg])
+    numpy.savez_compressed(out, **res)
+
+
 def case_rowops(out):
     """Row operations on the path's edges, from the reference's own code:
 
@@ -611,6 +646,7 @@ ALL_CASES = {
     'ref_wproj_2chan_2pol': case_wproj_2chan_2pol,
     'ref_wstack': case_wstack,
     'ref_kernels': case_kernels,
+    'ref_wkernels_noaaf': case_wkernels_noaaf,
     'ref_weighting': case_weighting,
     'ref_blocks': case_blocks,
     'ref_hogbom': case_hogbom,
@@ -618,6 +654,7 @@ ALL_CASES = {
     'ref_msclean': case_msclean,
     'ref_msmfsclean': case_msmfsclean,
     'ref_rowops': case_rowops,
+    'ref_rotate_uvw': case_rotate_uvw,
     'ref_api': case_api,
 }
 

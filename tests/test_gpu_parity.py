@@ -200,6 +200,17 @@ def test_kernels_match_reference(arl, golden):
     assert numpy.array_equal(numpy.array([[b[0], *b[1], *b[2]] for b in bb]), d['bbox'])
 
 
+def test_wkernels_without_aaf_match_reference(arl, golden):
+    """create_awterm_convolutionfunction(use_aaf=False): the w-screens without
+    the anti-aliasing function's inverse, and an all-ones gcf."""
+    d = golden('ref_wkernels_noaaf.npz')
+    im = make_image(arl, 256, 0.001, [1e8], 1e6)
+    gcf, cfw = arl.create_awterm_convolutionfunction(im, nw=5, wstep=20.0, oversampling=4, support=8, use_aaf=False,
+                                                     maxsupport=128)
+    assert rel(cfw.data[0, 0], d['wker']) < 1e-12
+    assert numpy.array_equal(gcf.data[0, 0], d['gcf'])
+
+
 # ---------------------------------------------------------------------------
 # Oracle parity on cases the fixtures do not cover
 # ---------------------------------------------------------------------------

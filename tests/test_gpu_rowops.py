@@ -88,6 +88,33 @@ def test_phase_rotation_matches_reference(arl, golden):
     assert rel(dfwd.vis.to(torch.complex128).cpu().numpy(), d['rot_fwd']) < 1e-6
 
 
+@pytest.mark.parametrize('inverse', [False, True])
+def test_phase_rotation_off_tangent_matches_reference(arl, golden, inverse):
+    """phaserotate_visibility(tangent=False) to a far phase centre: phases as on
+    the tangent plane (FP64 1e-10, as above), uvw re-projected through earth
+    coordinates (1e-13) and the new phase centre, against the reference's
+    results; a DeviceVisibility gets the same uvw."""
+    d = golden('ref_rowops.npz')
+    g = golden('ref_rotate_uvw.npz')
+    tag = 'inv' if inverse else 'fwd'
+    frame = arl.PolarisationFrame('stokesIQ')
+    n = d['rot_uvw'].shape[0]
+    vis = arl.Visibility(uvw=d['rot_uvw'], frequency=numpy.full(n, 1e8), vis=d['rot_vis'].copy(),
+                         weight=numpy.ones((n, 2)), polarisation_frame=frame)
+    vis.phasecentre = arl.PhaseCentre(*d['rot_vis_pc'])
+    new = arl.PhaseCentre(*d['rot_far_pc'])
+    out = arl.phaserotate_visibility(vis, new, tangent=False, inverse=inverse)
+    assert rel(out.vis, g['vis_' + tag]) < 1e-10
+    assert rel(out.uvw, g['uvw_' + tag]) < 1e-13
+    assert (out.phasecentre.ra_deg, out.phasecentre.dec_deg) == tuple(g['pc_' + tag])
+    assert numpy.array_equal(vis.uvw, d['rot_uvw'])  # the input is not modified
+    dvis = arl.DeviceVisibility.from_visibility(vis, 'fp64')
+    dvis.phasecentre = vis.phasecentre
+    dout = arl.phaserotate_visibility(dvis, new, tangent=False, inverse=inverse)
+    assert rel(dout.uvw.cpu().numpy(), g['uvw_' + tag]) < 1e-13
+    assert rel(dout.vis.cpu().numpy(), g['vis_' + tag]) < 1e-10
+
+
 @pytest.mark.parametrize('precision,tol', [('fp64', 1e-10), ('fp32c', 1e-6)])
 def test_skycomponents_match_reference(arl, golden, precision, tol):
     """predict_skycomponent_visibility on rows (3 channels, 2 polarisations) and
