@@ -195,6 +195,67 @@ def case_wstack(out):
                            model=model, predict=pvis.vis, dirty_nonorm=dirty_nn.data, sumwt_nonorm=sumwt_nn)
 
 
+def case_workflow_trace(out):
+    """The reference's serial workflows (``workflows/serial/imaging/imaging_serial.py:
+    41-216``) with context 'wstack' on the ``ref_wstack`` rows, their imaging
+    context (``workflows/shared/imaging/imaging_shared.py:21-94``) wrapped so
+    that every call the workflow makes is recorded: the row masks its
+    vis_iterator yields, each invert's keyword arguments and (image, sumwt),
+    each predict's rows.  A test replays the same calls through the package's
+    own context functions."""
+    from workflows.serial.imaging import imaging_serial
+    d = numpy.load(os.path.join(OUT, 'ref_wstack.npz'))
+    N, K = int(d['N']), int(d['K'])
+    im = make_image(N, float(d['cell']), numpy.array([float(d['freq0'])]), float(d['dfreq']), 'stokesI')
+    gcfcf = kernels.create_pswf_convolutionfunction(im, oversampling=int(d['O']), support=int(d['S']))
+    n = d['uvw'].shape[0]
+    z = numpy.zeros(n)
+    vis = Visibility(uvw=d['uvw'], time=z, frequency=d['frequency'], channel_bandwidth=z + float(d['dfreq']),
+                     vis=d['vis'].copy(), weight=d['wt'], imaging_weight=d['wt'], integration_time=z + 1.0,
+                     antenna1=z.astype(int), antenna2=z.astype(int), polarisation_frame=PolarisationFrame('stokesI'))
+    vis.phasecentre = im.phasecentre
+    model = create_image_from_array(d['model'], im.wcs, im.polarisation_frame)
+    calls = {'masks': [], 'inv_img': [], 'inv_sw': [], 'inv_kw': [], 'pred': []}
+    original = imaging_serial.imaging_context
+
+    def traced(context):
+        c = dict(original(context))
+        inv, pred, it = c['invert'], c['predict'], c['vis_iterator']
+
+        def vis_iterator(v, vis_slices=1):
+            for rows in it(v, vis_slices):
+                calls['masks'].append(numpy.array(rows, dtype=bool))
+                yield rows
+
+        def invert(v, model_im, dopsf=False, normalize=True, **kw):
+            r = inv(v, model_im, dopsf=dopsf, normalize=normalize, **kw)
+            calls['inv_img'].append(r[0].data.copy())
+            calls['inv_sw'].append(numpy.array(r[1]))
+            calls['inv_kw'].append([int(dopsf), int(normalize)])
+            return r
+
+        def predict(v, model_im, **kw):
+            r = pred(v, model_im, **kw)
+            calls['pred'].append(r.vis.copy())
+            return r
+        c.update(invert=invert, predict=predict, vis_iterator=vis_iterator)
+        return c
+    imaging_serial.imaging_context = traced
+    try:
+        (dirty, sumwt), = imaging_serial.invert_list_serial_workflow([vis], [im], context='wstack', vis_slices=K,
+                                                                     gcfcf=[gcfcf])
+        (psf, _), = imaging_serial.invert_list_serial_workflow([vis], [im], context='wstack', vis_slices=K,
+                                                               dopsf=True, normalize=False, gcfcf=[gcfcf])
+        (pv,) = imaging_serial.predict_list_serial_workflow([vis], [model], context='wstack', vis_slices=K,
+                                                            gcfcf=[gcfcf])
+    finally:
+        imaging_serial.imaging_context = original
+    numpy.savez_compressed(out, masks=numpy.array(calls['masks']), inv_img=numpy.array(calls['inv_img']),
+                           inv_sw=numpy.array(calls['inv_sw']), inv_kw=numpy.array(calls['inv_kw']),
+                           pred=numpy.concatenate(calls['pred']), pred_len=numpy.array([len(p) for p in calls['pred']]),
+                           dirty=dirty.data, sumwt=sumwt, psf=psf.data, predict=pv.vis)
+
+
 def case_kernels(out):
     """Kernel values of the reference's kernel tests
     (``tests/processing_components/test_griddata_kernels.py:33-139``) plus a small
@@ -645,6 +706,7 @@ ALL_CASES = {
     'ref_2d_pswf': case_2d_pswf,
     'ref_wproj_2chan_2pol': case_wproj_2chan_2pol,
     'ref_wstack': case_wstack,
+    'ref_workflow_trace': case_workflow_trace,
     'ref_kernels': case_kernels,
     'ref_wkernels_noaaf': case_wkernels_noaaf,
     'ref_weighting': case_weighting,

@@ -60,6 +60,50 @@ def test_wstack_workflow_unnormalised_matches_reference(arl, golden, precision):
 
 
 @pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
+def test_reference_workflow_calls_replayed(arl, golden, precision):
+    """The reference's serial 'wstack' workflows (invert normalised, invert of the
+    PSF unnormalised, predict) had every call into their imaging context
+    recorded (tests/golden/ref_workflow_trace.npz).  Replayed through this
+    package's own imaging_contexts()['wstack']: its vis_iterator yields the
+    same row masks, and each invert / predict called with the workflow's
+    arguments on those rows returns the reference's (image, sumwt) and rows;
+    the workflow's assembly of those results gives the reference's dirty
+    image and predicted visibilities."""
+    d = golden('ref_wstack.npz')
+    t = golden('ref_workflow_trace.npz')
+    im, gcf, cf, vis = _case(arl, d)
+    K = int(d['K'])
+    ctx = arl.imaging_contexts()['wstack']
+    masks = [numpy.asarray(m) for m in ctx['vis_iterator'](vis, K)]
+    assert all(numpy.array_equal(m, t['masks'][k]) for k, m in enumerate(masks))
+    assert numpy.array_equal(t['masks'][:K], t['masks'][K:2 * K])
+    acc = numpy.zeros_like(t['dirty'])
+    total = numpy.zeros_like(t['sumwt'])
+    for k in range(2 * K):
+        row_vis = arl.data_models.create_visibility_from_rows(vis, t['masks'][k])
+        dopsf, normalize = (bool(x) for x in t['inv_kw'][k])
+        img, sw = ctx['invert'](row_vis, im, dopsf=dopsf, normalize=normalize, context='wstack', gcfcf=(gcf, cf),
+                                precision=precision)
+        assert_image(img.data, t['inv_img'][k], d['gcf'], precision)
+        assert numpy.allclose(sw, t['inv_sw'][k], rtol=1e-12 if precision == 'fp64' else 1e-6)
+        if k < K:
+            acc += sw[:, :, None, None] * img.data
+            total += sw
+    dirty = arl.normalize_sumwt(arl.create_image_from_array(acc, im.wcs, im.polarisation_frame), total)
+    assert_image(dirty.data, t['dirty'], d['gcf'], precision)
+    model = arl.create_image_from_array(d['model'], im.wcs, im.polarisation_frame)
+    pv = numpy.zeros_like(t['predict'])
+    start = numpy.concatenate([[0], numpy.cumsum(t['pred_len'])])
+    for j in range(K):
+        mask = t['masks'][2 * K + j]
+        row_vis = arl.data_models.create_visibility_from_rows(vis, mask)
+        out = ctx['predict'](row_vis, model, context='wstack', gcfcf=(gcf, cf), precision=precision)
+        assert rel(out.vis, t['pred'][start[j]:start[j + 1]]) < TOL[precision]
+        pv[mask] = out.vis
+    assert rel(pv, t['predict']) < TOL[precision]
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32c'])
 def test_wstack_single_matches_oracle(arl, oracle, golden, precision):
     d = golden('ref_wstack.npz')
     im, gcf, cf, vis = _case(arl, d)
