@@ -196,3 +196,19 @@ def test_clean_windows_and_psf_crop(arl):
     assert psf.data.shape == (1, 1, 8, 8) and numpy.array_equal(psf.data, full[..., 4:12, 2:10])
     dc.crop_psf_to_support(psf, 5)  # larger than half the cropped PSF: unchanged
     assert psf.data.shape == (1, 1, 8, 8)
+
+
+def test_uvw_reprojection_matches_reference(arl, golden):
+    """phaserotate_visibility(tangent=False)'s uvw re-projection through earth
+    coordinates (coordinate_support.py:59-113), on the CPU: the reference's
+    rotated uvw for the phase-rotation rows, forward and inverse (the same
+    rotation: both move the rows to the new phase centre's tangent plane)."""
+    import numpy
+    import torch
+    d = golden('ref_rowops.npz')
+    g = golden('ref_rotate_uvw.npz')
+    old, new = arl.PhaseCentre(*d['rot_vis_pc']), arl.PhaseCentre(*d['rot_far_pc'])
+    got = arl.imaging._reproject_uvw(torch.as_tensor(d['rot_uvw']), old, new).numpy()
+    for tag in ('fwd', 'inv'):
+        want = g['uvw_' + tag]
+        assert numpy.max(numpy.abs(got - want)) <= 1e-13 * numpy.max(numpy.abs(want))
