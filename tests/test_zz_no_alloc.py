@@ -4,7 +4,8 @@ real-time code that allocates only at start-up).  Called through the C ABI
 and checked against arlgpu_grid, which grids the same rows with a
 caller-provided workspace.  The shared scratch array keeps the previous
 call's plan, so the check runs after a call on a different case (more rows,
-other uv values, a larger grid with more bins), and twice in a row.
+other uv values, a larger grid with more bins), twice in a row, and as a
+CUDA graph recorded once and replayed.
 
 Kept in a file that pytest collects last, so a failure here cannot stop the
 rest of the suite from running first."""
@@ -105,6 +106,46 @@ def test_noalloc_matches_workspace_gridder_twice(case, other_case):
         # the order of the atomic additions
         assert numpy.max(numpy.abs(got - ref)) / numpy.max(numpy.abs(ref)) < 1e-5
         assert numpy.allclose(sw, ref_sw, rtol=1e-12)
+
+
+def test_noalloc_replays_in_a_cuda_graph(case, other_case):
+    """Recorded once under stream capture (no allocation may happen there)
+    and replayed twice, with another case gridded in between: each replay
+    rebuilds its plan in the shared scratch and gives the workspace result."""
+    arl, t, gd, cd, cf_t, n = case
+    nat = arl._native
+    lib = nat.load()
+    dev = t['uvw'].device
+    ref, ref_sw, _ = _grid(arl, t, gd, cd, cf_t, n, noalloc=False)
+    grid = torch.empty((gd.nchan, gd.npol, gd.nw, gd.ny, gd.nx), dtype=torch.complex64, device=dev)
+    sumwt = torch.empty((gd.nchan, gd.npol), dtype=torch.float64, device=dev)
+    nbad = torch.empty((1,), dtype=torch.int64, device=dev)
+
+    def call():
+        nat.check(lib.arlgpu_grid_noalloc(nat.ptr(t['uvw']), nat.ptr(t['freq']), nat.ptr(t['vis']), nat.ptr(t['wt']),
+                                          n, nat.FP32C, nat.ptr(cf_t), ctypes.byref(cd), nat.ptr(grid),
+                                          ctypes.byref(gd), nat.ptr(sumwt), nat.ptr(nbad), nat.stream_ptr()))
+
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        call()  # scratch address and kernel attributes set up before capture
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        call()
+    for _ in range(2):
+        _grid(*other_case, noalloc=True)  # another plan left in the scratch
+        grid.fill_(7.0)
+        sumwt.fill_(7.0)
+        nbad.fill_(7)
+        g.replay()
+        torch.cuda.synchronize()
+        got = grid.to(torch.complex128).cpu().numpy()
+        assert int(nbad.item()) == 0
+        assert numpy.max(numpy.abs(got - ref)) / numpy.max(numpy.abs(ref)) < 1e-5
+        assert numpy.allclose(sumwt.cpu().numpy(), ref_sw, rtol=1e-12)
 
 
 def test_noalloc_rejects_oversize_calls(case):
