@@ -2419,6 +2419,9 @@ int plan_carve(void *ws, size_t bytes, int64_t nvis, const Geom &g, PlanBufs *b)
   size_t need = plan_bytes(nvis, g);
   if (!ws || bytes < need)
     return fail(ARLGPU_ERR_WORKSPACE, "workspace of %zu bytes is smaller than the %zu needed", bytes, need);
+  // the row maps move as 128-bit loads and stores
+  if (reinterpret_cast<uintptr_t>(ws) & 15)
+    return fail(ARLGPU_ERR_INVALID, "workspace must start on a 16-byte boundary");
   char *p = static_cast<char *>(ws);
   size_t n = (size_t)nvis;
   b->keys = reinterpret_cast<uint32_t *>(p);

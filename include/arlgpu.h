@@ -13,7 +13,10 @@
  *     Work is enqueued asynchronously; results are valid once the stream has
  *     been synchronised.
  *   - Scratch memory comes from the caller through `workspace` /
- *     `workspace_bytes`, sized by arlgpu_plan_workspace_bytes().
+ *     `workspace_bytes`, sized by arlgpu_plan_workspace_bytes().  A plan
+ *     workspace starts on a 16-byte boundary (cudaMalloc and the PyTorch
+ *     allocator give 256); an unaligned one is rejected with
+ *     ARLGPU_ERR_INVALID before any GPU work.
  *   - Array layouts are ARL's (row-major, C order):
  *       uvw        [nvis][3]            float64, wavelengths
  *       frequency  [nvis]               float64, Hz
