@@ -98,6 +98,12 @@ def test_plan_build_rejects_bad_rows_and_workspace(nat, descs):
     # workspace too small (checked before any device access)
     assert lib.arlgpu_plan_build(ptr, ptr, 100, ctypes.byref(g), ctypes.byref(c), ptr, need - 1, None, None) == WORKSPACE
     assert 'workspace' in last_error(nat)
+    # workspace off a 16-byte boundary (the row maps move as 128-bit accesses)
+    big = ctypes.create_string_buffer(need + 64)
+    base = ctypes.addressof(big)
+    odd = ctypes.c_void_p(base + (16 - base % 16) % 16 + 4)
+    assert lib.arlgpu_plan_build(ptr, ptr, 100, ctypes.byref(g), ctypes.byref(c), odd, need, None, None) == INVALID
+    assert '16-byte' in last_error(nat)
     # bad precision on the gridding entry point
     assert lib.arlgpu_grid_planned(ptr, ptr, 100, 7, ptr, ctypes.byref(c), ptr, ctypes.byref(g), None, ptr, need,
                                    None) == INVALID
