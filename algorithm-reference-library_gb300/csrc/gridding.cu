@@ -1262,7 +1262,10 @@ __global__ void k_gather_rows(const uint32_t *__restrict__ sidx, const uint32_t 
 // in a second integer plane.  A flushed cell is (sum + residual sum 2^-f) 2^-e,
 // formed with one FMA: the sum of the FP32 contributions to within 2^-f-1 of a
 // unit per contribution (about 2^-42 of the segment's largest contribution for
-// segments of up to 512 rows) plus the final FP32 rounding.  Without RESID
+// segments of up to 512 rows) plus the final FP32 rounding.  With biased raw
+// sums (fx_add, the default instantiations) f = min(20, 21 - ceil(log2 rows)):
+// 2^-34 of the largest contribution for 512 rows, still 2^-10 of the FP32
+// rounding of that contribution itself.  Without RESID
 // (grid_kernel 5, measurement only) each contribution carries a quantisation
 // error of up to half a unit, 2^-e-1.
 // int32 -> FP32 with round-to-nearest, without the conversion instruction
@@ -1275,18 +1278,39 @@ __device__ __forceinline__ float i2f_rn(int q) {
   return fmaf(fh, 65536.0f, fl);
 }
 
-template <bool RESID>
+// BIASED (with RESID, segments of at most 512 rows): each atomic adds the
+// rounded value's float bit pattern itself, kFxBias + q, instead of q, which
+// saves one integer subtraction per atomic (four per tap).  Every tap adds to
+// all the planes of its cell, so each raw cell sum is n kFxBias + (its sum),
+// modulo 2^32, with n the number of taps the cell took, the same for every
+// plane of the cell.  The flush recovers n from the real residual plane:
+// kFxBias = 301 * 2^22, so n kFxBias only touches bits 22-31, where it is
+// 2^22 (301 n mod 1024); with the residual unit chosen so that the plane's
+// true sum stays below 2^20 in magnitude, the low 22 bits of the raw sum are
+// that true sum (sign-extended), the high 10 bits are 301 n mod 1024, and
+// n = 677 * (those bits) mod 1024 (677 = 301^-1 mod 1024; n <= 512).  A raw
+// residual sum of zero means n = 0: the cell took no tap.
+constexpr uint32_t kFxBias = 0x4B400000u;  // bit pattern of 1.5 * 2^23
+constexpr uint32_t kFxBiasInv = 677u;      // inverse of 301 modulo 2^10
+
+template <bool RESID, bool BIASED = false>
 __device__ __forceinline__ void fx_add(int *q, int *r, float x, float scale, float rscale) {
   const float t = fmaf(x, scale, 12582912.0f);
-  atomicAdd(q, __float_as_int(t) - 0x4B400000);
+  atomicAdd(q, BIASED ? __float_as_int(t) : __float_as_int(t) - 0x4B400000);
   if (RESID) {
     // residual x * scale - round(x * scale), |.| <= 1/2, as a second limb in
     // units of 1 / rscale: |limb| <= rscale / 2 <= 2^19, and a cell's sum of
-    // limbs stays below 2^29 (rscale <= 2^30 / rows)
+    // limbs stays below 2^29 (rscale <= 2^30 / rows; 2^20 when BIASED)
     const float rs = fmaf(x, scale, 12582912.0f - t);
     const float t2 = fmaf(rs, rscale, 12582912.0f);
-    atomicAdd(r, __float_as_int(t2) - 0x4B400000);
+    atomicAdd(r, BIASED ? __float_as_int(t2) : __float_as_int(t2) - 0x4B400000);
   }
+}
+
+// Tap count n of a cell from its raw real-residual sum (BIASED sums).
+__device__ __forceinline__ uint32_t fx_taps(uint32_t raw_r) {
+  const int low = (int)(raw_r << 10) >> 10;  // the plane's true sum
+  return (((raw_r - (uint32_t)low) >> 22) * kFxBiasInv) & 1023u;
 }
 
 template <int NPOL, int NW, bool RESID, int LPR = 0, int SGC = 0, bool SORTED = false, bool STASH = false>
@@ -1308,6 +1332,8 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
   int *subq = reinterpret_cast<int *>(smraw);
   int *subr = subq + (size_t)2 * NPOL * SG2;
   constexpr int kPlanes = RESID ? 4 * NPOL : 2 * NPOL;
+  // Biased raw sums (fx_add): segments of at most kStashRows rows.
+  constexpr bool BIASED = RESID && STASH;
   unsigned char *tab = smraw + (size_t)kPlanes * SG2 * 4;
   const uint32_t nvalid = off[g.nbins];
   // Chunks of sorted rows: chunk blockIdx.x, then every gridDim.x-th after it
@@ -1353,7 +1379,8 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         inv = ldexpf(1.f, 1 - e);
       }
       const int lr = 32 - __clz((int)rows - 1);  // ceil(log2(rows))
-      const int f = min(20, 30 - lr);
+      // a cell's residual sum: at most rows * rscale / 2 = 2^(lr + f - 1)
+      const int f = min(20, (BIASED ? 21 : 30) - lr);
       rscale = ldexpf(1.f, f);
       rinv = ldexpf(1.f, -f);
     }
@@ -1479,8 +1506,9 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
               for (int p = 0; p < NPOL; ++p) {
                 const float cx = tp[p][u].x * vw[p].x + tp[p][u].y * vw[p].y;  // conj(tap) * vw
                 const float cy = tp[p][u].x * vw[p].y - tp[p][u].y * vw[p].x;
-                fx_add<RESID>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
-                fx_add<RESID>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale, rscale);
+                fx_add<RESID, BIASED>(subq + 2 * p * SG2 + so, subr + 2 * p * SG2 + so, cx, scale, rscale);
+                fx_add<RESID, BIASED>(subq + (2 * p + 1) * SG2 + so, subr + (2 * p + 1) * SG2 + so, cy, scale,
+                                      rscale);
               }
             }
           };
@@ -1527,19 +1555,29 @@ k_grid_fx(Geom g, const RowMap *__restrict__ smap, const uint32_t *__restrict__ 
         const int gy = sg.v0 + y;
         for (int x = box.x0 + lane; x < box.x1; x += 32) {
           const int gx = sg.u0 + x, cell = y * SP + x;
+          uint32_t bias = 0;  // BIASED: n kFxBias, carried by every raw sum of the cell
+          if constexpr (BIASED) {
+            const uint32_t raw = (uint32_t)subr[cell];
+            if (raw == 0u) continue;  // no tap: every plane of the cell is zero
+            bias = fx_taps(raw) * kFxBias;
+          }
 #pragma unroll
           for (int p = 0; p < NPOL; ++p) {
-            const int qx = subq[2 * p * SG2 + cell], qy = subq[(2 * p + 1) * SG2 + cell];
-            const int rx = RESID ? subr[2 * p * SG2 + cell] : 0;
-            const int ry = RESID ? subr[(2 * p + 1) * SG2 + cell] : 0;
-            if (qx == 0 && qy == 0 && rx == 0 && ry == 0) continue;
+            const int qx = (int)((uint32_t)subq[2 * p * SG2 + cell] - bias);
+            const int qy = (int)((uint32_t)subq[(2 * p + 1) * SG2 + cell] - bias);
+            const int rx = RESID ? (int)((uint32_t)subr[2 * p * SG2 + cell] - bias) : 0;
+            const int ry = RESID ? (int)((uint32_t)subr[(2 * p + 1) * SG2 + cell] - bias) : 0;
+            // an untouched cell's planes are already zero; a touched cell's
+            // raw sums (BIASED) are cleared even where its true sums are zero
+            const bool zero = qx == 0 && qy == 0 && rx == 0 && ry == 0;
+            if (zero && !BIASED) continue;
             subq[2 * p * SG2 + cell] = 0;
             subq[(2 * p + 1) * SG2 + cell] = 0;
             if (RESID) {
               subr[2 * p * SG2 + cell] = 0;
               subr[(2 * p + 1) * SG2 + cell] = 0;
             }
-            if (gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
+            if (zero || gy < 0 || gy >= g.ny || gx < 0 || gx >= g.nx) continue;
             // inv and rinv * inv are powers of two: one rounding in the FMA
             // (and in the int -> float conversions of sums beyond 2^24)
             float2 val;

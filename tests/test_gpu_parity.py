@@ -214,12 +214,15 @@ def test_wkernels_without_aaf_match_reference(arl, golden):
 # ---------------------------------------------------------------------------
 # Oracle parity on cases the fixtures do not cover
 # ---------------------------------------------------------------------------
-def _random_case(arl, oracle, rng, N, cell, O, S, nvis, nchan=1, npol=1, nz=1, zstep=1e15, distinct_chan=False):
+def _random_case(arl, oracle, rng, N, cell, O, S, nvis, nchan=1, npol=1, nz=1, zstep=1e15, distinct_chan=False,
+                 lim_px=None):
+    """Random rows, weights and cf taps; uv uniform over the grid, or within
+    +/- lim_px pixels of its centre."""
     freqs = 1e8 + 1e7 * numpy.arange(nchan)
     pf = {1: 'stokesI', 2: 'stokesIQ', 4: 'stokesIQUV'}[npol]
     im = make_image(arl, N, cell, freqs, 1e7, pf)
     du = abs(1.0 / (N * cell))
-    lim = (N // 2 - S // 2 - 2) * du
+    lim = ((N // 2 - S // 2 - 2) if lim_px is None else lim_px) * du
     uvw = numpy.stack([rng.uniform(-lim, lim, nvis), rng.uniform(-lim, lim, nvis),
                        rng.uniform(-0.45 * nz * zstep, 0.45 * nz * zstep, nvis) if nz > 1 else
                        rng.uniform(-50, 50, nvis)], axis=1)
@@ -579,6 +582,22 @@ def test_bin_order_rows_vs_oracle(arl, oracle, gather_rows, persistent, stash_ro
         assert rel(out.to(torch.complex128).cpu().numpy(), oracle.degrid_vec(g_ref, maps, cf.data)) < TOL['fp32c']
     finally:
         arl.tune.set_tuning(**before)
+
+
+@pytest.mark.parametrize('S,npol', [(8, 1), (12, 1), (8, 4)])
+def test_dense_cells_vs_oracle(arl, oracle, S, npol):
+    """30,000 rows within 1.5 pixels of the grid centre: every segment is a
+    full chunk of 512 rows and the cells under it take up to 512 taps each,
+    the most the fixed-point gridder's biased cell sums carry (the tap count
+    comes back from the residual plane's high bits).  Held to 1e-6, ten times
+    tighter than the other FP32C grid checks."""
+    rng = numpy.random.default_rng(71 + S + npol)
+    im, cf, vis, maps, gax = _random_case(arl, oracle, rng, 64, 4e-3, 8, S, 30000, 1, npol, lim_px=1.5)
+    g_ref, sw_ref = oracle.grid_vec(vis.vis, vis.imaging_weight, maps, cf.data, gax['shape'])
+    gd = arl.create_griddata_from_image(im)
+    gd, sw = arl.grid_visibility_to_griddata(vis, gd, cf, precision='fp32c')
+    assert rel(gd.data, g_ref) < 1e-6
+    assert rel(sw, sw_ref) < TOLW['fp32c']
 
 
 def _degrid_planned_with_flags(arl, vis, gd_h, cf, precision='fp32c'):
