@@ -32,13 +32,24 @@ template <> struct Cplx<double> { using T = double2; };
 //   pu, pv : nearest grid pixel (ARL pu_grid / pv_grid)
 //   sub    : pu_off | pv_off << 8 | pwc << 16
 //   cz     : pfreq | pwg << 16
-// 16-byte aligned, so that a row's map moves as one 128-bit load or store:
-// the plan's scatter writes each row's map to a random place in bin order,
-// and four 32-bit stores there cost four L2 requests instead of one.
-struct __align__(16) RowMap {
+struct RowMap {
   int32_t pu, pv;
   uint32_t sub, cz;
 };
+
+// 128-bit copies of a row map, for the plan kernels: the scatter writes each
+// row's map to a random slot in bin order, where four 32-bit stores cost four
+// L2 requests instead of one.  The plan's arrays start on 16-byte boundaries
+// (the workspace must), so every element is 16-byte aligned.  The gridding
+// kernels keep plain struct loads: 128-bit loads there made the degridder's
+// four-rows-per-warp variant 7 % slower on C5.
+__device__ __forceinline__ RowMap ld_map16(const RowMap *p) {
+  const uint4 v = *reinterpret_cast<const uint4 *>(p);
+  return RowMap{(int32_t)v.x, (int32_t)v.y, v.z, v.w};
+}
+__device__ __forceinline__ void st_map16(RowMap *p, const RowMap &m) {
+  *reinterpret_cast<uint4 *>(p) = make_uint4((uint32_t)m.pu, (uint32_t)m.pv, m.sub, m.cz);
+}
 
 // Geometry handed to the device kernels by value.
 // Row pitch of the fixed-point gridder's shared-memory subgrid.  An edge that

@@ -81,7 +81,7 @@ __global__ void k_map(const double *__restrict__ uvw, const double *__restrict__
       rm.sub = (uint32_t)m.uf | ((uint32_t)m.vf << 8) | ((uint32_t)m.zc << 16);
       rm.cz = (uint32_t)m.ch | ((uint32_t)m.zg << 16);
       key = m.ok ? bin_of(m.ch, m.zg, m.pu, m.pv, g) : g.nbins;
-      maps[r] = rm;
+      st_map16(maps + r, rm);
       keys[r] = key;
     }
     // Warp-aggregated histogram increment.
@@ -235,7 +235,7 @@ __global__ void k_scatter(const uint32_t *__restrict__ keys, const RowMap *__res
     if (key != 0xffffffffu) {
       uint32_t pos = off[key] + start + __popc(same & ((1u << lane) - 1u));
       sidx[pos] = (uint32_t)r;
-      smap[pos] = maps[r];
+      st_map16(smap + pos, ld_map16(maps + r));
     }
   }
 }
@@ -2457,7 +2457,7 @@ int plan_carve(void *ws, size_t bytes, int64_t nvis, const Geom &g, PlanBufs *b)
   size_t need = plan_bytes(nvis, g);
   if (!ws || bytes < need)
     return fail(ARLGPU_ERR_WORKSPACE, "workspace of %zu bytes is smaller than the %zu needed", bytes, need);
-  // the row maps move as 128-bit loads and stores
+  // the plan kernels move row maps as 128-bit loads and stores
   if (reinterpret_cast<uintptr_t>(ws) & 15)
     return fail(ARLGPU_ERR_INVALID, "workspace must start on a 16-byte boundary");
   char *p = static_cast<char *>(ws);
