@@ -116,19 +116,32 @@ class Clocks:
          'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
          'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, period_ms=50):
         self.idx = gpu_index
         self.f = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
         try:
             self.p = subprocess.Popen(['nvidia-smi', '-i', str(gpu_index), '--query-gpu=' + self.Q,
-                                       '--format=csv,noheader,nounits', '-lms', '200'],
+                                       '--format=csv,noheader,nounits', '-lms', str(period_ms)],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.p = None
+        self._wait_lines(1, 5.0)  # sampling is running before the caller's timed region starts
+
+    def _lines(self):
+        with open(self.f.name) as fh:
+            return sum(1 for line in fh if line.count(',') >= 8)
+
+    def _wait_lines(self, n, seconds):
+        t0 = time.time()
+        while self.p is not None and self.p.poll() is None and time.time() - t0 < seconds:
+            if self._lines() >= n:
+                return
+            time.sleep(0.01)
 
     def stop(self):
         if self.p is None:
             return None
+        self._wait_lines(self._lines() + 1, 1.0)  # one sample after the timed region ends
         self.p.terminate()
         try:
             self.p.wait(timeout=5)
